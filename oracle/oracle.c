@@ -1,0 +1,885 @@
+/*
+ * oracle.c -- CPU oracle for the gc-fg binary-MRF graph-cut path.
+ *
+ * TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
+ * cpu_baseline leg of bench.py as the checker; never by the product library.
+ *
+ * Compile with -ffp-contract=off so that the generators and the double
+ * arithmetic below give bit-identical results on x86-64 and aarch64.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------------ */
+/* Deterministic PRNG + math                                                 */
+/* ------------------------------------------------------------------------ */
+
+/* splitmix64 (Steele, Lea, Flood 2014). */
+uint64_t or_splitmix64(uint64_t *state) {
+    uint64_t z = (*state += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+double or_uniform(uint64_t *state) {
+    return (double)(or_splitmix64(state) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+/* Natural log from the atanh series: log(m) = 2 * sum t^(2k+1)/(2k+1),
+ * t = (m-1)/(m+1), after splitting x = m * 2^e with m in [sqrt(1/2), sqrt 2).
+ * Only +,-,*,/ are used, so the result is identical on every IEEE platform. */
+double or_det_log(double x) {
+    if (!(x > 0.0)) return -INFINITY;
+    int e;
+    double m = frexp(x, &e);            /* exact */
+    if (m < 0.70710678118654752440) { m *= 2.0; e -= 1; }
+    double t = (m - 1.0) / (m + 1.0);
+    double t2 = t * t;
+    double term = t, sum = 0.0;
+    for (int k = 0; k < 14; ++k) {
+        sum += term / (double)(2 * k + 1);
+        term *= t2;
+    }
+    return 2.0 * sum + (double)e * 0.69314718055994530942;
+}
+
+/* Cosine from its Taylor series after reducing to [-pi, pi]. */
+double or_det_cos(double x) {
+    const double two_pi = 6.28318530717958647692;
+    double k = floor(x / two_pi + 0.5);
+    double y = x - k * two_pi;
+    double y2 = y * y;
+    double term = 1.0, sum = 0.0;
+    for (int i = 0; i < 22; ++i) {
+        sum += term;
+        term *= -y2 / (double)((2 * i + 1) * (2 * i + 2));
+    }
+    return sum;
+}
+
+/* Box-Muller, cosine branch only (one uniform pair per normal). */
+double or_normal(uint64_t *state) {
+    double u1 = 1.0 - or_uniform(state); /* (0,1] */
+    double u2 = or_uniform(state);
+    return sqrt(-2.0 * or_det_log(u1)) * or_det_cos(6.28318530717958647692 * u2);
+}
+
+static inline uint8_t quant_u8(double v) {
+    if (v < 0.0) v = 0.0;
+    if (v > 255.0) v = 255.0;
+    return (uint8_t)(int)floor(v + 0.5);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Synthetic images                                                          */
+/* ------------------------------------------------------------------------ */
+
+static const double FG_MEAN[3] = {200.0, 60.0, 60.0};
+static const double BG_MEAN[3] = {60.0, 120.0, 200.0};
+
+void or_gen_defaults(int cfg, int W, int H, uint64_t seed, or_gen_params *p) {
+    memset(p, 0, sizeof(*p));
+    p->W = W;
+    p->H = H;
+    p->seed = seed;
+    p->ax = 80.0;
+    p->ay = 60.0;
+    p->sd_fg = 20.0;
+    p->sd_bg = 25.0;
+    p->stripe_period = 17.0;
+    switch (cfg) {
+    case 1: /* 1920x1080 family: 3 extra ellipses, colour noise sd 30 */
+    case 4: {
+        double s = (double)(W < H ? W : H) / 1080.0;
+        if (s > 1.0) s = 1.0;
+        p->n_extra = 3;
+        p->extra_lo = 40.0 * s;
+        p->extra_hi = 200.0 * s;
+        p->sd_fg = 30.0;
+        p->sd_bg = 30.0;
+        break;
+    }
+    case 2: /* blobs on a striped background */
+        p->family = 1;
+        p->n_blobs = 2000;
+        p->r_lo = 3.0;
+        p->r_hi = 15.0;
+        p->sd_fg = 20.0;
+        p->sd_bg = 40.0;
+        p->stripe_amp = 30.0;
+        break;
+    case 3: /* config-0 generator, ellipse scaled with the image */
+        p->ax = 80.0 * (double)W / 256.0;
+        p->ay = 60.0 * (double)H / 256.0;
+        break;
+    default: /* 0 */
+        break;
+    }
+}
+
+static void scribbles(int W, int H, uint8_t *scrib) {
+    int fx0 = W / 2 - 10, fy0 = H / 2 - 10;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            uint8_t s = 0;
+            if (x < 10 || x >= W - 10 || y < 10 || y >= H - 10) s = 2;
+            if (x >= fx0 && x < fx0 + 20 && y >= fy0 && y < fy0 + 20) s = 1;
+            scrib[(int64_t)y * W + x] = s;
+        }
+}
+
+int or_generate(const or_gen_params *p, uint8_t *rgb, uint8_t *scrib) {
+    const int W = p->W, H = p->H;
+    if (W <= 0 || H <= 0) return -1;
+    uint64_t st = p->seed;
+    const int64_t n = (int64_t)W * H;
+    uint8_t *fg = (uint8_t *)calloc((size_t)n, 1);
+    if (!fg) return -2;
+    const double cx0 = (double)(W / 2), cy0 = (double)(H / 2);
+    if (p->family == 0) {
+        double ex[64][4];
+        int ne = p->n_extra > 64 ? 64 : p->n_extra;
+        for (int k = 0; k < ne; ++k) {
+            ex[k][0] = or_uniform(&st) * W;
+            ex[k][1] = or_uniform(&st) * H;
+            ex[k][2] = p->extra_lo + or_uniform(&st) * (p->extra_hi - p->extra_lo);
+            ex[k][3] = p->extra_lo + or_uniform(&st) * (p->extra_hi - p->extra_lo);
+        }
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                double dx = ((double)x - cx0) / p->ax, dy = ((double)y - cy0) / p->ay;
+                int in = dx * dx + dy * dy <= 1.0;
+                for (int k = 0; k < ne && !in; ++k) {
+                    double ux = ((double)x - ex[k][0]) / ex[k][2];
+                    double uy = ((double)y - ex[k][1]) / ex[k][3];
+                    in = ux * ux + uy * uy <= 1.0;
+                }
+                fg[(int64_t)y * W + x] = (uint8_t)in;
+            }
+    } else {
+        for (int b = 0; b < p->n_blobs; ++b) {
+            double bx, by, r;
+            if (b == 0) {
+                bx = cx0; by = cy0; r = p->r_hi;
+            } else {
+                bx = or_uniform(&st) * W;
+                by = or_uniform(&st) * H;
+                r = p->r_lo + or_uniform(&st) * (p->r_hi - p->r_lo);
+            }
+            int x0 = (int)floor(bx - r), x1 = (int)ceil(bx + r);
+            int y0 = (int)floor(by - r), y1 = (int)ceil(by + r);
+            if (x0 < 0) x0 = 0;
+            if (y0 < 0) y0 = 0;
+            if (x1 > W - 1) x1 = W - 1;
+            if (y1 > H - 1) y1 = H - 1;
+            for (int y = y0; y <= y1; ++y)
+                for (int x = x0; x <= x1; ++x) {
+                    double dx = (double)x - bx, dy = (double)y - by;
+                    if (dx * dx + dy * dy <= r * r) fg[(int64_t)y * W + x] = 1;
+                }
+        }
+    }
+    double *stripe = (double *)calloc((size_t)W, sizeof(double));
+    if (!stripe) { free(fg); return -2; }
+    if (p->stripe_amp != 0.0)
+        for (int x = 0; x < W; ++x)
+            stripe[x] = p->stripe_amp *
+                        or_det_cos(6.28318530717958647692 * (double)x / p->stripe_period -
+                                   1.57079632679489661923);
+    for (int64_t i = 0; i < n; ++i) {
+        int x = (int)(i % W);
+        const double *mean = fg[i] ? FG_MEAN : BG_MEAN;
+        double sd = fg[i] ? p->sd_fg : p->sd_bg;
+        double add = fg[i] ? 0.0 : stripe[x];
+        for (int c = 0; c < 3; ++c) rgb[3 * i + c] = quant_u8(mean[c] + sd * or_normal(&st) + add);
+    }
+    free(stripe);
+    free(fg);
+    if (scrib) scribbles(W, H, scrib);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Data term                                                                 */
+/* ------------------------------------------------------------------------ */
+
+static inline int color_bin(const uint8_t *c) {
+    return ((c[0] >> 4) << 8) | ((c[1] >> 4) << 4) | (c[2] >> 4);
+}
+
+void or_histograms(const uint8_t *rgb, const uint8_t *scrib, int n, int32_t *hf, int32_t *hb) {
+    memset(hf, 0, 4096 * sizeof(int32_t));
+    memset(hb, 0, 4096 * sizeof(int32_t));
+    for (int i = 0; i < n; ++i) {
+        if (scrib[i] == 1) hf[color_bin(rgb + 3 * (int64_t)i)]++;
+        else if (scrib[i] == 2) hb[color_bin(rgb + 3 * (int64_t)i)]++;
+    }
+}
+
+/* dp (source / foreground link) = round(10 * -log p_bg(bin)),
+ * dn (sink / background link)   = round(10 * -log p_fg(bin)),
+ * p_k(bin) = (H_k[bin] + 1) / (N_k + 4096). */
+void or_tlink_lut(const int32_t *hf, const int32_t *hb, double *raw_dp, double *raw_dn,
+                  int32_t *dp_lut, int32_t *dn_lut) {
+    int64_t nf = 0, nb = 0;
+    for (int b = 0; b < 4096; ++b) { nf += hf[b]; nb += hb[b]; }
+    for (int b = 0; b < 4096; ++b) {
+        double pf = (double)(hf[b] + 1) / (double)(nf + 4096);
+        double pb = (double)(hb[b] + 1) / (double)(nb + 4096);
+        double rdn = 10.0 * -log(pf);
+        double rdp = 10.0 * -log(pb);
+        if (raw_dp) raw_dp[b] = rdp;
+        if (raw_dn) raw_dn[b] = rdn;
+        dp_lut[b] = (int32_t)round(rdp);
+        dn_lut[b] = (int32_t)round(rdn);
+    }
+}
+
+void or_tlinks(const uint8_t *rgb, int n, const int32_t *dp_lut, const int32_t *dn_lut,
+               int32_t *dp, int32_t *dn) {
+    for (int i = 0; i < n; ++i) {
+        int b = color_bin(rgb + 3 * (int64_t)i);
+        dp[i] = dp_lut[b];
+        dn[i] = dn_lut[b];
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* N-links                                                                   */
+/* ------------------------------------------------------------------------ */
+
+static inline int diff2(const uint8_t *a, const uint8_t *b) {
+    int d0 = (int)a[0] - b[0], d1 = (int)a[1] - b[1], d2 = (int)a[2] - b[2];
+    return d0 * d0 + d1 * d1 + d2 * d2;
+}
+
+void or_sigma_sum(const uint8_t *rgb, int W, int H, int64_t *sum, int64_t *count) {
+    int64_t s = 0;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const uint8_t *p = rgb + 3 * ((int64_t)y * W + x);
+            if (x + 1 < W) s += diff2(p, p + 3);
+            if (y + 1 < H) s += diff2(p, p + 3 * (int64_t)W);
+        }
+    *sum = s;
+    *count = (int64_t)(W - 1) * H + (int64_t)W * (H - 1);
+}
+
+/* w(d2) = lambda * exp(-d2 / (2 sigma^2)), sigma^2 = sum / count; a constant
+ * image (sum == 0) gives w = lambda. */
+double or_nlink_weight_raw(int d2, double lambda, int64_t sum, int64_t count) {
+    if (sum == 0 || count == 0) return lambda;
+    double s2 = (double)sum / (double)count;
+    double a = -(double)d2 / (2.0 * s2);
+    return lambda * exp(a);
+}
+
+void or_nlinks(const uint8_t *rgb, int W, int H, double lambda, int32_t *up, int32_t *down,
+               int32_t *left, int32_t *right) {
+    int64_t sum, count;
+    or_sigma_sum(rgb, W, H, &sum, &count);
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            int64_t i = (int64_t)y * W + x;
+            const uint8_t *p = rgb + 3 * i;
+            right[i] = x + 1 < W ? (int32_t)round(or_nlink_weight_raw(diff2(p, p + 3), lambda, sum, count)) : 0;
+            left[i] = x > 0 ? (int32_t)round(or_nlink_weight_raw(diff2(p, p - 3), lambda, sum, count)) : 0;
+            down[i] = y + 1 < H ? (int32_t)round(or_nlink_weight_raw(diff2(p, p + 3 * (int64_t)W), lambda, sum, count)) : 0;
+            up[i] = y > 0 ? (int32_t)round(or_nlink_weight_raw(diff2(p, p - 3 * (int64_t)W), lambda, sum, count)) : 0;
+        }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Graph construction in the reference's conventions                        */
+/* ------------------------------------------------------------------------ */
+
+enum { DL = 0, DR = 1, DU = 2, DD = 3 };
+
+/* Follows InitGraph / InitGraphVarEdges (GraphCutKernels.cu:112-214):
+ * only x in [1,W-2], y in [1,H-2] are nodes; their excess is dp - dn; their
+ * caps come from the arrays (or the constant penalty); the cap of every edge
+ * that points into the border ring is zeroed (:143-146, :200-203). */
+void or_build(int W, int H, const int32_t *dp, const int32_t *dn, int penalty,
+              const int32_t *up, const int32_t *down, const int32_t *left,
+              const int32_t *right, int32_t *caps, int32_t *excess) {
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            int64_t i = (int64_t)y * W + x;
+            int32_t *c = caps + 4 * i;
+            int inside = x > 0 && y > 0 && x < W - 1 && y < H - 1;
+            if (!inside) {
+                c[0] = c[1] = c[2] = c[3] = 0;
+                excess[i] = 0;
+                continue;
+            }
+            if (up) {
+                c[DL] = left[i]; c[DR] = right[i]; c[DU] = up[i]; c[DD] = down[i];
+            } else {
+                c[DL] = c[DR] = c[DU] = c[DD] = penalty;
+            }
+            if (x == 1) c[DL] = 0;
+            if (x == W - 2) c[DR] = 0;
+            if (y == 1) c[DU] = 0;
+            if (y == H - 2) c[DD] = 0;
+            excess[i] = dp[i] - dn[i];
+        }
+}
+
+static inline int64_t nbr(int64_t i, int d, int W) {
+    switch (d) {
+    case DL: return i - 1;
+    case DR: return i + 1;
+    case DU: return i - W;
+    default: return i + W;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Push-relabel (sequential restatement of the reference's solver)           */
+/* ------------------------------------------------------------------------ */
+
+/* Global relabel as in InitGlobalRelabel/GlobalRelabel
+ * (GraphCutKernels.cu:757-875): sink-connected nodes (excess < 0) get height
+ * 1, every other node gets its residual BFS distance to them, unreachable
+ * nodes get INF.  Done here as an exact BFS. */
+static void pr_global_relabel(int W, int H, const int32_t *caps, const int32_t *excess,
+                              int32_t *h, int32_t INF, int64_t *queue) {
+    int64_t n = (int64_t)W * H, qh = 0, qt = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        h[i] = INF;
+        if (excess[i] < 0) { h[i] = 1; queue[qt++] = i; }
+    }
+    while (qh < qt) {
+        int64_t v = queue[qh++];
+        int x = (int)(v % W), y = (int)(v / W);
+        for (int d = 0; d < 4; ++d) {
+            if ((d == DL && x == 0) || (d == DR && x == W - 1) || (d == DU && y == 0) || (d == DD && y == H - 1))
+                continue;
+            int64_t u = nbr(v, d, W);
+            /* u -> v is u's edge in direction opposite to d */
+            if (h[u] == INF && caps[4 * u + (d ^ 1)] > 0) {
+                h[u] = h[v] + 1;
+                queue[qt++] = u;
+            }
+        }
+    }
+}
+
+int or_maxflow_pr(int W, int H, int32_t *caps, int32_t *excess, or_stats *st) {
+    int64_t n = (int64_t)W * H;
+    const int32_t INF = (int32_t)(n + 1);
+    int32_t *h = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+    int64_t *queue = (int64_t *)malloc((size_t)(n + 1) * sizeof(int64_t));
+    int64_t *fifo = (int64_t *)malloc((size_t)(n + 1) * sizeof(int64_t));
+    uint8_t *inq = (uint8_t *)calloc((size_t)n, 1);
+    if (!h || !queue || !fifo || !inq) {
+        free(h); free(queue); free(fifo); free(inq);
+        return -2;
+    }
+    or_stats s = {0};
+    int64_t work_since_gr = 0;
+    int64_t fh = 0, fcount = 0, cap_q = n + 1;
+
+#define FIFO_PUSH(v) do { fifo[(fh + fcount) % cap_q] = (v); fcount++; inq[v] = 1; } while (0)
+
+    pr_global_relabel(W, H, caps, excess, h, INF, queue);
+    s.global_relabels++;
+    for (int64_t i = 0; i < n; ++i)
+        if (excess[i] > 0 && h[i] < INF) FIFO_PUSH(i);
+
+    while (fcount > 0) {
+        int64_t u = fifo[fh];
+        fh = (fh + 1) % cap_q;
+        fcount--;
+        inq[u] = 0;
+        int x = (int)(u % W), y = (int)(u / W);
+        while (excess[u] > 0 && h[u] < INF) {
+            int pushed_any = 0;
+            for (int d = 0; d < 4 && excess[u] > 0; ++d) {
+                int32_t r = caps[4 * u + d];
+                if (r <= 0) continue;
+                int64_t v = nbr(u, d, W);
+                if (h[u] != h[v] + 1) continue;
+                int32_t f = excess[u] < r ? excess[u] : r;
+                caps[4 * u + d] -= f;
+                caps[4 * v + (d ^ 1)] += f;
+                excess[u] -= f;
+                int32_t ev = excess[v];
+                excess[v] += f;
+                s.pushes++;
+                pushed_any = 1;
+                if (ev <= 0 && excess[v] > 0 && !inq[v] && h[v] < INF) FIFO_PUSH(v);
+            }
+            if (excess[u] <= 0) break;
+            (void)pushed_any;
+            /* relabel (Relabel kernel, GraphCutKernels.cu:667-689) */
+            int32_t m = INF;
+            for (int d = 0; d < 4; ++d) {
+                if (caps[4 * u + d] <= 0) continue;
+                int64_t v = nbr(u, d, W);
+                if (h[v] < m) m = h[v];
+            }
+            h[u] = m >= INF - 1 ? INF : m + 1;
+            s.relabels++;
+            work_since_gr += 12;
+            (void)x; (void)y;
+        }
+        if (work_since_gr > 6 * n + 64 && fcount > 0) {
+            pr_global_relabel(W, H, caps, excess, h, INF, queue);
+            s.global_relabels++;
+            work_since_gr = 0;
+            fh = 0;
+            fcount = 0;
+            memset(inq, 0, (size_t)n);
+            for (int64_t i = 0; i < n; ++i)
+                if (excess[i] > 0 && h[i] < INF) FIFO_PUSH(i);
+        }
+    }
+#undef FIFO_PUSH
+    /* Exactness check: no positive excess may still reach the sink. */
+    pr_global_relabel(W, H, caps, excess, h, INF, queue);
+    int ok = 1;
+    for (int64_t i = 0; i < n; ++i)
+        if (excess[i] > 0 && h[i] < INF) { ok = 0; break; }
+    free(h); free(queue); free(fifo); free(inq);
+    if (st) *st = s;
+    return ok ? 0 : -3;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Boykov-Kolmogorov augmenting paths (written from Boykov & Kolmogorov,     */
+/* "An Experimental Comparison of Min-Cut/Max-Flow Algorithms for Energy     */
+/* Minimization in Vision", PAMI 2004).                                      */
+/* ------------------------------------------------------------------------ */
+
+enum { P_NONE = -1, P_TERM = 4, P_ORPHAN = 5 };
+enum { T_FREE = 0, T_S = 1, T_T = 2 };
+
+typedef struct {
+    int W, H;
+    int64_t n;
+    int32_t *caps, *tr;
+    int8_t *tree, *par;
+    int32_t *ts, *dist;
+    int64_t *active; /* ring buffer */
+    uint8_t *inact;
+    int64_t ah, acount;
+    int64_t *orph; /* FIFO of orphans */
+    int64_t oh, ocount;
+    int32_t time;
+} bk_t;
+
+static inline int bk_has_nbr(const bk_t *b, int64_t i, int d) {
+    int x = (int)(i % b->W), y = (int)(i / b->W);
+    return !((d == DL && x == 0) || (d == DR && x == b->W - 1) || (d == DU && y == 0) || (d == DD && y == b->H - 1));
+}
+
+static inline void bk_activate(bk_t *b, int64_t i) {
+    if (b->inact[i]) return;
+    b->inact[i] = 1;
+    b->active[(b->ah + b->acount) % b->n] = i;
+    b->acount++;
+}
+
+static inline void bk_orphan(bk_t *b, int64_t i) {
+    b->par[i] = P_ORPHAN;
+    b->orph[(b->oh + b->ocount) % b->n] = i;
+    b->ocount++;
+}
+
+static void bk_augment(bk_t *b, int64_t a, int64_t t, int dab, int64_t *flow) {
+    int32_t *caps = b->caps;
+    int32_t delta = caps[4 * a + dab];
+    int64_t x = a;
+    while (b->par[x] != P_TERM) {
+        int pd = b->par[x];
+        int64_t y = nbr(x, pd, b->W);
+        int32_t c = caps[4 * y + (pd ^ 1)];
+        if (c < delta) delta = c;
+        x = y;
+    }
+    if (b->tr[x] < delta) delta = b->tr[x];
+    x = t;
+    while (b->par[x] != P_TERM) {
+        int pd = b->par[x];
+        int32_t c = caps[4 * x + pd];
+        if (c < delta) delta = c;
+        x = nbr(x, pd, b->W);
+    }
+    if (-b->tr[x] < delta) delta = -b->tr[x];
+
+    caps[4 * a + dab] -= delta;
+    caps[4 * t + (dab ^ 1)] += delta;
+    x = a;
+    while (b->par[x] != P_TERM) {
+        int pd = b->par[x];
+        int64_t y = nbr(x, pd, b->W);
+        caps[4 * y + (pd ^ 1)] -= delta;
+        caps[4 * x + pd] += delta;
+        if (caps[4 * y + (pd ^ 1)] == 0) bk_orphan(b, x);
+        x = y;
+    }
+    b->tr[x] -= delta;
+    if (b->tr[x] == 0) bk_orphan(b, x);
+    x = t;
+    while (b->par[x] != P_TERM) {
+        int pd = b->par[x];
+        int64_t y = nbr(x, pd, b->W);
+        caps[4 * x + pd] -= delta;
+        caps[4 * y + (pd ^ 1)] += delta;
+        if (caps[4 * x + pd] == 0) bk_orphan(b, x);
+        x = y;
+    }
+    b->tr[x] += delta;
+    if (b->tr[x] == 0) bk_orphan(b, x);
+    *flow += delta;
+}
+
+/* Distance of a tree node to its terminal, or -1 if its chain hits an
+ * orphan; marks the chain with the current timestamp. */
+static int32_t bk_origin_dist(bk_t *b, int64_t q) {
+    int32_t d = 0;
+    int64_t j = q;
+    for (;;) {
+        if (b->ts[j] == b->time) { d += b->dist[j]; break; }
+        d++;
+        if (b->par[j] == P_TERM) {
+            b->ts[j] = b->time;
+            b->dist[j] = 1;
+            break;
+        }
+        if (b->par[j] == P_ORPHAN || b->par[j] == P_NONE) return -1;
+        j = nbr(j, b->par[j], b->W);
+    }
+    int32_t dd = d;
+    for (j = q; b->ts[j] != b->time; j = nbr(j, b->par[j], b->W)) {
+        b->ts[j] = b->time;
+        b->dist[j] = dd--;
+    }
+    return d;
+}
+
+static void bk_adopt(bk_t *b, int64_t p) {
+    int tree = b->tree[p];
+    int best = -1;
+    int32_t best_d = 0x7fffffff;
+    for (int d = 0; d < 4; ++d) {
+        if (!bk_has_nbr(b, p, d)) continue;
+        int64_t q = nbr(p, d, b->W);
+        if (b->tree[q] != tree) continue;
+        int32_t c = tree == T_S ? b->caps[4 * q + (d ^ 1)] : b->caps[4 * p + d];
+        if (c <= 0) continue;
+        int32_t od = bk_origin_dist(b, q);
+        if (od >= 0 && od < best_d) { best_d = od; best = d; }
+    }
+    if (best >= 0) {
+        b->par[p] = (int8_t)best;
+        b->ts[p] = b->time;
+        b->dist[p] = best_d + 1;
+        return;
+    }
+    /* no parent: p becomes free; its tree neighbours may reclaim it */
+    for (int d = 0; d < 4; ++d) {
+        if (!bk_has_nbr(b, p, d)) continue;
+        int64_t q = nbr(p, d, b->W);
+        if (b->tree[q] != tree) continue;
+        int32_t c = tree == T_S ? b->caps[4 * q + (d ^ 1)] : b->caps[4 * p + d];
+        if (c > 0) bk_activate(b, q);
+        if (b->par[q] >= 0 && b->par[q] < 4 && nbr(q, b->par[q], b->W) == p) bk_orphan(b, q);
+    }
+    b->tree[p] = T_FREE;
+    b->par[p] = P_NONE;
+}
+
+int or_maxflow_bk(int W, int H, int32_t *caps, int32_t *excess, or_stats *st) {
+    bk_t b;
+    memset(&b, 0, sizeof(b));
+    b.W = W;
+    b.H = H;
+    b.n = (int64_t)W * H;
+    b.caps = caps;
+    b.tr = excess;
+    b.tree = (int8_t *)calloc((size_t)b.n, 1);
+    b.par = (int8_t *)malloc((size_t)b.n);
+    b.ts = (int32_t *)calloc((size_t)b.n, sizeof(int32_t));
+    b.dist = (int32_t *)calloc((size_t)b.n, sizeof(int32_t));
+    b.active = (int64_t *)malloc((size_t)b.n * sizeof(int64_t));
+    b.inact = (uint8_t *)calloc((size_t)b.n, 1);
+    b.orph = (int64_t *)malloc((size_t)b.n * sizeof(int64_t));
+    if (!b.tree || !b.par || !b.ts || !b.dist || !b.active || !b.inact || !b.orph) {
+        free(b.tree); free(b.par); free(b.ts); free(b.dist); free(b.active); free(b.inact); free(b.orph);
+        return -2;
+    }
+    memset(b.par, P_NONE, (size_t)b.n);
+    or_stats s = {0};
+    int64_t flow = 0;
+    for (int64_t i = 0; i < b.n; ++i) {
+        if (excess[i] > 0) { b.tree[i] = T_S; b.par[i] = P_TERM; b.dist[i] = 1; bk_activate(&b, i); }
+        else if (excess[i] < 0) { b.tree[i] = T_T; b.par[i] = P_TERM; b.dist[i] = 1; bk_activate(&b, i); }
+    }
+    b.time = 0;
+    int64_t cur = -1;
+    for (;;) {
+        if (cur < 0) {
+            while (b.acount > 0) {
+                int64_t i = b.active[b.ah];
+                b.ah = (b.ah + 1) % b.n;
+                b.acount--;
+                b.inact[i] = 0;
+                if (b.tree[i] != T_FREE) { cur = i; break; }
+            }
+            if (cur < 0) break;
+        }
+        int64_t p = cur;
+        int64_t ea = -1, et = -1;
+        int edir = -1;
+        for (int d = 0; d < 4; ++d) {
+            if (!bk_has_nbr(&b, p, d)) continue;
+            int64_t q = nbr(p, d, W);
+            if (b.tree[p] == T_S) {
+                if (caps[4 * p + d] <= 0) continue;
+                if (b.tree[q] == T_FREE) {
+                    b.tree[q] = T_S; b.par[q] = (int8_t)(d ^ 1);
+                    b.ts[q] = b.ts[p]; b.dist[q] = b.dist[p] + 1;
+                    bk_activate(&b, q);
+                } else if (b.tree[q] == T_T) {
+                    ea = p; et = q; edir = d;
+                    break;
+                } else if (b.ts[q] <= b.ts[p] && b.dist[q] > b.dist[p]) {
+                    b.par[q] = (int8_t)(d ^ 1);
+                    b.ts[q] = b.ts[p]; b.dist[q] = b.dist[p] + 1;
+                }
+            } else {
+                if (caps[4 * q + (d ^ 1)] <= 0) continue;
+                if (b.tree[q] == T_FREE) {
+                    b.tree[q] = T_T; b.par[q] = (int8_t)(d ^ 1);
+                    b.ts[q] = b.ts[p]; b.dist[q] = b.dist[p] + 1;
+                    bk_activate(&b, q);
+                } else if (b.tree[q] == T_S) {
+                    ea = q; et = p; edir = d ^ 1;
+                    break;
+                } else if (b.ts[q] <= b.ts[p] && b.dist[q] > b.dist[p]) {
+                    b.par[q] = (int8_t)(d ^ 1);
+                    b.ts[q] = b.ts[p]; b.dist[q] = b.dist[p] + 1;
+                }
+            }
+        }
+        b.time++;
+        if (edir >= 0) {
+            bk_augment(&b, ea, et, edir, &flow);
+            s.augments++;
+            while (b.ocount > 0) {
+                int64_t o = b.orph[b.oh];
+                b.oh = (b.oh + 1) % b.n;
+                b.ocount--;
+                if (b.par[o] == P_ORPHAN) bk_adopt(&b, o);
+            }
+            if (b.tree[p] == T_FREE) cur = -1;
+        } else {
+            cur = -1;
+        }
+    }
+    free(b.tree); free(b.par); free(b.ts); free(b.dist); free(b.active); free(b.inact); free(b.orph);
+    if (st) *st = s;
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Cuts                                                                      */
+/* ------------------------------------------------------------------------ */
+
+/* smax: complement of the sink-reachable set (InitLabels + SpreadLabels,
+ * GraphCutKernels.cu:228-351, with SPREAD_ZEROS, GraphCut.h:37);
+ * smin: nodes reachable from positive-excess nodes along residual edges. */
+void or_cuts(int W, int H, const int32_t *caps, const int32_t *excess, uint8_t *smin, uint8_t *smax) {
+    int64_t n = (int64_t)W * H;
+    int64_t *queue = (int64_t *)malloc((size_t)(n + 1) * sizeof(int64_t));
+    uint8_t *mark = (uint8_t *)calloc((size_t)n, 1);
+    int64_t qh = 0, qt = 0;
+    for (int64_t i = 0; i < n; ++i)
+        if (excess[i] < 0) { mark[i] = 1; queue[qt++] = i; }
+    while (qh < qt) {
+        int64_t v = queue[qh++];
+        int x = (int)(v % W), y = (int)(v / W);
+        for (int d = 0; d < 4; ++d) {
+            if ((d == DL && x == 0) || (d == DR && x == W - 1) || (d == DU && y == 0) || (d == DD && y == H - 1))
+                continue;
+            int64_t u = nbr(v, d, W);
+            if (!mark[u] && caps[4 * u + (d ^ 1)] > 0) { mark[u] = 1; queue[qt++] = u; }
+        }
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        int x = (int)(i % W), y = (int)(i / W);
+        int inside = x > 0 && y > 0 && x < W - 1 && y < H - 1;
+        smax[i] = (uint8_t)(inside && !mark[i]);
+    }
+    memset(mark, 0, (size_t)n);
+    qh = qt = 0;
+    for (int64_t i = 0; i < n; ++i)
+        if (excess[i] > 0) { mark[i] = 1; queue[qt++] = i; }
+    while (qh < qt) {
+        int64_t u = queue[qh++];
+        int x = (int)(u % W), y = (int)(u / W);
+        for (int d = 0; d < 4; ++d) {
+            if ((d == DL && x == 0) || (d == DR && x == W - 1) || (d == DU && y == 0) || (d == DD && y == H - 1))
+                continue;
+            int64_t v = nbr(u, d, W);
+            if (!mark[v] && caps[4 * u + d] > 0) { mark[v] = 1; queue[qt++] = v; }
+        }
+    }
+    for (int64_t i = 0; i < n; ++i) smin[i] = mark[i];
+    free(queue);
+    free(mark);
+}
+
+int64_t or_cut_energy(int W, int H, const int32_t *dp, const int32_t *dn, int penalty,
+                      const int32_t *up, const int32_t *down, const int32_t *left,
+                      const int32_t *right, const uint8_t *label) {
+    int64_t n = (int64_t)W * H;
+    int32_t *caps = (int32_t *)malloc((size_t)(4 * n) * sizeof(int32_t));
+    int32_t *ex = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+    or_build(W, H, dp, dn, penalty, up, down, left, right, caps, ex);
+    int64_t e = 0;
+    for (int y = 1; y < H - 1; ++y)
+        for (int x = 1; x < W - 1; ++x) {
+            int64_t i = (int64_t)y * W + x;
+            if (label[i]) {
+                e += dn[i];
+                for (int d = 0; d < 4; ++d) {
+                    int64_t j = nbr(i, d, W);
+                    if (!label[j]) e += caps[4 * i + d];
+                }
+            } else {
+                e += dp[i];
+            }
+        }
+    free(caps);
+    free(ex);
+    return e;
+}
+
+int64_t or_interior_dp(int W, int H, const int32_t *dp) {
+    int64_t s = 0;
+    for (int y = 1; y < H - 1; ++y)
+        for (int x = 1; x < W - 1; ++x) s += dp[(int64_t)y * W + x];
+    return s;
+}
+
+int32_t or_reference_energy(int W, int H, const int32_t *dp, const int32_t *excess_final) {
+    int wex = 32 * ((W + 31) / 32);
+    int64_t size = (int64_t)W * H;
+    uint32_t init = 0, fin = 0;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            int64_t t = (int64_t)x + (int64_t)y * wex; /* padded position */
+            int32_t v = dp[(int64_t)y * W + x];
+            if (t < size && v > 0) init += (uint32_t)v;
+        }
+    for (int64_t i = 0; i < size; ++i)
+        if (excess_final[i] > 0) fin += (uint32_t)excess_final[i];
+    return (int32_t)(init - fin);
+}
+
+int or_solve(int W, int H, const int32_t *dp, const int32_t *dn, int penalty,
+             const int32_t *up, const int32_t *down, const int32_t *left,
+             const int32_t *right, int solver, uint8_t *smin, uint8_t *smax,
+             int64_t *flow, int32_t *excess_out, or_stats *st) {
+    int64_t n = (int64_t)W * H;
+    int32_t *caps = (int32_t *)malloc((size_t)(4 * n) * sizeof(int32_t));
+    int32_t *ex = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+    if (!caps || !ex) { free(caps); free(ex); return -2; }
+    or_build(W, H, dp, dn, penalty, up, down, left, right, caps, ex);
+    or_stats s;
+    int rc = solver == 1 ? or_maxflow_bk(W, H, caps, ex, &s) : or_maxflow_pr(W, H, caps, ex, &s);
+    if (rc == 0) {
+        int64_t pos = 0;
+        for (int64_t i = 0; i < n; ++i) if (ex[i] > 0) pos += ex[i];
+        s.flow = or_interior_dp(W, H, dp) - pos;
+        if (flow) *flow = s.flow;
+        if (smin && smax) or_cuts(W, H, caps, ex, smin, smax);
+        if (excess_out) memcpy(excess_out, ex, (size_t)n * sizeof(int32_t));
+        if (st) *st = s;
+    }
+    free(caps);
+    free(ex);
+    return rc;
+}
+
+int or_segment(const uint8_t *rgb, const uint8_t *scrib, int W, int H, double lambda, int solver,
+               int32_t *dp, int32_t *dn, int32_t *up, int32_t *down, int32_t *left, int32_t *right,
+               uint8_t *smin, uint8_t *smax, int64_t *flow) {
+    int32_t hf[4096], hb[4096], dpl[4096], dnl[4096];
+    int n = W * H;
+    or_histograms(rgb, scrib, n, hf, hb);
+    or_tlink_lut(hf, hb, NULL, NULL, dpl, dnl);
+    or_tlinks(rgb, n, dpl, dnl, dp, dn);
+    or_nlinks(rgb, W, H, lambda, up, down, left, right);
+    return or_solve(W, H, dp, dn, 0, up, down, left, right, solver, smin, smax, flow, NULL, NULL);
+}
+
+/* ---- batch over host threads ---- */
+typedef struct {
+    int n_img;
+    const int *Ws, *Hs;
+    const int64_t *offs;
+    const uint8_t *rgb, *scrib;
+    const double *lambdas;
+    int solver;
+    uint8_t *smin, *smax;
+    int64_t *flows;
+    int next;
+    int err;
+    pthread_mutex_t mu;
+} batch_ctx;
+
+static void *batch_worker(void *arg) {
+    batch_ctx *c = (batch_ctx *)arg;
+    for (;;) {
+        pthread_mutex_lock(&c->mu);
+        int k = c->next++;
+        pthread_mutex_unlock(&c->mu);
+        if (k >= c->n_img) break;
+        int W = c->Ws[k], H = c->Hs[k];
+        int64_t off = c->offs[k], n = (int64_t)W * H;
+        int32_t *buf = (int32_t *)malloc((size_t)(6 * n) * sizeof(int32_t));
+        if (!buf) { c->err = -2; continue; }
+        int rc = or_segment(c->rgb + 3 * off, c->scrib + off, W, H, c->lambdas[k], c->solver,
+                            buf, buf + n, buf + 2 * n, buf + 3 * n, buf + 4 * n, buf + 5 * n,
+                            c->smin + off, c->smax + off, c->flows + k);
+        if (rc) c->err = rc;
+        free(buf);
+    }
+    return NULL;
+}
+
+int or_segment_batch(int n_img, const int *Ws, const int *Hs, const int64_t *offs,
+                     const uint8_t *rgb, const uint8_t *scrib, const double *lambdas,
+                     int solver, int nthreads, uint8_t *smin, uint8_t *smax, int64_t *flows) {
+    batch_ctx c;
+    memset(&c, 0, sizeof(c));
+    c.n_img = n_img; c.Ws = Ws; c.Hs = Hs; c.offs = offs; c.rgb = rgb; c.scrib = scrib;
+    c.lambdas = lambdas; c.solver = solver; c.smin = smin; c.smax = smax; c.flows = flows;
+    pthread_mutex_init(&c.mu, NULL);
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    pthread_t th[256];
+    for (int t = 0; t < nthreads; ++t) pthread_create(&th[t], NULL, batch_worker, &c);
+    for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+    pthread_mutex_destroy(&c.mu);
+    return c.err;
+}
+
+uint64_t or_fnv1a(const void *data, int64_t n) {
+    const uint8_t *p = (const uint8_t *)data;
+    uint64_t h = 1469598103934665603ULL;
+    for (int64_t i = 0; i < n; ++i) {
+        h ^= p[i];
+        h *= 1099511628211ULL;
+    }
+    return h;
+}

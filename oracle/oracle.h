@@ -1,0 +1,141 @@
+/*
+ * oracle.h -- CPU oracle for the gc-fg binary-MRF graph-cut path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links, loads or
+ * calls this code; only the test suite, the smoke check and the CPU-baseline
+ * leg of bench.py use it, and only as the checker.
+ *
+ * It restates, in plain C:
+ *   - the deterministic synthetic inputs (images + scribbles);
+ *   - the colour-histogram data term and the contrast-sensitive n-links;
+ *   - the reference's graph construction conventions
+ *     (GraphCutKernels.cu:112-214: interior-only nodes, edges into the 1-pixel
+ *     border zeroed, reduced t-link excess = dp - dn);
+ *   - two exact max-flow solvers: a sequential push-relabel that follows the
+ *     reference's algorithm (GraphCut.cu:385-534, GraphCutKernels.cu:600-875)
+ *     and a Boykov-Kolmogorov augmenting-path solver (the CPU solver the
+ *     reference's published comparison used), written from the 2004 paper;
+ *   - cut extraction: S_max (the reference's SpreadLabels output,
+ *     GraphCutKernels.cu:228-351) and S_min (source-reachable set).
+ *
+ * Parity of this oracle is pinned by running the reference's own CUDA
+ * solver under a CPU thread emulator (oracle/refemu) on the same inputs.
+ */
+#ifndef GCFG_ORACLE_H
+#define GCFG_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- deterministic PRNG and math (bit-identical on x86-64 and aarch64) ---- */
+uint64_t or_splitmix64(uint64_t *state);
+double or_uniform(uint64_t *state);              /* [0,1), 53-bit */
+double or_normal(uint64_t *state);               /* Box-Muller, own log/cos */
+double or_det_log(double x);
+double or_det_cos(double x);
+
+/* ---- synthetic image families ----
+ * family 0: "ellipse" (central ellipse + n_extra random ellipses)
+ * family 1: "blobs"   (n_blobs discs on a striped, noisy background)
+ * rgb: 3*W*H bytes interleaved, scrib: W*H bytes (0 none, 1 fg, 2 bg). */
+typedef struct {
+    int family;
+    int W, H;
+    uint64_t seed;
+    double ax, ay;           /* central ellipse semi-axes (family 0) */
+    int n_extra;             /* random ellipses (family 0) */
+    double extra_lo, extra_hi;
+    int n_blobs;             /* family 1 */
+    double r_lo, r_hi;       /* blob radii (family 1) */
+    double sd_fg, sd_bg;     /* colour noise per channel */
+    double stripe_amp;       /* family 1: background stripe amplitude */
+    double stripe_period;    /* family 1: stripe period in pixels */
+} or_gen_params;
+
+void or_gen_defaults(int cfg, int W, int H, uint64_t seed, or_gen_params *p);
+int or_generate(const or_gen_params *p, uint8_t *rgb, uint8_t *scrib);
+
+/* ---- data term: 16^3 histograms, +1 Laplace smoothing, round(10*-log p) ---- */
+void or_histograms(const uint8_t *rgb, const uint8_t *scrib, int n,
+                   int32_t *hist_fg, int32_t *hist_bg);
+void or_tlink_lut(const int32_t *hist_fg, const int32_t *hist_bg,
+                  double *raw_dp, double *raw_dn,
+                  int32_t *dp_lut, int32_t *dn_lut);
+void or_tlinks(const uint8_t *rgb, int n, const int32_t *dp_lut,
+               const int32_t *dn_lut, int32_t *dp, int32_t *dn);
+
+/* ---- n-links: sigma^2 = mean ||dI||^2 over all 4-neighbour pairs ---- */
+void or_sigma_sum(const uint8_t *rgb, int W, int H, int64_t *sum, int64_t *count);
+double or_nlink_weight_raw(int d2, double lambda, int64_t sum, int64_t count);
+void or_nlinks(const uint8_t *rgb, int W, int H, double lambda,
+               int32_t *up, int32_t *down, int32_t *left, int32_t *right);
+
+/* ---- graph in the reference's conventions ----
+ * caps: 4*W*H ints, per pixel {left, right, up, down} residual capacity.
+ * excess: W*H ints, dp - dn on interior pixels, 0 elsewhere.
+ * up/down/left/right may be NULL, in which case `penalty` is used
+ * (GraphCutKernels.cu:112-157 vs 165-214). */
+void or_build(int W, int H, const int32_t *dp, const int32_t *dn, int penalty,
+              const int32_t *up, const int32_t *down, const int32_t *left,
+              const int32_t *right, int32_t *caps, int32_t *excess);
+
+/* ---- solvers: operate in place on caps/excess from or_build ---- */
+typedef struct {
+    int64_t flow;          /* exact max-flow value (int64) */
+    int64_t pushes, relabels, global_relabels, augments;
+} or_stats;
+
+int or_maxflow_pr(int W, int H, int32_t *caps, int32_t *excess, or_stats *st);
+int or_maxflow_bk(int W, int H, int32_t *caps, int32_t *excess, or_stats *st);
+
+/* ---- cut extraction from a final residual graph ----
+ * smax[i] = 1 iff interior and cannot reach the sink (reference labels);
+ * smin[i] = 1 iff reachable from the source (from positive-excess nodes). */
+void or_cuts(int W, int H, const int32_t *caps, const int32_t *excess,
+             uint8_t *smin, uint8_t *smax);
+
+/* Energy of a labelling under the original capacities (interior only). */
+int64_t or_cut_energy(int W, int H, const int32_t *dp, const int32_t *dn,
+                      int penalty, const int32_t *up, const int32_t *down,
+                      const int32_t *left, const int32_t *right,
+                      const uint8_t *label);
+
+/* Sum over interior of dp (int64). */
+int64_t or_interior_dp(int W, int H, const int32_t *dp);
+
+/* The number the reference prints as "Final energy level", reproduced with
+ * its int32 arithmetic and its padded-layout reduction (GraphCut.cu:359-376,
+ * 399-401, 456-457; GraphCutKernels.cu:883-898). */
+int32_t or_reference_energy(int W, int H, const int32_t *dp, const int32_t *excess_final);
+
+/* One-call solve: build + solve + cuts. solver 0 = push-relabel, 1 = BK.
+ * Returns 0 on success. */
+int or_solve(int W, int H, const int32_t *dp, const int32_t *dn, int penalty,
+             const int32_t *up, const int32_t *down, const int32_t *left,
+             const int32_t *right, int solver, uint8_t *smin, uint8_t *smax,
+             int64_t *flow, int32_t *excess_out, or_stats *st);
+
+/* Full segmentation pipeline on one image: data term, n-links, solve. */
+int or_segment(const uint8_t *rgb, const uint8_t *scrib, int W, int H,
+               double lambda, int solver, int32_t *dp, int32_t *dn,
+               int32_t *up, int32_t *down, int32_t *left, int32_t *right,
+               uint8_t *smin, uint8_t *smax, int64_t *flow);
+
+/* Batch of independent solves over `nthreads` host threads (one image per
+ * task), for the CPU baseline. Arrays are concatenated; offs[i] is the pixel
+ * offset of image i.  Returns 0 on success. */
+int or_segment_batch(int n_img, const int *Ws, const int *Hs, const int64_t *offs,
+                     const uint8_t *rgb, const uint8_t *scrib, const double *lambdas,
+                     int solver, int nthreads, uint8_t *smin, uint8_t *smax,
+                     int64_t *flows);
+
+/* FNV-1a 64-bit hash of a byte buffer (fixture checks). */
+uint64_t or_fnv1a(const void *data, int64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
