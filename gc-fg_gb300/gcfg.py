@@ -1,0 +1,268 @@
+"""Python mirror of the reference's graph-cut interface over libgcfg.so.
+
+The reference exposes C++ free functions (GraphCut.cu:187-568) and a
+DataTerm namespace (DataTerm.h:9-19).  This module binds the C ABI of the
+CUDA library (include/gcfg.h) with ctypes and offers the same operations
+with the same names and argument meanings (GC_Init, GC_SetDataterms,
+GC_SetEdges, GC_SetPenalty, GC_SetGraph, GC_Optimize, GC_End), taking CUDA
+device buffers as torch tensors.  There is no CPU path: if libgcfg.so is
+missing or no GPU is present, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgcfg.so")
+
+GCFG_OK = 0
+GCFG_ERR_INVALID = 1
+GCFG_ERR_OOM = 2
+GCFG_ERR_CUDA = 3
+GCFG_ERR_NOT_CONVERGED = 4
+GCFG_ERR_STATE = 5
+GCFG_ERR_CAPACITY = 6
+GCFG_MAX_CAP = (1 << 28) - 1
+
+# Every function declared in include/gcfg.h (checked by the CPU test suite).
+EXPORTS = [
+    "gcfg_init", "gcfg_set_dataterms", "gcfg_set_edges", "gcfg_set_penalty", "gcfg_set_graph",
+    "gcfg_optimize", "gcfg_get_cuts", "gcfg_end", "gcfg_set_stream", "gcfg_set_schedule",
+    "gcfg_tlinks", "gcfg_nlinks", "gcfg_seg_create", "gcfg_seg_run", "gcfg_seg_run_host",
+    "gcfg_seg_set_stream", "gcfg_seg_destroy", "gcfg_strerror", "gcfg_launch_count",
+]
+
+
+class GcfgError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        self.status = status
+        super().__init__(f"{what}: {strerror(status)} ({status})")
+
+
+class Result(C.Structure):
+    _fields_ = [("flow", C.c_int64), ("ref_energy", C.c_int32), ("status", C.c_int32),
+                ("global_relabels", C.c_int32), ("gr_sweeps", C.c_int32),
+                ("push_rounds", C.c_int32), ("cut_sweeps", C.c_int32),
+                ("active_after_first_gr", C.c_int64), ("ms", C.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libgcfg.so.  Raises if it is missing: there is no fallback."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libgcfg.so not built ({path}); run __graft_entry__.build()")
+    lib = C.CDLL(path)
+    P = C.c_void_p
+    I = C.c_int
+    S = C.c_int  # gcfg_status
+    sig = {
+        "gcfg_init": (S, [I, I, P, P, C.c_int32, P, P, P, P, C.POINTER(P)]),
+        "gcfg_set_dataterms": (S, [P, P, P]),
+        "gcfg_set_edges": (S, [P, P, P, P, P]),
+        "gcfg_set_penalty": (S, [P, C.c_int32]),
+        "gcfg_set_graph": (S, [P]),
+        "gcfg_optimize": (S, [P, P, C.POINTER(Result)]),
+        "gcfg_get_cuts": (S, [P, P, P]),
+        "gcfg_end": (S, [P]),
+        "gcfg_set_stream": (S, [P, P]),
+        "gcfg_set_schedule": (S, [P, I, I]),
+        "gcfg_tlinks": (S, [P, P, I, P, P, P, P, P]),
+        "gcfg_nlinks": (S, [P, I, I, C.c_double, P, P, P, P, P]),
+        "gcfg_seg_create": (S, [I, I, C.POINTER(P)]),
+        "gcfg_seg_run": (S, [P, P, P, I, I, C.c_double, P, P, C.POINTER(Result)]),
+        "gcfg_seg_run_host": (S, [P, P, P, I, I, C.c_double, P, P, C.POINTER(Result)]),
+        "gcfg_seg_set_stream": (S, [P, P]),
+        "gcfg_seg_destroy": (S, [P]),
+        "gcfg_strerror": (C.c_char_p, [I]),
+        "gcfg_launch_count": (C.c_int64, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def strerror(status: int) -> str:
+    try:
+        return load().gcfg_strerror(status).decode()
+    except Exception:  # library not loadable: still give a message
+        return f"status {status}"
+
+
+def _check(rc: int, what: str):
+    if rc != GCFG_OK:
+        raise GcfgError(rc, what)
+
+
+def _ptr(t):
+    """Device (or host) address of a torch tensor / numpy array, or None."""
+    if t is None:
+        return None
+    if hasattr(t, "data_ptr"):
+        return C.c_void_p(t.data_ptr())
+    return t.ctypes.data_as(C.c_void_p)
+
+
+def launch_count() -> int:
+    return load().gcfg_launch_count()
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    return C.c_void_p(getattr(stream, "cuda_stream", stream))
+
+
+# ---------------------------------------------------------------------------
+# Graph API: GC_* names, argument meaning and order as in GraphCut.cu
+# ---------------------------------------------------------------------------
+
+class GlobalWrapper:
+    """Handle of one residual graph (GraphCut.h:110-128's GlobalWrapper)."""
+
+    def __init__(self, handle, width, height):
+        self.handle = handle
+        self.width = width
+        self.height = height
+        # keep caller tensors alive while the graph refers to them
+        self._refs = []
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            try:
+                load().gcfg_end(self.handle)
+            except Exception:
+                pass
+            self.handle = None
+
+
+def GC_Init(width, height, data_positive=None, data_negative=None, penalty=0, up=None, down=None,
+            left=None, right=None) -> GlobalWrapper:
+    """GC_Init (GraphCut.cu:187): device int32 [H, W] tensors, caller-owned."""
+    h = C.c_void_p()
+    rc = load().gcfg_init(int(width), int(height), _ptr(data_positive), _ptr(data_negative),
+                          int(penalty), _ptr(up), _ptr(down), _ptr(left), _ptr(right), C.byref(h))
+    _check(rc, "GC_Init")
+    gw = GlobalWrapper(h, width, height)
+    gw._refs = [data_positive, data_negative, up, down, left, right]
+    return gw
+
+
+def GC_SetDataterms(gw, data_positive, data_negative):
+    _check(load().gcfg_set_dataterms(gw.handle, _ptr(data_positive), _ptr(data_negative)),
+           "GC_SetDataterms")
+    gw._refs[:2] = [data_positive, data_negative]
+
+
+def GC_SetEdges(gw, up, down, left, right):
+    _check(load().gcfg_set_edges(gw.handle, _ptr(up), _ptr(down), _ptr(left), _ptr(right)),
+           "GC_SetEdges")
+    gw._refs[2:] = [up, down, left, right]
+
+
+def GC_SetPenalty(gw, p):
+    _check(load().gcfg_set_penalty(gw.handle, int(p)), "GC_SetPenalty")
+
+
+def GC_SetGraph(gw):
+    _check(load().gcfg_set_graph(gw.handle), "GC_SetGraph")
+
+
+def GC_SetStream(gw, stream):
+    _check(load().gcfg_set_stream(gw.handle, _stream_ptr(stream)), "GC_SetStream")
+
+
+def GC_SetSchedule(gw, push_rounds_per_gr, max_tile_sweeps):
+    _check(load().gcfg_set_schedule(gw.handle, int(push_rounds_per_gr), int(max_tile_sweeps)),
+           "GC_SetSchedule")
+
+
+def GC_Optimize(gw, label=None) -> dict:
+    """GC_Optimize (GraphCut.cu:385): label is an optional host int32 numpy
+    array [H, W] that receives the reference-style labels.  Returns the
+    result record (exact flow value, reference-printed energy, counters)."""
+    res = Result()
+    rc = load().gcfg_optimize(gw.handle, _ptr(label), C.byref(res))
+    _check(rc, "GC_Optimize")
+    return res.as_dict()
+
+
+def GC_GetCuts(gw, smin=None, smax=None):
+    """Both canonical cuts into device uint8 [H, W] tensors."""
+    _check(load().gcfg_get_cuts(gw.handle, _ptr(smin), _ptr(smax)), "GC_GetCuts")
+
+
+def GC_End(gw):
+    if gw.handle:
+        _check(load().gcfg_end(gw.handle), "GC_End")
+        gw.handle = None
+
+
+# ---------------------------------------------------------------------------
+# Data term and n-links
+# ---------------------------------------------------------------------------
+
+def tlinks(d_rgb, d_scrib, d_dp, d_dn, raw=False, stream=None):
+    """Histogram t-links into device int32 tensors.  With raw=True returns the
+    per-bin pre-rounding doubles (numpy float64[4096] each)."""
+    import numpy as np
+    rdp = np.empty(4096, np.float64) if raw else None
+    rdn = np.empty(4096, np.float64) if raw else None
+    n = d_scrib.numel()
+    _check(load().gcfg_tlinks(_ptr(d_rgb), _ptr(d_scrib), int(n), _ptr(d_dp), _ptr(d_dn),
+                              _ptr(rdp), _ptr(rdn), _stream_ptr(stream)), "gcfg_tlinks")
+    return (rdp, rdn) if raw else None
+
+
+def nlinks(d_rgb, width, height, lam, d_up, d_down, d_left, d_right, stream=None):
+    _check(load().gcfg_nlinks(_ptr(d_rgb), int(width), int(height), float(lam), _ptr(d_up),
+                              _ptr(d_down), _ptr(d_left), _ptr(d_right), _stream_ptr(stream)),
+           "gcfg_nlinks")
+
+
+class Segmenter:
+    """Reusable one-image pipeline (data term, n-links, exact cut)."""
+
+    def __init__(self, max_w, max_h):
+        h = C.c_void_p()
+        _check(load().gcfg_seg_create(int(max_w), int(max_h), C.byref(h)), "gcfg_seg_create")
+        self.handle = h
+
+    def set_stream(self, stream):
+        _check(load().gcfg_seg_set_stream(self.handle, _stream_ptr(stream)), "gcfg_seg_set_stream")
+
+    def run(self, d_rgb, d_scrib, width, height, lam, d_smin=None, d_smax=None) -> dict:
+        res = Result()
+        _check(load().gcfg_seg_run(self.handle, _ptr(d_rgb), _ptr(d_scrib), int(width), int(height),
+                                   float(lam), _ptr(d_smin), _ptr(d_smax), C.byref(res)),
+               "gcfg_seg_run")
+        return res.as_dict()
+
+    def run_host(self, h_rgb, h_scrib, width, height, lam, h_smin=None, h_smax=None) -> dict:
+        res = Result()
+        _check(load().gcfg_seg_run_host(self.handle, _ptr(h_rgb), _ptr(h_scrib), int(width),
+                                        int(height), float(lam), _ptr(h_smin), _ptr(h_smax),
+                                        C.byref(res)), "gcfg_seg_run_host")
+        return res.as_dict()
+
+    def close(self):
+        if self.handle:
+            load().gcfg_seg_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

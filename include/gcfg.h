@@ -1,0 +1,139 @@
+/*
+ * gcfg.h -- C ABI of the GB300-native gc-fg graph-cut path (libgcfg.so).
+ *
+ * Plain pointers and sizes only.  Device-pointer arguments are CUDA device
+ * addresses; host-pointer arguments are ordinary host memory.  Every entry
+ * point returns a gcfg_status (0 = success) instead of aborting the process,
+ * and every loop inside the solver is bounded.  Streams are passed as
+ * `void *` holding a cudaStream_t (NULL = legacy default stream).
+ *
+ * The graph entry points replace the reference's C++ host API
+ * (GraphCut.cu, compiled into each application via #include):
+ *   gcfg_init          <- GC_Init          GraphCut.cu:187-263
+ *   gcfg_set_dataterms <- GC_SetDataterms  GraphCut.cu:265-269
+ *   gcfg_set_edges     <- GC_SetEdges      GraphCut.cu:271-289
+ *   gcfg_set_penalty   <- GC_SetPenalty    GraphCut.cu:296-299
+ *   gcfg_set_graph     <- GC_SetGraph      GraphCut.cu:301-319
+ *   gcfg_optimize      <- GC_Optimize      GraphCut.cu:385-534
+ *   gcfg_end           <- GC_End           GraphCut.cu:542-568
+ * The data-term entry points replace the DataTerm:: namespace
+ * (DataTerm.h:9-19, DataTerm.cpp:52-205).
+ */
+#ifndef GCFG_H
+#define GCFG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GCFG_OK = 0,
+    GCFG_ERR_INVALID = 1,         /* bad sizes, NULL handle, or out-of-range capacities */
+    GCFG_ERR_OOM = 2,             /* device allocation failed */
+    GCFG_ERR_CUDA = 3,            /* a CUDA call failed */
+    GCFG_ERR_NOT_CONVERGED = 4,   /* an iteration cap was reached */
+    GCFG_ERR_STATE = 5,           /* call out of order (e.g. optimize before set_graph) */
+    GCFG_ERR_CAPACITY = 6         /* admission refused: over the memory cap */
+} gcfg_status;
+
+/* Largest accepted capacity (t-links and n-links).  Keeps every excess and
+ * residual value inside int32 during the solve. */
+#define GCFG_MAX_CAP ((1 << 28) - 1)
+
+typedef struct gcfg_graph gcfg_graph;
+
+typedef struct {
+    int64_t flow;            /* exact max-flow value = energy of the min cut */
+    int32_t ref_energy;      /* the value GC_Optimize prints as "Final energy level"
+                                (GraphCut.cu:456-457): int32, border dp included */
+    int32_t status;          /* gcfg_status of the solve */
+    int32_t global_relabels; /* exact global relabels run */
+    int32_t gr_sweeps;       /* tile sweeps launched inside global relabels */
+    int32_t push_rounds;     /* checkerboard push/relabel rounds launched */
+    int32_t cut_sweeps;      /* tile sweeps of the source-side reachability pass */
+    int64_t active_after_first_gr; /* active nodes after the first global relabel */
+    float ms;                /* device time of the solve (CUDA events) */
+} gcfg_result;
+
+/* ---------------- graph API (drop-in for GraphCut.cu) ---------------- */
+
+/* GC_Init: allocate the residual graph for a w x h grid.  dp/dn are the
+ * source (positive) and sink (negative) t-link capacities, W*H int32,
+ * row-major, device memory, caller-owned.  If up != NULL the four arrays give
+ * per-direction n-link capacities (cap from pixel p to its upper/lower/left/
+ * right neighbour), else every n-link is `penalty`.  When dp != NULL the graph
+ * is built immediately (GC_Init calls GC_SetGraph, GraphCut.cu:250-260). */
+gcfg_status gcfg_init(int w, int h, const int32_t *dp, const int32_t *dn, int32_t penalty,
+                      const int32_t *up, const int32_t *down, const int32_t *left,
+                      const int32_t *right, gcfg_graph **out);
+gcfg_status gcfg_set_dataterms(gcfg_graph *g, const int32_t *dp, const int32_t *dn);
+gcfg_status gcfg_set_edges(gcfg_graph *g, const int32_t *up, const int32_t *down,
+                           const int32_t *left, const int32_t *right);
+gcfg_status gcfg_set_penalty(gcfg_graph *g, int32_t penalty);
+/* GC_SetGraph: (re)build the residual graph from the stored inputs. */
+gcfg_status gcfg_set_graph(gcfg_graph *g);
+/* GC_Optimize: solve to the exact max flow.  If host_label != NULL it
+ * receives W*H int32 labels: 1 = source side of the maximal source set
+ * (pixels that cannot reach the sink), 0 = sink side and the 1-pixel border,
+ * exactly like the reference's output (GraphCut.cu:507-529).  res may be
+ * NULL. */
+gcfg_status gcfg_optimize(gcfg_graph *g, int32_t *host_label, gcfg_result *res);
+/* After gcfg_optimize: both canonical cuts into device buffers (W*H bytes
+ * each, either may be NULL): smin = pixels reachable from the source in the
+ * final residual graph, smax = pixels that cannot reach the sink. */
+gcfg_status gcfg_get_cuts(gcfg_graph *g, uint8_t *d_smin, uint8_t *d_smax);
+/* GC_End: free everything the graph owns (caller arrays are not freed). */
+gcfg_status gcfg_end(gcfg_graph *g);
+/* Stream used by every later call on this graph (void* = cudaStream_t). */
+gcfg_status gcfg_set_stream(gcfg_graph *g, void *stream);
+/* Pushes launched per checkerboard colour between global relabels. */
+gcfg_status gcfg_set_schedule(gcfg_graph *g, int push_rounds_per_gr, int max_tile_sweeps);
+
+/* ---------------- data term + n-links (spec steps a, b) ---------------- */
+
+/* Colour-histogram t-links for one image: 16^3 bins of (r>>4, g>>4, b>>4)
+ * over fg (scrib == 1) and bg (scrib == 2) pixels, +1 Laplace smoothing;
+ * dp = round(10 * -log p_bg), dn = round(10 * -log p_fg) (int32).
+ * d_rgb: 3*n bytes interleaved, d_scrib: n bytes, d_dp/d_dn: n int32 (device).
+ * h_raw_dp/h_raw_dn: optional host double[4096] receiving the pre-rounding
+ * per-bin values. */
+gcfg_status gcfg_tlinks(const uint8_t *d_rgb, const uint8_t *d_scrib, int n, int32_t *d_dp,
+                        int32_t *d_dn, double *h_raw_dp, double *h_raw_dn, void *stream);
+/* Contrast-sensitive 4-connected n-links for a w x h image:
+ * w = round(lambda * exp(-||dI||^2 / (2 sigma^2))), sigma^2 = mean ||dI||^2
+ * over all horizontally and vertically adjacent pixel pairs.
+ * Outputs W*H int32 per direction (device); edges leaving the image are 0. */
+gcfg_status gcfg_nlinks(const uint8_t *d_rgb, int w, int h, double lambda, int32_t *d_up,
+                        int32_t *d_down, int32_t *d_left, int32_t *d_right, void *stream);
+
+/* ---------------- one-image segmentation pipeline ---------------- */
+
+typedef struct gcfg_segmenter gcfg_segmenter;
+
+/* A reusable solver for images up to max_w x max_h (buffers allocated once). */
+gcfg_status gcfg_seg_create(int max_w, int max_h, gcfg_segmenter **out);
+/* Data term + n-links + graph build + exact solve + both cuts for one image
+ * already on the device.  d_smin/d_smax: W*H bytes (device, may be NULL). */
+gcfg_status gcfg_seg_run(gcfg_segmenter *s, const uint8_t *d_rgb, const uint8_t *d_scrib, int w,
+                         int h, double lambda, uint8_t *d_smin, uint8_t *d_smax,
+                         gcfg_result *res);
+/* The same, end to end from host memory: copies the image and scribbles in,
+ * solves, copies the labels out (h_smin/h_smax W*H bytes, may be NULL). */
+gcfg_status gcfg_seg_run_host(gcfg_segmenter *s, const uint8_t *h_rgb, const uint8_t *h_scrib,
+                              int w, int h, double lambda, uint8_t *h_smin, uint8_t *h_smax,
+                              gcfg_result *res);
+gcfg_status gcfg_seg_set_stream(gcfg_segmenter *s, void *stream);
+gcfg_status gcfg_seg_destroy(gcfg_segmenter *s);
+
+/* ---------------- misc ---------------- */
+const char *gcfg_strerror(gcfg_status s);
+/* Number of kernel launches issued by this library in this process. */
+int64_t gcfg_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

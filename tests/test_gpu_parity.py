@@ -1,0 +1,176 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle and
+the reference's own outputs.  Integer work is compared bit for bit."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import gcfg  # noqa: E402
+import oracle as O  # noqa: E402
+from gpu_util import dev, gpu_segment, gpu_solve  # noqa: E402
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+META = json.load(open(os.path.join(GOLDEN, "reference_pins.json")))["cases"]
+DATA = np.load(os.path.join(GOLDEN, "reference_pins.npz"))
+
+
+def _case(c):
+    name = c["name"]
+    dp = DATA[f"{name}__dp"].astype(np.int32)
+    dn = DATA[f"{name}__dn"].astype(np.int32)
+    kw = {"penalty": c["penalty"]}
+    if c["arrays"]:
+        for k in ("up", "down", "left", "right"):
+            kw[k] = DATA[f"{name}__{k}"].astype(np.int32)
+    n = c["W"] * c["H"]
+    labels = np.unpackbits(DATA[f"{name}__ref_labels"])[:n].reshape(c["H"], c["W"])
+    return dp, dn, kw, labels
+
+
+@pytest.mark.parametrize("case", META, ids=[c["name"] for c in META])
+def test_reference_pins(case):
+    """GC_Optimize labels and printed energy equal the reference's own."""
+    dp, dn, kw, ref_labels = _case(case)
+    label, smin, smax, res = gpu_solve(dp, dn, **kw)
+    assert np.array_equal(label, ref_labels.astype(np.int32))
+    assert res["ref_energy"] == case["ref_energy"]
+    assert res["flow"] == case["oracle_flow"]
+    o = O.solve(dp, dn, **kw)
+    assert np.array_equal(smin, o["smin"]) and np.array_equal(smax, o["smax"])
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_grids_vs_oracle(seed):
+    rng = np.random.default_rng(7000 + seed)
+    for _ in range(6):
+        H, W = (int(v) for v in rng.integers(3, 150, 2))
+        dp = rng.integers(0, 300, (H, W)).astype(np.int32)
+        dn = rng.integers(0, 300, (H, W)).astype(np.int32)
+        if rng.random() < 0.5:
+            kw = {k: rng.integers(0, 120, (H, W)).astype(np.int32) for k in ("up", "down", "left", "right")}
+        else:
+            kw = {"penalty": int(rng.integers(0, 150))}
+        label, smin, smax, res = gpu_solve(dp, dn, **kw)
+        o = O.solve(dp, dn, **kw)
+        assert res["flow"] == o["flow"]
+        assert np.array_equal(smax, o["smax"]) and np.array_equal(smin, o["smin"])
+        assert np.array_equal(label, o["smax"].astype(np.int32))
+
+
+@pytest.mark.parametrize("schedule", [(1, 1), (1, 4), (8, 256)])
+def test_schedules_do_not_change_result(schedule):
+    rng = np.random.default_rng(11)
+    H, W = 97, 131
+    dp = rng.integers(0, 300, (H, W)).astype(np.int32)
+    dn = rng.integers(0, 300, (H, W)).astype(np.int32)
+    label, smin, smax, res = gpu_solve(dp, dn, penalty=60, schedule=schedule)
+    o = O.solve(dp, dn, penalty=60)
+    assert res["flow"] == o["flow"]
+    assert np.array_equal(smin, o["smin"]) and np.array_equal(smax, o["smax"])
+
+
+def test_long_paths_vs_oracle():
+    """Flow that must cross many tiles (worst case for tile-local pushes)."""
+    H, W = 40, 600
+    dp = np.zeros((H, W), np.int32)
+    dn = np.zeros((H, W), np.int32)
+    dp[:, 1] = 500
+    dn[:, W - 2] = 500
+    label, smin, smax, res = gpu_solve(dp, dn, penalty=7)
+    o = O.solve(dp, dn, penalty=7)
+    assert res["flow"] == o["flow"] == 7 * (H - 2)
+    assert np.array_equal(smin, o["smin"]) and np.array_equal(smax, o["smax"])
+
+
+def test_tlinks_bit_exact():
+    rgb, scrib = O.generate(0, 256, 256, 0)
+    H, W = scrib.shape
+    dp = torch.empty((H, W), dtype=torch.int32, device="cuda")
+    dn = torch.empty_like(dp)
+    rdp, rdn = gcfg.tlinks(dev(rgb), dev(scrib), dp, dn, raw=True)
+    hf, hb = O.histograms(rgb, scrib)
+    odp_raw, odn_raw, _, _ = O.tlink_lut(hf, hb)
+    # pre-quantisation values: within 1e-6 relative (they agree far closer)
+    np.testing.assert_allclose(rdp, odp_raw, rtol=1e-12)
+    np.testing.assert_allclose(rdn, odn_raw, rtol=1e-12)
+    odp, odn = O.tlinks(rgb, scrib)
+    assert np.array_equal(dp.cpu().numpy(), odp) and np.array_equal(dn.cpu().numpy(), odn)
+
+
+@pytest.mark.parametrize("lam", [10.0, 50.0, 200.0])
+def test_nlinks_bit_exact(lam):
+    rgb, _ = O.generate(1, 320, 200, 5)
+    H, W = rgb.shape[:2]
+    outs = [torch.empty((H, W), dtype=torch.int32, device="cuda") for _ in range(4)]
+    gcfg.nlinks(dev(rgb), W, H, lam, *outs)
+    ref = O.nlinks(rgb, lam)
+    for a, b in zip(outs, ref):
+        assert np.array_equal(a.cpu().numpy(), b)
+
+
+def test_segment_cfg0_vs_oracle():
+    rgb, scrib = O.generate(0, 256, 256, 0)
+    smin, smax, res = gpu_segment(rgb, scrib, 50.0)
+    o = O.segment(rgb, scrib, 50.0)
+    assert res["flow"] == o["flow"]
+    assert np.array_equal(smin, o["smin"]) and np.array_equal(smax, o["smax"])
+
+
+@pytest.mark.parametrize("seed,lam", [(1, 10.0), (2, 50.0), (3, 200.0)])
+def test_segment_cfg1_vs_oracle(seed, lam):
+    rgb, scrib = O.generate(1, 1920, 1080, seed)
+    smin, smax, res = gpu_segment(rgb, scrib, lam)
+    o = O.segment(rgb, scrib, lam)
+    assert res["flow"] == o["flow"]
+    assert np.array_equal(smin, o["smin"]) and np.array_equal(smax, o["smax"])
+
+
+def test_segment_cfg2_vs_oracle():
+    rgb, scrib = O.generate(2, 4096, 4096, 2)
+    smin, smax, res = gpu_segment(rgb, scrib, 100.0)
+    o = O.segment(rgb, scrib, 100.0)
+    assert res["flow"] == o["flow"]
+    assert np.array_equal(smin, o["smin"]) and np.array_equal(smax, o["smax"])
+
+
+def test_host_entry_point_matches_device_path():
+    rgb, scrib = O.generate(3, 300, 200, 1005)
+    seg = gcfg.Segmenter(512, 512)
+    smin_d, smax_d, res_d = gpu_segment(rgb, scrib, 50.0, seg)
+    smin_h = np.zeros(scrib.shape, np.uint8)
+    smax_h = np.zeros(scrib.shape, np.uint8)
+    res_h = seg.run_host(rgb, scrib, 300, 200, 50.0, smin_h, smax_h)
+    assert res_h["flow"] == res_d["flow"]
+    assert np.array_equal(smin_h, smin_d) and np.array_equal(smax_h, smax_d)
+
+
+def test_invalid_capacities_rejected():
+    dp = np.full((8, 8), 5, np.int32)
+    dn = np.full((8, 8), 3, np.int32)
+    dp[3, 3] = -1
+    with pytest.raises(gcfg.GcfgError) as ei:
+        gpu_solve(dp, dn, penalty=1)
+    assert ei.value.status == gcfg.GCFG_ERR_INVALID
+    dp[3, 3] = gcfg.GCFG_MAX_CAP + 1
+    with pytest.raises(gcfg.GcfgError):
+        gpu_solve(dp, dn, penalty=1)
+
+
+def test_optimize_twice_needs_set_graph():
+    """As in the reference the graph is consumed by the solve."""
+    dp = np.full((16, 16), 9, np.int32)
+    dn = np.full((16, 16), 4, np.int32)
+    t = [dev(dp), dev(dn)]
+    gw = gcfg.GC_Init(16, 16, t[0], t[1], 3)
+    r1 = gcfg.GC_Optimize(gw)
+    with pytest.raises(gcfg.GcfgError) as ei:
+        gcfg.GC_Optimize(gw)
+    assert ei.value.status == gcfg.GCFG_ERR_STATE
+    gcfg.GC_SetGraph(gw)
+    r2 = gcfg.GC_Optimize(gw)
+    assert r1["flow"] == r2["flow"]
+    gcfg.GC_End(gw)
