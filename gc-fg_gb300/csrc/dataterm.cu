@@ -248,10 +248,8 @@ static int hist_blocks(int n) {
 static gcfg_status run_tlut(DataTermBufs &b, const uint8_t *rgb, const uint8_t *scrib, int n,
                             cudaStream_t st) {
     GCFG_CK(cudaMemsetAsync(b.hist, 0, 2 * NBINS * sizeof(int), st));
-    k_hist<<<hist_blocks(n), 256, 0, st>>>(rgb, scrib, n, b.hist);
-    GCFG_LAUNCHED();
-    k_tlut<<<1, 1024, 0, st>>>(b.hist, b.dp_lut, b.dn_lut, b.raw_dp, b.raw_dn);
-    GCFG_LAUNCHED();
+    GCFG_LAUNCH(GCFG_PK_HIST, st, k_hist<<<hist_blocks(n), 256, 0, st>>>(rgb, scrib, n, b.hist));
+    GCFG_LAUNCH(GCFG_PK_TLUT, st, k_tlut<<<1, 1024, 0, st>>>(b.hist, b.dp_lut, b.dn_lut, b.raw_dp, b.raw_dn));
     GCFG_CK(cudaGetLastError());
     return GCFG_OK;
 }
@@ -259,11 +257,9 @@ static gcfg_status run_tlut(DataTermBufs &b, const uint8_t *rgb, const uint8_t *
 static gcfg_status run_wlut(DataTermBufs &b, const uint8_t *rgb, int W, int H, double lambda,
                             cudaStream_t st) {
     GCFG_CK(cudaMemsetAsync(b.sigma, 0, sizeof(unsigned long long), st));
-    k_sigma<<<hist_blocks(W * H), 256, 0, st>>>(rgb, W, H, b.sigma);
-    GCFG_LAUNCHED();
+    GCFG_LAUNCH(GCFG_PK_SIGMA, st, k_sigma<<<hist_blocks(W * H), 256, 0, st>>>(rgb, W, H, b.sigma));
     const long long count = (long long)(W - 1) * H + (long long)W * (H - 1);
-    k_wlut<<<div_up(MAX_D2 + 1, 256), 256, 0, st>>>(b.sigma, count, lambda, b.wlut);
-    GCFG_LAUNCHED();
+    GCFG_LAUNCH(GCFG_PK_WLUT, st, k_wlut<<<div_up(MAX_D2 + 1, 256), 256, 0, st>>>(b.sigma, count, lambda, b.wlut));
     GCFG_CK(cudaGetLastError());
     return GCFG_OK;
 }
@@ -296,8 +292,7 @@ gcfg_status gcfg_tlinks(const uint8_t *d_rgb, const uint8_t *d_scrib, int n, int
     gcfg_status rc = b.alloc();
     if (rc == GCFG_OK) rc = run_tlut(b, d_rgb, d_scrib, n, st);
     if (rc == GCFG_OK) {
-        k_tlinks_apply<<<div_up(n, 256), 256, 0, st>>>(d_rgb, n, b.dp_lut, b.dn_lut, d_dp, d_dn);
-        GCFG_LAUNCHED();
+        GCFG_LAUNCH(GCFG_PK_OTHER, st, k_tlinks_apply<<<div_up(n, 256), 256, 0, st>>>(d_rgb, n, b.dp_lut, b.dn_lut, d_dp, d_dn));
         if (cudaGetLastError() != cudaSuccess) rc = GCFG_ERR_CUDA;
     }
     if (rc == GCFG_OK && h_raw_dp &&
@@ -322,8 +317,7 @@ gcfg_status gcfg_nlinks(const uint8_t *d_rgb, int w, int h, double lambda, int32
     if (rc == GCFG_OK) rc = run_wlut(b, d_rgb, w, h, lambda, st);
     if (rc == GCFG_OK) {
         dim3 blk(32, 8), grd(div_up(w, 32), div_up(h, 8));
-        k_nlinks_apply<<<grd, blk, 0, st>>>(d_rgb, w, h, b.wlut, d_up, d_down, d_left, d_right);
-        GCFG_LAUNCHED();
+        GCFG_LAUNCH(GCFG_PK_OTHER, st, k_nlinks_apply<<<grd, blk, 0, st>>>(d_rgb, w, h, b.wlut, d_up, d_down, d_left, d_right));
         if (cudaGetLastError() != cudaSuccess) rc = GCFG_ERR_CUDA;
     }
     if (cudaStreamSynchronize(st) != cudaSuccess && rc == GCFG_OK) rc = GCFG_ERR_CUDA;
@@ -376,8 +370,7 @@ gcfg_status gcfg_seg_run(gcfg_segmenter *s, const uint8_t *d_rgb, const uint8_t 
     GCFG_TRY(run_wlut(s->dt, d_rgb, w, h, lambda, st));
     GCFG_CK(cudaMemsetAsync(s->s.cnt, 0, sizeof(Counters), st));
     dim3 blk(32, 8), grd(g.Wp / 32, g.Hp / 8);
-    k_build_image<<<grd, blk, 0, st>>>(g, d_rgb, s->dt.dp_lut, s->dt.dn_lut, s->dt.wlut, s->s.cnt);
-    GCFG_LAUNCHED();
+    GCFG_LAUNCH(GCFG_PK_BUILD, st, k_build_image<<<grd, blk, 0, st>>>(g, d_rgb, s->dt.dp_lut, s->dt.dn_lut, s->dt.wlut, s->s.cnt));
     GCFG_CK(cudaGetLastError());
     gcfg_result r;
     memset(&r, 0, sizeof(r));

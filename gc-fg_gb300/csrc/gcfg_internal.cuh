@@ -46,12 +46,27 @@ struct Counters {
     unsigned long long ref_init;      // reference's "Initial energy level" (wraps like int32)
     unsigned long long pos_excess;    // sum of positive excess
     unsigned long long active;        // active nodes (e > 0, h < INF)
+    unsigned long long push_tiles;    // tiles processed by push launches
     int changed;                      // a tile sweep changed something
     int error;                        // input validation failure
     int pad[2];
 };
 
 extern std::atomic<long long> g_launches;
+
+constexpr int PK_COUNT_KINDS = GCFG_PK_NKINDS;
+bool prof_on();
+void prof_begin(cudaStream_t st);
+void prof_end(int kind, cudaStream_t st);
+
+// Launch a kernel, counting it and (when profiling) timing it with events.
+#define GCFG_LAUNCH(kind, st, ...)                      \
+    do {                                                \
+        ::gcfg::prof_begin(st);                         \
+        __VA_ARGS__;                                    \
+        ::gcfg::prof_end(kind, st);                     \
+        ::gcfg::g_launches.fetch_add(1, std::memory_order_relaxed); \
+    } while (0)
 
 inline int div_up(int a, int b) { return (a + b - 1) / b; }
 

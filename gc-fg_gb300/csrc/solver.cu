@@ -203,11 +203,13 @@ __global__ void __launch_bounds__(TILE_THREADS) k_count(GraphDev g, Counters *cn
 // Tile push/relabel (one checkerboard colour per launch)
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(TILE_THREADS) k_push_tile(GraphDev g, int color, int max_sweeps) {
+__global__ void __launch_bounds__(TILE_THREADS) k_push_tile(GraphDev g, int color, int max_sweeps,
+                                                             Counters *cnt) {
     const int tx = blockIdx.x, ty = blockIdx.y;
     if (((tx + ty) & 1) != color) return;
     const int t = ty * g.tiles_x + tx;
     if (!g.tile_active[t]) return;
+    if (threadIdx.x == 0) atomicAdd(&cnt->push_tiles, 1ULL);
 
     __shared__ int h_s[TILE_H + 2][TILE_W + 2];
     __shared__ int e_s[TILE_H][TILE_W];
@@ -511,8 +513,7 @@ gcfg_status build_from_arrays(SolverState &s, const GraphDev &g, const int *dp, 
     GCFG_CK(cudaMemsetAsync(s.cnt, 0, sizeof(Counters), st));
     dim3 blk(32, 8);
     dim3 grd(g.Wp / 32, g.Hp / 8);
-    k_build_arrays<<<grd, blk, 0, st>>>(g, dp, dn, penalty, up, down, left, right, s.cnt);
-    GCFG_LAUNCHED();
+    GCFG_LAUNCH(GCFG_PK_BUILD, st, k_build_arrays<<<grd, blk, 0, st>>>(g, dp, dn, penalty, up, down, left, right, s.cnt));
     GCFG_CK(cudaGetLastError());
     GCFG_TRY(read_counters(s, st));
     if (s.h_cnt->error) return GCFG_ERR_INVALID;
@@ -530,14 +531,12 @@ static int grid_stride_blocks(size_t n) {
 static gcfg_status global_relabel(SolverState &s, const GraphDev &g, cudaStream_t st,
                                   gcfg_result *res) {
     const size_t n = (size_t)g.Wp * g.Hp;
-    k_gr_init<<<grid_stride_blocks(n), 256, 0, st>>>(g);
-    GCFG_LAUNCHED();
+    GCFG_LAUNCH(GCFG_PK_GR_INIT, st, k_gr_init<<<grid_stride_blocks(n), 256, 0, st>>>(g));
     dim3 tg(g.tiles_x, g.tiles_y);
     int launches = 0;
     for (;;) {
         GCFG_CK(cudaMemsetAsync(&s.cnt->changed, 0, sizeof(int), st));
-        k_gr_tile<<<tg, TILE_THREADS, 0, st>>>(g, s.cnt);
-        GCFG_LAUNCHED();
+        GCFG_LAUNCH(GCFG_PK_GR_TILE, st, k_gr_tile<<<tg, TILE_THREADS, 0, st>>>(g, s.cnt));
         launches++;
         GCFG_TRY(read_counters(s, st));
         if (!s.h_cnt->changed) break;
@@ -546,10 +545,10 @@ static gcfg_status global_relabel(SolverState &s, const GraphDev &g, cudaStream_
     if (res) {
         res->global_relabels++;
         res->gr_sweeps += launches;
+        res->gr_tiles += (long long)launches * g.tiles_x * g.tiles_y;
     }
     GCFG_CK(cudaMemsetAsync(&s.cnt->pos_excess, 0, 2 * sizeof(unsigned long long), st));
-    k_count<<<tg, TILE_THREADS, 0, st>>>(g, s.cnt);
-    GCFG_LAUNCHED();
+    GCFG_LAUNCH(GCFG_PK_COUNT, st, k_count<<<tg, TILE_THREADS, 0, st>>>(g, s.cnt));
     GCFG_TRY(read_counters(s, st));
     return GCFG_OK;
 }
@@ -570,8 +569,7 @@ gcfg_status solve(SolverState &s, const GraphDev &g, cudaStream_t st, int push_r
         if (outer >= MAX_OUTER) { rc = GCFG_ERR_NOT_CONVERGED; break; }
         for (int r = 0; r < push_rounds; ++r) {
             for (int color = 0; color < 2; ++color) {
-                k_push_tile<<<tg, TILE_THREADS, 0, st>>>(g, color, max_sweeps);
-                GCFG_LAUNCHED();
+                GCFG_LAUNCH(GCFG_PK_PUSH, st, k_push_tile<<<tg, TILE_THREADS, 0, st>>>(g, color, max_sweeps, s.cnt));
             }
             local.push_rounds++;
         }
@@ -582,15 +580,14 @@ gcfg_status solve(SolverState &s, const GraphDev &g, cudaStream_t st, int push_r
         // the same counter block and arrive with every counter read-back.
         const long long pos = (long long)s.h_cnt->pos_excess;
         local.flow = (long long)s.h_cnt->interior_dp - pos;
+        local.push_tiles = (long long)s.h_cnt->push_tiles;
         local.ref_energy = (int32_t)((uint32_t)s.h_cnt->ref_init - (uint32_t)(unsigned long long)pos);
         // source-side reachability
         const size_t n = (size_t)g.Wp * g.Hp;
-        k_reach_init<<<grid_stride_blocks(n), 256, 0, st>>>(g);
-        GCFG_LAUNCHED();
+        GCFG_LAUNCH(GCFG_PK_REACH_INIT, st, k_reach_init<<<grid_stride_blocks(n), 256, 0, st>>>(g));
         for (int it = 0;; ++it) {
             GCFG_CK(cudaMemsetAsync(&s.cnt->changed, 0, sizeof(int), st));
-            k_reach_tile<<<tg, TILE_THREADS, 0, st>>>(g, s.cnt);
-            GCFG_LAUNCHED();
+            GCFG_LAUNCH(GCFG_PK_REACH, st, k_reach_tile<<<tg, TILE_THREADS, 0, st>>>(g, s.cnt));
             local.cut_sweeps++;
             GCFG_TRY(read_counters(s, st));
             if (!s.h_cnt->changed) break;
@@ -610,8 +607,7 @@ gcfg_status solve(SolverState &s, const GraphDev &g, cudaStream_t st, int push_r
 gcfg_status extract(const GraphDev &g, uint8_t *smin, uint8_t *smax, int *label, cudaStream_t st) {
     dim3 blk(32, 8);
     dim3 grd(div_up(g.W, 32), div_up(g.H, 8));
-    k_extract<<<grd, blk, 0, st>>>(g, smin, smax, label);
-    GCFG_LAUNCHED();
+    GCFG_LAUNCH(GCFG_PK_EXTRACT, st, k_extract<<<grd, blk, 0, st>>>(g, smin, smax, label));
     GCFG_CK(cudaGetLastError());
     return GCFG_OK;
 }

@@ -31,7 +31,11 @@ EXPORTS = [
     "gcfg_optimize", "gcfg_get_cuts", "gcfg_end", "gcfg_set_stream", "gcfg_set_schedule",
     "gcfg_tlinks", "gcfg_nlinks", "gcfg_seg_create", "gcfg_seg_run", "gcfg_seg_run_host",
     "gcfg_seg_set_stream", "gcfg_seg_destroy", "gcfg_strerror", "gcfg_launch_count",
+    "gcfg_profile_enable", "gcfg_profile_read",
 ]
+
+PROF_KINDS = ["hist", "tlut", "sigma", "wlut", "build", "gr_init", "gr_tile", "count", "push",
+              "reach_init", "reach", "extract", "other"]
 
 
 class GcfgError(RuntimeError):
@@ -44,10 +48,15 @@ class Result(C.Structure):
     _fields_ = [("flow", C.c_int64), ("ref_energy", C.c_int32), ("status", C.c_int32),
                 ("global_relabels", C.c_int32), ("gr_sweeps", C.c_int32),
                 ("push_rounds", C.c_int32), ("cut_sweeps", C.c_int32),
-                ("active_after_first_gr", C.c_int64), ("ms", C.c_float)]
+                ("active_after_first_gr", C.c_int64), ("push_tiles", C.c_int64),
+                ("gr_tiles", C.c_int64), ("ms", C.c_float)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ProfEntry(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("launches", C.c_int32), ("ms", C.c_double)]
 
 
 _lib = None
@@ -84,6 +93,8 @@ def load(path: str = LIB_PATH):
         "gcfg_seg_destroy": (S, [P]),
         "gcfg_strerror": (C.c_char_p, [I]),
         "gcfg_launch_count": (C.c_int64, []),
+        "gcfg_profile_enable": (S, [I]),
+        "gcfg_profile_read": (S, [C.POINTER(ProfEntry), I, C.POINTER(I)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -116,6 +127,18 @@ def _ptr(t):
 
 def launch_count() -> int:
     return load().gcfg_launch_count()
+
+
+def profile_enable(on: bool = True):
+    _check(load().gcfg_profile_enable(1 if on else 0), "gcfg_profile_enable")
+
+
+def profile_read() -> dict:
+    """Per-kernel-kind {launches, ms} since the last read (syncs the device)."""
+    arr = (ProfEntry * len(PROF_KINDS))()
+    n = C.c_int()
+    _check(load().gcfg_profile_read(arr, len(PROF_KINDS), C.byref(n)), "gcfg_profile_read")
+    return {PROF_KINDS[e.kind]: dict(launches=e.launches, ms=e.ms) for e in arr[: n.value]}
 
 
 def _stream_ptr(stream):

@@ -55,6 +55,8 @@ typedef struct {
     int32_t push_rounds;     /* checkerboard push/relabel rounds launched */
     int32_t cut_sweeps;      /* tile sweeps of the source-side reachability pass */
     int64_t active_after_first_gr; /* active nodes after the first global relabel */
+    int64_t push_tiles;      /* 32x32 tiles processed by push/relabel launches */
+    int64_t gr_tiles;        /* 32x32 tiles processed by global-relabel launches */
     float ms;                /* device time of the solve (CUDA events) */
 } gcfg_result;
 
@@ -127,6 +129,26 @@ gcfg_status gcfg_seg_run_host(gcfg_segmenter *s, const uint8_t *h_rgb, const uin
                               gcfg_result *res);
 gcfg_status gcfg_seg_set_stream(gcfg_segmenter *s, void *stream);
 gcfg_status gcfg_seg_destroy(gcfg_segmenter *s);
+
+/* ---------------- profiling (off by default) ---------------- */
+
+/* Kernel kinds reported by gcfg_profile_read (index = kind). */
+typedef enum {
+    GCFG_PK_HIST = 0, GCFG_PK_TLUT, GCFG_PK_SIGMA, GCFG_PK_WLUT, GCFG_PK_BUILD,
+    GCFG_PK_GR_INIT, GCFG_PK_GR_TILE, GCFG_PK_COUNT, GCFG_PK_PUSH, GCFG_PK_REACH_INIT,
+    GCFG_PK_REACH, GCFG_PK_EXTRACT, GCFG_PK_OTHER, GCFG_PK_NKINDS
+} gcfg_prof_kind;
+
+typedef struct {
+    int32_t kind;
+    int32_t launches;
+    double ms;               /* summed device duration (CUDA events) */
+} gcfg_prof_entry;
+
+/* Bracket every kernel launch with CUDA events (adds host overhead). */
+gcfg_status gcfg_profile_enable(int on);
+/* Per-kind totals since the last read; out must hold GCFG_PK_NKINDS entries. */
+gcfg_status gcfg_profile_read(gcfg_prof_entry *out, int max_entries, int *n_out);
 
 /* ---------------- misc ---------------- */
 const char *gcfg_strerror(gcfg_status s);
