@@ -1,0 +1,35 @@
+// dataterm.cuh -- host launchers of the batched data-term kernels.
+#pragma once
+
+#include "engine.cuh"
+
+namespace gcfg {
+
+constexpr int NBINS = 4096;                   // 16^3 colour bins per class
+constexpr int MAX_D2 = 3 * 255 * 255;         // largest ||dI||^2 of two RGB pixels
+constexpr int WLUT_STRIDE = MAX_D2 + 1;       // n-link table entries per image
+constexpr int CHUNK_PX = 8192;                // pixels per block in per-image passes
+
+// Device buffers of the data term for a batch (per image: 2*4096 histogram
+// bins, 4096 dp and dn entries, WLUT_STRIDE n-link weights).
+struct DtArgs {
+    int n_img;
+    long long total_chunks;
+    const uint8_t *rgb;       // packed row-major RGB of all images
+    const uint8_t *scrib;     // packed row-major scribbles (0 none, 1 fg, 2 bg)
+    const ImgDesc *img;
+    ImgState *ist;
+    const long long *chunk_off;
+    int *hist;
+    int *dp_lut, *dn_lut;
+    double *raw_dp, *raw_dn;  // optional (NULL): pre-rounding per-bin values
+    int *wlut;
+};
+
+gcfg_status dt_tables(const DtArgs &a, cudaStream_t st);
+gcfg_status dt_build(const Batch &b, const DtArgs &a, cudaStream_t st);
+gcfg_status dt_apply_tlinks(const DtArgs &a, long long n, int *dp, int *dn, cudaStream_t st);
+gcfg_status dt_apply_nlinks(const DtArgs &a, int W, int H, int *up, int *down, int *left, int *right,
+                            cudaStream_t st);
+
+}  // namespace gcfg

@@ -1,0 +1,741 @@
+// engine.cu -- persistent tile-space push-relabel solver (GB300, sm_103a).
+//
+// Algorithm (exact max-flow on a 4-connected grid, the reference's model):
+//   excess e = dp - dn (+ inflow - outflow); heights = residual distance to
+//   the sink (sink-connected nodes, e < 0, have height 1); the solve ends
+//   when, after an exact global relabel, no node with e > 0 can reach the
+//   sink.  Cuts: S_max = nodes that cannot reach the sink (the reference's
+//   labels, GraphCutKernels.cu:228-351), S_min = nodes reachable from the
+//   source (from nodes with e > 0).
+//
+// GPU organisation:
+//   * Tile BFS: a 32x32 tile is 32 row bitmasks per residual direction; one
+//     warp (lane = row) grows the BFS frontier of the whole tile with shifts,
+//     warp shuffles and ballots, seeded by sink nodes (level 1) and by the
+//     halo's heights.  It gives exact distances for the tile given the halo.
+//   * Global relabel (GraphCutKernels.cu:757-875 does 10 Bellman-Ford steps
+//     per launch with a host round trip each): tiles recompute with the tile
+//     BFS until no tile border changes; a tile whose border distances
+//     decrease queues its neighbours (frontier of tiles, de-duplicated).
+//   * Push (GraphCutKernels.cu:433-581 WavePush + :600-724 Relabel): tiles
+//     of one checkerboard colour run at a time, so a running tile's halo is
+//     frozen; inside the tile, shared-memory push/relabel sweeps with an
+//     exact local relabel (tile BFS against the frozen halo) every few
+//     sweeps; flow pushed into the halo is handed over with atomics and the
+//     receiving tile is queued for the next colour phase.
+//   * Everything above runs in one cooperative persistent kernel; phases are
+//     separated by a grid barrier whose spin is bounded (on timeout the
+//     kernel records an error and returns).
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "engine.cuh"
+
+namespace gcfg {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int BFS_MAX_ITERS = TPX + 4 * 32 + 8;
+constexpr unsigned long long SPIN_LIMIT = 1ull << 25;   // about a second of polling
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+
+struct TileGeo {
+    int img, tx, ty, color;
+    int nb[4];  // left, right, up, down tile (-1 at the image edge)
+};
+
+__device__ __forceinline__ TileGeo tile_geo(const Batch &b, int t) {
+    TileGeo g;
+    g.img = __ldg(b.tile_img + t);
+    const int tile0 = __ldg(&b.img[g.img].tile0);
+    const int tx_n = __ldg(&b.img[g.img].tiles_x);
+    const int ty_n = __ldg(&b.img[g.img].tiles_y);
+    const int lt = t - tile0;
+    g.tx = lt % tx_n;
+    g.ty = lt / tx_n;
+    g.color = (g.tx + g.ty) & 1;
+    g.nb[0] = g.tx > 0 ? t - 1 : -1;
+    g.nb[1] = g.tx < tx_n - 1 ? t + 1 : -1;
+    g.nb[2] = g.ty > 0 ? t - tx_n : -1;
+    g.nb[3] = g.ty < ty_n - 1 ? t + tx_n : -1;
+    return g;
+}
+
+__device__ __forceinline__ void set_error(const Batch &b, int code) {
+    atomicExch(&b.ctl->err, 1);
+    atomicCAS(&b.ctl->err_code, 0, code);
+}
+
+// Queue tile t under `tag` in list `slot` unless it is already queued for it.
+// A queue never holds a tile twice, so it cannot overflow; the bound check
+// records an error instead of writing out of range should that ever fail.
+__device__ __forceinline__ void enqueue(const Batch &b, int *mark, int slot, int tag, int t) {
+    if (atomicMax(mark + t, tag) < tag) {
+        const int pos = atomicAdd(&b.ctl->size[slot], 1);
+        if (pos < b.list_cap) b.lists[(size_t)slot * b.list_cap + pos] = t;
+        else set_error(b, ERRC_QUEUE);
+    }
+}
+
+// Grid-wide barrier over the co-resident blocks of the cooperative launch.
+// The last block to arrive clears the queues named in reset_mask before it
+// releases the others.  The spin is bounded: on timeout the error flag is
+// set and every block returns false.
+__device__ bool grid_sync(const Batch &b, unsigned reset_mask) {
+    Ctl *c = b.ctl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = &c->bar_gen;
+        const unsigned gen = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(&c->bar_count, 1u);
+        if (arrived == gridDim.x - 1) {
+            for (int s = 0; s < L_NLISTS; ++s)
+                if ((reset_mask >> s) & 1u) {
+                    c->size[s] = 0;
+                    c->take[s] = 0;
+                }
+            c->bar_count = 0;
+            __threadfence();
+            atomicAdd(&c->bar_gen, 1u);
+        } else {
+            unsigned long long it = 0;
+            while (*vgen == gen) {
+                if (++it > SPIN_LIMIT) {
+                    set_error(b, ERRC_BARRIER);
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int *)&c->err == 0;
+}
+
+__device__ __forceinline__ int vload(const int *p) { return *(volatile const int *)p; }
+
+// ---------------------------------------------------------------------------
+// Bit-parallel tile BFS (one warp, lane = row)
+// ---------------------------------------------------------------------------
+// Rl/Rr/Ru/Rd: row masks of residual capacity toward left/right/up/down.
+// sink: nodes of this row at level 1 (e < 0).
+// hl/hr: level of this row's left/right halo node; ht/hb: level of the halo
+// node above/below column `lane`.  Levels of the tile are written to
+// hs[row * stride + col]; unreachable nodes get INF.
+__device__ void tile_bfs(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd, unsigned sink, int hl,
+                         int hr, int ht, int hb, int *hs, int stride) {
+    const int lane = threadIdx.x & 31;
+    int *row = hs + lane * stride;
+#pragma unroll 8
+    for (int x = 0; x < 32; ++x) row[x] = INF_H;
+    unsigned S = sink;
+    for (unsigned m = sink; m; m &= m - 1) row[__ffs(m) - 1] = 1;
+    int lvl = 1;
+    for (int it = 0; it < BFS_MAX_ITERS; ++it) {
+        const unsigned T = __ballot_sync(FULL, ht <= lvl);
+        const unsigned B = __ballot_sync(FULL, hb <= lvl);
+        unsigned up = __shfl_up_sync(FULL, S, 1);
+        unsigned dn = __shfl_down_sync(FULL, S, 1);
+        if (lane == 0) up = T;
+        if (lane == 31) dn = B;
+        const unsigned lin = (S << 1) | (hl <= lvl ? 1u : 0u);
+        const unsigned rin = (S >> 1) | (hr <= lvl ? 0x80000000u : 0u);
+        unsigned nw = ((Rl & lin) | (Rr & rin) | (Ru & up) | (Rd & dn)) & ~S;
+        if (__any_sync(FULL, nw != 0)) {
+            S |= nw;
+            ++lvl;
+            for (; nw; nw &= nw - 1) row[__ffs(nw) - 1] = lvl;
+        } else {
+            int cand = INF_H;
+            if (hl > lvl) cand = min(cand, hl);
+            if (hr > lvl) cand = min(cand, hr);
+            if (ht > lvl) cand = min(cand, ht);
+            if (hb > lvl) cand = min(cand, hb);
+            const int nxt = __reduce_min_sync(FULL, cand);
+            if (nxt >= INF_H) break;
+            lvl = nxt;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Shared memory of the persistent kernel (phases reuse the same bytes)
+// ---------------------------------------------------------------------------
+
+struct SmemPush {
+    int4 c[TILE_H][TILE_W];
+    int e[TILE_H][TILE_W];
+    int h[TILE_H + 2][TILE_W + 2];
+    int halo_in[4][32];
+    unsigned m[5][32];  // left, right, up, down, sink row masks
+    int idx;
+    int flag;
+};
+struct SmemWarp {
+    int hs[8][32 * 33];
+};
+union Smem {
+    SmemPush p;
+    SmemWarp w;
+};
+
+// ---------------------------------------------------------------------------
+// Global relabel / reach (warp per tile)
+// ---------------------------------------------------------------------------
+
+// Load the residual row masks of tile t (lane = row after the loop).
+__device__ __forceinline__ void load_masks(const Batch &b, size_t base, unsigned &Rl, unsigned &Rr,
+                                           unsigned &Ru, unsigned &Rd, unsigned &neg, unsigned &pos,
+                                           int &e_row0, int &e_row31) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll 4
+    for (int r = 0; r < 32; ++r) {
+        const int4 c = __ldcg(b.cap + base + r * 32 + lane);
+        const int e = __ldcg(b.exc + base + r * 32 + lane);
+        const unsigned ml = __ballot_sync(FULL, c.x > 0);
+        const unsigned mr = __ballot_sync(FULL, c.y > 0);
+        const unsigned mu = __ballot_sync(FULL, c.z > 0);
+        const unsigned md = __ballot_sync(FULL, c.w > 0);
+        const unsigned mn = __ballot_sync(FULL, e < 0);
+        const unsigned mp = __ballot_sync(FULL, e > 0);
+        if (lane == r) {
+            Rl = ml; Rr = mr; Ru = mu; Rd = md; neg = mn; pos = mp;
+        }
+        if (r == 0) e_row0 = e;
+        if (r == 31) e_row31 = e;
+    }
+}
+
+__device__ __forceinline__ int halo_level(const Batch &b, int nt, int px, bool from_exc) {
+    if (nt < 0) return INF_H;
+    const size_t q = (size_t)nt * TPX + px;
+    if (from_exc) return __ldcg(b.exc + q) < 0 ? 1 : INF_H;
+    return __ldcg(b.h + q);
+}
+
+// Exact distances of tile t given its halo; queues neighbours whose halo
+// (our border) decreased.  round0: heights of every tile are stale, so the
+// halo and "old" border values are derived from the excess instead.
+__device__ void gr_tile(const Batch &b, int t, bool round0, int tag_next, int slot_next, int *hs) {
+    const int lane = threadIdx.x & 31;
+    const TileGeo g = tile_geo(b, t);
+    const size_t base = (size_t)t * TPX;
+    unsigned Rl = 0, Rr = 0, Ru = 0, Rd = 0, neg = 0, pos = 0;
+    int e0 = 0, e31 = 0;
+    load_masks(b, base, Rl, Rr, Ru, Rd, neg, pos, e0, e31);
+    int o_top, o_bot, o_lft, o_rgt;
+    if (round0) {
+        o_top = e0 < 0 ? 1 : INF_H;
+        o_bot = e31 < 0 ? 1 : INF_H;
+        o_lft = (neg & 1u) ? 1 : INF_H;
+        o_rgt = (neg >> 31) ? 1 : INF_H;
+    } else {
+        o_top = __ldcg(b.h + base + lane);
+        o_bot = __ldcg(b.h + base + 31 * 32 + lane);
+        o_lft = __ldcg(b.h + base + lane * 32);
+        o_rgt = __ldcg(b.h + base + lane * 32 + 31);
+    }
+    const int ht = halo_level(b, g.nb[2], 31 * 32 + lane, round0);
+    const int hb = halo_level(b, g.nb[3], lane, round0);
+    const int hl = halo_level(b, g.nb[0], lane * 32 + 31, round0);
+    const int hr = halo_level(b, g.nb[1], lane * 32, round0);
+    tile_bfs(Rl, Rr, Ru, Rd, neg, hl, hr, ht, hb, hs, 33);
+    __syncwarp();
+#pragma unroll 4
+    for (int r = 0; r < 32; ++r) b.h[base + r * 32 + lane] = hs[r * 33 + lane];
+    const bool ch_top = __any_sync(FULL, hs[lane] != o_top);
+    const bool ch_bot = __any_sync(FULL, hs[31 * 33 + lane] != o_bot);
+    const bool ch_lft = __any_sync(FULL, hs[lane * 33] != o_lft);
+    const bool ch_rgt = __any_sync(FULL, hs[lane * 33 + 31] != o_rgt);
+    if (lane == 0 && ch_lft && g.nb[0] >= 0) enqueue(b, b.mark_gr, slot_next, tag_next, g.nb[0]);
+    if (lane == 1 && ch_rgt && g.nb[1] >= 0) enqueue(b, b.mark_gr, slot_next, tag_next, g.nb[1]);
+    if (lane == 2 && ch_top && g.nb[2] >= 0) enqueue(b, b.mark_gr, slot_next, tag_next, g.nb[2]);
+    if (lane == 3 && ch_bot && g.nb[3] >= 0) enqueue(b, b.mark_gr, slot_next, tag_next, g.nb[3]);
+    __syncwarp();
+}
+
+// Source-side reachability closure of tile t given the halo's reach bits.
+__device__ void reach_tile(const Batch &b, int t, bool round0, int tag_next, int slot_next) {
+    const int lane = threadIdx.x & 31;
+    const TileGeo g = tile_geo(b, t);
+    const size_t base = (size_t)t * TPX;
+    unsigned Rl = 0, Rr = 0, Ru = 0, Rd = 0, neg = 0, pos = 0;
+    int e0, e31;
+    load_masks(b, base, Rl, Rr, Ru, Rd, neg, pos, e0, e31);
+    const unsigned old = round0 ? 0u : __ldcg(b.reach + (size_t)t * 32 + lane);
+    // halo nodes that are reached and have residual capacity into the tile
+    unsigned Tin = 0, Bin = 0;
+    unsigned lbit = 0, rbit = 0;
+    if (g.nb[2] >= 0) {
+        const unsigned rr = __ldcg(b.reach + (size_t)g.nb[2] * 32 + 31);
+        const int4 c = __ldcg(b.cap + (size_t)g.nb[2] * TPX + 31 * 32 + lane);
+        Tin = rr & __ballot_sync(FULL, c.w > 0);
+    }
+    if (g.nb[3] >= 0) {
+        const unsigned rr = __ldcg(b.reach + (size_t)g.nb[3] * 32 + 0);
+        const int4 c = __ldcg(b.cap + (size_t)g.nb[3] * TPX + lane);
+        Bin = rr & __ballot_sync(FULL, c.z > 0);
+    }
+    if (g.nb[0] >= 0) {
+        const unsigned rr = __ldcg(b.reach + (size_t)g.nb[0] * 32 + lane);
+        const int4 c = __ldcg(b.cap + (size_t)g.nb[0] * TPX + lane * 32 + 31);
+        lbit = ((rr >> 31) & 1u) && c.y > 0 ? 1u : 0u;
+    }
+    if (g.nb[1] >= 0) {
+        const unsigned rr = __ldcg(b.reach + (size_t)g.nb[1] * 32 + lane);
+        const int4 c = __ldcg(b.cap + (size_t)g.nb[1] * TPX + lane * 32);
+        rbit = (rr & 1u) && c.x > 0 ? 0x80000000u : 0u;
+    }
+    unsigned S = pos | old;
+    for (int it = 0; it < BFS_MAX_ITERS; ++it) {
+        unsigned up = __shfl_up_sync(FULL, S & Rd, 1);
+        unsigned dn = __shfl_down_sync(FULL, S & Ru, 1);
+        if (lane == 0) up = Tin;
+        if (lane == 31) dn = Bin;
+        const unsigned nw = ((((S & Rr) << 1) | lbit) | (((S & Rl) >> 1) | rbit) | up | dn) & ~S;
+        if (!__any_sync(FULL, nw != 0)) break;
+        S |= nw;
+    }
+    b.reach[(size_t)t * 32 + lane] = S;
+    const unsigned fresh = S & ~old;
+    const bool out_l = __any_sync(FULL, (fresh & Rl & 1u) != 0);
+    const bool out_r = __any_sync(FULL, (fresh & Rr & 0x80000000u) != 0);
+    const bool out_u = __any_sync(FULL, lane == 0 && (fresh & Ru) != 0);
+    const bool out_d = __any_sync(FULL, lane == 31 && (fresh & Rd) != 0);
+    if (lane == 0 && out_l && g.nb[0] >= 0) enqueue(b, b.mark_gr, slot_next, tag_next, g.nb[0]);
+    if (lane == 1 && out_r && g.nb[1] >= 0) enqueue(b, b.mark_gr, slot_next, tag_next, g.nb[1]);
+    if (lane == 2 && out_u && g.nb[2] >= 0) enqueue(b, b.mark_gr, slot_next, tag_next, g.nb[2]);
+    if (lane == 3 && out_d && g.nb[3] >= 0) enqueue(b, b.mark_gr, slot_next, tag_next, g.nb[3]);
+}
+
+// ---------------------------------------------------------------------------
+// Push/relabel on one tile (whole block)
+// ---------------------------------------------------------------------------
+
+__device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int phase, SmemPush &s) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const TileGeo g = tile_geo(b, t);
+    const size_t base = (size_t)t * TPX;
+#pragma unroll
+    for (int k = 0; k < ROWS_PER_WARP; ++k) {
+        const int r = warp + 8 * k;
+        s.c[r][lane] = __ldcg(b.cap + base + r * 32 + lane);
+        s.e[r][lane] = __ldcg(b.exc + base + r * 32 + lane);
+        s.h[r + 1][lane + 1] = __ldcg(b.h + base + r * 32 + lane);
+    }
+    if (warp == 0) s.h[0][lane + 1] = g.nb[2] >= 0 ? __ldcg(b.h + (size_t)g.nb[2] * TPX + 31 * 32 + lane) : INF_H;
+    if (warp == 1) s.h[TILE_H + 1][lane + 1] = g.nb[3] >= 0 ? __ldcg(b.h + (size_t)g.nb[3] * TPX + lane) : INF_H;
+    if (warp == 2) s.h[lane + 1][0] = g.nb[0] >= 0 ? __ldcg(b.h + (size_t)g.nb[0] * TPX + lane * 32 + 31) : INF_H;
+    if (warp == 3) s.h[lane + 1][TILE_W + 1] = g.nb[1] >= 0 ? __ldcg(b.h + (size_t)g.nb[1] * TPX + lane * 32) : INF_H;
+    if (warp < 4) s.halo_in[warp][lane] = 0;
+    __syncthreads();
+
+    int any = 1;
+    for (int sw = 0; sw < prm.max_sweeps; ++sw) {
+        if (sw % prm.bfs_every == 0) {
+            // exact local relabel against the frozen halo
+#pragma unroll
+            for (int k = 0; k < ROWS_PER_WARP; ++k) {
+                const int r = warp + 8 * k;
+                const int4 c = s.c[r][lane];
+                const int e = s.e[r][lane];
+                const unsigned ml = __ballot_sync(FULL, c.x > 0);
+                const unsigned mr = __ballot_sync(FULL, c.y > 0);
+                const unsigned mu = __ballot_sync(FULL, c.z > 0);
+                const unsigned md = __ballot_sync(FULL, c.w > 0);
+                const unsigned mn = __ballot_sync(FULL, e < 0);
+                if (lane == 0) {
+                    s.m[0][r] = ml; s.m[1][r] = mr; s.m[2][r] = mu; s.m[3][r] = md; s.m[4][r] = mn;
+                }
+            }
+            __syncthreads();
+            if (warp == 0)
+                tile_bfs(s.m[0][lane], s.m[1][lane], s.m[2][lane], s.m[3][lane], s.m[4][lane],
+                         s.h[lane + 1][0], s.h[lane + 1][TILE_W + 1], s.h[0][lane + 1],
+                         s.h[TILE_H + 1][lane + 1], &s.h[1][1], TILE_W + 2);
+            __syncthreads();
+        }
+        // ---- push phase: heights fixed ----
+#pragma unroll
+        for (int k = 0; k < ROWS_PER_WARP; ++k) {
+            const int r = warp + 8 * k;
+            int e = s.e[r][lane];
+            const int hh = s.h[r + 1][lane + 1];
+            if (e > 0 && hh < INF_H) {
+                const int4 c = s.c[r][lane];
+                const int e0 = e;
+                if (c.x > 0 && hh == s.h[r + 1][lane] + 1) {
+                    const int f = min(e, c.x);
+                    e -= f;
+                    s.c[r][lane].x = c.x - f;
+                    if (lane > 0) { s.c[r][lane - 1].y += f; atomicAdd(&s.e[r][lane - 1], f); }
+                    else atomicAdd(&s.halo_in[0][r], f);
+                }
+                if (e > 0 && c.y > 0 && hh == s.h[r + 1][lane + 2] + 1) {
+                    const int f = min(e, c.y);
+                    e -= f;
+                    s.c[r][lane].y = c.y - f;
+                    if (lane < TILE_W - 1) { s.c[r][lane + 1].x += f; atomicAdd(&s.e[r][lane + 1], f); }
+                    else atomicAdd(&s.halo_in[1][r], f);
+                }
+                if (e > 0 && c.z > 0 && hh == s.h[r][lane + 1] + 1) {
+                    const int f = min(e, c.z);
+                    e -= f;
+                    s.c[r][lane].z = c.z - f;
+                    if (r > 0) { s.c[r - 1][lane].w += f; atomicAdd(&s.e[r - 1][lane], f); }
+                    else atomicAdd(&s.halo_in[2][lane], f);
+                }
+                if (e > 0 && c.w > 0 && hh == s.h[r + 2][lane + 1] + 1) {
+                    const int f = min(e, c.w);
+                    e -= f;
+                    s.c[r][lane].w = c.w - f;
+                    if (r < TILE_H - 1) { s.c[r + 1][lane].z += f; atomicAdd(&s.e[r + 1][lane], f); }
+                    else atomicAdd(&s.halo_in[3][lane], f);
+                }
+                if (e != e0) atomicSub(&s.e[r][lane], e0 - e);
+            }
+        }
+        __syncthreads();
+        // ---- relabel phase: capacities and excess fixed ----
+        int act = 0;
+#pragma unroll
+        for (int k = 0; k < ROWS_PER_WARP; ++k) {
+            const int r = warp + 8 * k;
+            const int e = s.e[r][lane];
+            int hh = s.h[r + 1][lane + 1];
+            if (e > 0 && hh < INF_H) {
+                const int4 c = s.c[r][lane];
+                int m = INF_H;
+                if (c.x > 0) m = min(m, s.h[r + 1][lane]);
+                if (c.y > 0) m = min(m, s.h[r + 1][lane + 2]);
+                if (c.z > 0) m = min(m, s.h[r][lane + 1]);
+                if (c.w > 0) m = min(m, s.h[r + 2][lane + 1]);
+                if (m >= hh) {
+                    hh = m >= INF_H - 1 ? INF_H : m + 1;
+                    s.h[r + 1][lane + 1] = hh;
+                }
+                act |= hh < INF_H;
+            }
+        }
+        any = __syncthreads_or(act);
+        if (!any) break;
+    }
+    // ---- write back ----
+#pragma unroll
+    for (int k = 0; k < ROWS_PER_WARP; ++k) {
+        const int r = warp + 8 * k;
+        b.cap[base + r * 32 + lane] = s.c[r][lane];
+        b.exc[base + r * 32 + lane] = s.e[r][lane];
+        b.h[base + r * 32 + lane] = s.h[r + 1][lane + 1];
+    }
+    // ---- hand halo flow to the (idle) neighbour tiles ----
+    if (warp < 4) {
+        const int f = s.halo_in[warp][lane];
+        const int nt = warp == 0 ? g.nb[0] : warp == 1 ? g.nb[1] : warp == 2 ? g.nb[2] : g.nb[3];
+        bool sent = false;
+        if (f && nt >= 0) {
+            int px, comp;
+            if (warp == 0) { px = lane * 32 + 31; comp = 1; }       // left tile, its RIGHT edge
+            else if (warp == 1) { px = lane * 32; comp = 0; }       // right tile, its LEFT edge
+            else if (warp == 2) { px = 31 * 32 + lane; comp = 3; }  // upper tile, its DOWN edge
+            else { px = lane; comp = 2; }                           // lower tile, its UP edge
+            const size_t q = (size_t)nt * TPX + px;
+            atomicAdd(b.exc + q, f);
+            atomicAdd(reinterpret_cast<int *>(b.cap + q) + comp, f);
+            sent = true;
+        }
+        if (__any_sync(FULL, sent) && lane == 0)
+            enqueue(b, b.mark_push, (phase + 1) % 3, phase + 1, nt);
+    }
+    if (any && threadIdx.x == 0) enqueue(b, b.mark_push, (phase + 2) % 3, phase + 2, t);
+}
+
+// ---------------------------------------------------------------------------
+// The persistent solve kernel
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(TILE_THREADS, 2) k_solve(Batch b, SolveParams prm) {
+    __shared__ Smem sm;
+    Ctl *ctl = b.ctl;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gwarp = blockIdx.x * 8 + warp, nwarps = gridDim.x * 8;
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+
+    // fresh de-duplication marks and reach bits for this solve
+    for (int t = gtid; t < b.n_tiles; t += nthreads) {
+        b.mark_push[t] = -1;
+        b.mark_gr[t] = -1;
+    }
+    for (size_t i = gtid; i < (size_t)b.n_tiles * 32; i += nthreads) b.reach[i] = 0;
+    if (!grid_sync(b, 0)) return;
+
+    int P = 0;  // push phase counter (even at the start of every outer iteration)
+    int G = 0;  // global relabel round counter (tags of the tile frontier)
+    bool finished = false;
+    for (int outer = 0; outer < prm.max_outer; ++outer) {
+        // ------------------------ exact global relabel ------------------------
+        for (int i = gtid; i < b.n_img; i += nthreads)
+            if (!b.ist[i].done) {
+                b.ist[i].pos_excess = 0;
+                b.ist[i].active = 0;
+            }
+        if (gtid == 0) ctl->total_active = 0;
+        for (int t = gwarp; t < b.n_tiles; t += nwarps) {
+            if (vload(&b.ist[__ldg(b.tile_img + t)].done)) continue;
+            gr_tile(b, t, true, G + 1, L_GR0 + ((G + 1) & 1), sm.w.hs[warp]);
+            if (lane == 0) atomicAdd(&ctl->gr_tiles, 1ull);
+        }
+        if (!grid_sync(b, (1u << L_PUSH0) | (1u << L_PUSH1) | (1u << L_PUSH2))) return;
+        ++G;
+        for (int k = 1;; ++k) {
+            const int slot = L_GR0 + (G & 1);
+            const int n = vload(&ctl->size[slot]);
+            if (n == 0) break;
+            if (k > prm.max_rounds) {
+                if (gtid == 0) set_error(b, ERRC_GR_ROUNDS);
+                return;
+            }
+            for (;;) {
+                int idx = 0;
+                if (lane == 0) idx = atomicAdd(&ctl->take[slot], 1);
+                idx = __shfl_sync(FULL, idx, 0);
+                if (idx >= n) break;
+                const int t = b.lists[(size_t)slot * b.list_cap + idx];
+                gr_tile(b, t, false, G + 1, L_GR0 + ((G + 1) & 1), sm.w.hs[warp]);
+                if (lane == 0) atomicAdd(&ctl->gr_tiles, 1ull);
+            }
+            if (!grid_sync(b, 1u << slot)) return;
+            ++G;
+            if (gtid == 0) ctl->gr_rounds++;
+        }
+        // ------------------------ count active nodes ------------------------
+        for (int t = gwarp; t < b.n_tiles; t += nwarps) {
+            const int img = __ldg(b.tile_img + t);
+            if (vload(&b.ist[img].done)) continue;
+            const size_t base = (size_t)t * TPX;
+            unsigned long long pos = 0;
+            int nact = 0;
+#pragma unroll 4
+            for (int r = 0; r < 32; ++r) {
+                const int e = __ldcg(b.exc + base + r * 32 + lane);
+                const int hh = __ldcg(b.h + base + r * 32 + lane);
+                if (e > 0) pos += (unsigned)e;
+                nact += __popc(__ballot_sync(FULL, e > 0 && hh < INF_H));
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) pos += __shfl_down_sync(FULL, pos, o);
+            if (lane == 0) {
+                if (pos) atomicAdd(&b.ist[img].pos_excess, pos);
+                if (nact) {
+                    atomicAdd(&b.ist[img].active, (unsigned long long)nact);
+                    atomicAdd(&ctl->total_active, (unsigned long long)nact);
+                    const TileGeo g = tile_geo(b, t);
+                    enqueue(b, b.mark_push, (P + g.color) % 3, P + g.color, t);
+                }
+            }
+        }
+        if (!grid_sync(b, 0)) return;
+        if (gtid == 0) {
+            ctl->global_relabels++;
+            ctl->outer_iters = outer + 1;
+        }
+        const unsigned long long total = *(volatile unsigned long long *)&ctl->total_active;
+        for (int i = gtid; i < b.n_img; i += nthreads)
+            if (!b.ist[i].done && *(volatile unsigned long long *)&b.ist[i].active == 0) b.ist[i].done = 1;
+        if (total == 0) {
+            finished = true;
+            break;
+        }
+        // ------------------------ checkerboard push rounds ------------------------
+        int last = P;
+        for (int r = 0; r < prm.push_rounds; ++r) {
+            bool more = true;
+            for (int c = 0; c < 2; ++c) {
+                const int p = P + 2 * r + c;
+                const int slot = p % 3;
+                last = p;
+                const int n = vload(&ctl->size[slot]);
+                for (;;) {
+                    if (threadIdx.x == 0) sm.p.idx = atomicAdd(&ctl->take[slot], 1);
+                    __syncthreads();
+                    const int idx = sm.p.idx;
+                    __syncthreads();
+                    if (idx >= n) break;
+                    push_tile(b, b.lists[(size_t)slot * b.list_cap + idx], prm, p, sm.p);
+                    if (threadIdx.x == 0) atomicAdd(&ctl->push_tiles, 1ull);
+                    __syncthreads();
+                }
+                if (!grid_sync(b, 1u << slot)) return;
+                if (gtid == 0) ctl->push_phases++;
+                if (vload(&ctl->size[(p + 1) % 3]) == 0 && vload(&ctl->size[(p + 2) % 3]) == 0) {
+                    more = false;
+                    break;
+                }
+            }
+            if (!more) break;
+        }
+        P = (last + 3) & ~1;
+    }
+    if (!finished) {
+        if (gtid == 0) set_error(b, ERRC_OUTER);
+        return;
+    }
+    // ------------------------ source-side reachability ------------------------
+    for (int t = gwarp; t < b.n_tiles; t += nwarps) reach_tile(b, t, true, G + 1, L_GR0 + ((G + 1) & 1));
+    if (!grid_sync(b, 0)) return;
+    ++G;
+    for (int k = 1;; ++k) {
+        const int slot = L_GR0 + (G & 1);
+        const int n = vload(&ctl->size[slot]);
+        if (n == 0) break;
+        if (k > prm.max_rounds) {
+            if (gtid == 0) set_error(b, ERRC_REACH_ROUNDS);
+            return;
+        }
+        for (;;) {
+            int idx = 0;
+            if (lane == 0) idx = atomicAdd(&ctl->take[slot], 1);
+            idx = __shfl_sync(FULL, idx, 0);
+            if (idx >= n) break;
+            reach_tile(b, b.lists[(size_t)slot * b.list_cap + idx], false, G + 1, L_GR0 + ((G + 1) & 1));
+            if (lane == 0) atomicAdd(&ctl->reach_tiles, 1ull);
+        }
+        if (!grid_sync(b, 1u << slot)) return;
+        ++G;
+        if (gtid == 0) ctl->reach_rounds++;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Build and extraction kernels (one block per tile)
+// ---------------------------------------------------------------------------
+
+// Residual graph of image 0 from caller arrays (GC_SetGraph).  Follows
+// InitGraph / InitGraphVarEdges (GraphCutKernels.cu:112-214): interior nodes
+// only, caps that point into the 1-pixel border zeroed, excess = dp - dn.
+__global__ void __launch_bounds__(TILE_THREADS) k_build_arrays(Batch b, const int *__restrict__ dp,
+                                                                const int *__restrict__ dn, int penalty,
+                                                                const int *__restrict__ up,
+                                                                const int *__restrict__ down,
+                                                                const int *__restrict__ left,
+                                                                const int *__restrict__ right) {
+    const int t = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const TileGeo g = tile_geo(b, t);
+    const int W = b.img[g.img].W, H = b.img[g.img].H;
+    unsigned long long idp = 0, rinit = 0;
+    int bad = 0;
+    const long long w32 = (long long)((W + 31) / 32) * 32;
+#pragma unroll
+    for (int k = 0; k < ROWS_PER_WARP; ++k) {
+        const int r = warp + 8 * k;
+        const int x = g.tx * TILE_W + lane, y = g.ty * TILE_H + r;
+        int4 c = make_int4(0, 0, 0, 0);
+        int e = 0;
+        if (x < W && y < H) {
+            const size_t i = (size_t)y * W + x;
+            const int vdp = dp[i];
+            // the reference sums max(dp,0) over padded positions x + y*W32 < W*H
+            // (GraphCut.cu:359-376, GraphCutKernels.cu:883-898)
+            if ((long long)x + (long long)y * w32 < (long long)W * H && vdp > 0) rinit += (unsigned)vdp;
+            if (x > 0 && y > 0 && x < W - 1 && y < H - 1) {
+                const int vdn = dn[i];
+                c = up ? make_int4(left[i], right[i], up[i], down[i])
+                       : make_int4(penalty, penalty, penalty, penalty);
+                bad |= (vdp < 0) | (vdn < 0) | (vdp > GCFG_MAX_CAP) | (vdn > GCFG_MAX_CAP) | (c.x < 0) |
+                       (c.y < 0) | (c.z < 0) | (c.w < 0) | (c.x > GCFG_MAX_CAP) | (c.y > GCFG_MAX_CAP) |
+                       (c.z > GCFG_MAX_CAP) | (c.w > GCFG_MAX_CAP);
+                if (x == 1) c.x = 0;
+                if (x == W - 2) c.y = 0;
+                if (y == 1) c.z = 0;
+                if (y == H - 2) c.w = 0;
+                e = vdp - vdn;
+                idp += (unsigned long long)(long long)vdp;
+            }
+        }
+        const size_t p = (size_t)t * TPX + r * 32 + lane;
+        b.cap[p] = c;
+        b.exc[p] = e;
+    }
+    if (bad) set_error(b, 100);
+    warp_atomic_add_u64(&b.ist[g.img].interior_dp, idp);
+    warp_atomic_add_u64(&b.ist[g.img].ref_init, rinit);
+}
+
+// Labels of every image, row-major, at each image's pix0 offset:
+// smin = source-reachable, smax = interior and cannot reach the sink,
+// label = smax as int32 (the reference's GC_Optimize output).
+__global__ void __launch_bounds__(TILE_THREADS) k_extract(Batch b, uint8_t *smin, uint8_t *smax,
+                                                           int *label) {
+    const int t = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const TileGeo g = tile_geo(b, t);
+    const int W = b.img[g.img].W, H = b.img[g.img].H;
+    const long long pix0 = b.img[g.img].pix0;
+#pragma unroll
+    for (int k = 0; k < ROWS_PER_WARP; ++k) {
+        const int r = warp + 8 * k;
+        const int x = g.tx * TILE_W + lane, y = g.ty * TILE_H + r;
+        if (x >= W || y >= H) continue;
+        const size_t p = (size_t)t * TPX + r * 32 + lane;
+        const size_t i = (size_t)pix0 + (size_t)y * W + x;
+        const bool inside = x > 0 && y > 0 && x < W - 1 && y < H - 1;
+        const uint8_t sm = inside && b.h[p] >= INF_H;
+        if (smin) smin[i] = (uint8_t)((b.reach[(size_t)t * 32 + r] >> lane) & 1u);
+        if (smax) smax[i] = sm;
+        if (label) label[i] = sm;
+    }
+}
+
+}  // namespace gcfg
+
+namespace gcfg {
+
+int solve_grid_blocks(int n_tiles) {
+    static int cached = 0;
+    if (!cached) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve, TILE_THREADS, 0);
+        cached = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+    }
+    // half the tiles run in a push phase; more blocks than that only make
+    // the grid barrier slower
+    const int want = (n_tiles + 1) / 2;
+    return want < 1 ? 1 : (want < cached ? want : cached);
+}
+
+gcfg_status launch_solve(const Batch &b, const SolveParams &prm, int n_tiles, cudaStream_t st) {
+    const int grid = solve_grid_blocks(n_tiles);
+    Batch bb = b;
+    SolveParams pp = prm;
+    void *args[] = {&bb, &pp};
+    prof_begin(st);
+    const cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_solve, dim3(grid), dim3(TILE_THREADS),
+                                                      args, 0, st);
+    prof_end(GCFG_PK_SOLVE, st);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return e == cudaSuccess ? GCFG_OK : GCFG_ERR_CUDA;
+}
+
+gcfg_status launch_build_arrays(const Batch &b, const int *dp, const int *dn, int penalty, const int *up,
+                                const int *down, const int *left, const int *right, cudaStream_t st) {
+    GCFG_LAUNCH(GCFG_PK_BUILD, st,
+                k_build_arrays<<<b.n_tiles, TILE_THREADS, 0, st>>>(b, dp, dn, penalty, up, down, left, right));
+    GCFG_CK(cudaGetLastError());
+    return GCFG_OK;
+}
+
+gcfg_status launch_extract(const Batch &b, uint8_t *smin, uint8_t *smax, int *label, cudaStream_t st) {
+    GCFG_LAUNCH(GCFG_PK_EXTRACT, st, k_extract<<<b.n_tiles, TILE_THREADS, 0, st>>>(b, smin, smax, label));
+    GCFG_CK(cudaGetLastError());
+    return GCFG_OK;
+}
+
+}  // namespace gcfg

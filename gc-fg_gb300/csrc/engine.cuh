@@ -1,0 +1,104 @@
+// engine.cuh -- the tile-space max-flow engine (batched, device-driven).
+//
+// Every image of a batch is cut into 32x32 tiles.  All tiles of all images
+// live in one tile-major arena: tile t owns pixel slots [t*1024, t*1024+1024)
+// in row-major order inside the tile, so a tile is 16 KB of capacities plus
+// 4 KB of excess plus 4 KB of heights, contiguous in HBM.  Tiles of one image
+// are consecutive and row-major, so a tile's neighbours are t-1, t+1,
+// t-tiles_x, t+tiles_x.  A batch is one big graph whose components are the
+// images; one image is a batch of one.
+//
+// The whole solve (global relabels, checkerboard push rounds, termination,
+// source-side reachability) runs in ONE persistent cooperative kernel that
+// takes its work from device queues of tiles and synchronises with a bounded
+// grid barrier, so the host never waits inside a solve.
+#pragma once
+
+#include "gcfg_internal.cuh"
+
+namespace gcfg {
+
+constexpr int TPX = TILE_W * TILE_H;  // pixels per tile
+
+// Immutable description of one image of a batch (uploaded by the host).
+struct ImgDesc {
+    int W, H, tiles_x, tiles_y;
+    int tile0, n_tiles;
+    long long pix0;   // offset of the image in packed row-major inputs/outputs
+    double lambda;
+};
+
+// Per-image state written by the device.
+struct ImgState {
+    unsigned long long interior_dp;  // sum of dp over interior pixels
+    unsigned long long ref_init;     // reference's initial energy (int32 wrap)
+    unsigned long long pos_excess;   // sum of positive excess (last count)
+    unsigned long long active;       // active nodes (last count)
+    unsigned long long sigma_sum;    // sum of ||dI||^2 over neighbour pairs
+    int done;
+    int d2lim;                       // n-link table length - 1
+    int pad[2];
+};
+
+enum { L_PUSH0 = 0, L_PUSH1, L_PUSH2, L_GR0, L_GR1, L_NLISTS };
+
+// Control block of one solve (zeroed before every launch).
+struct Ctl {
+    unsigned bar_count;
+    unsigned bar_gen;
+    int err;          // nonzero: a barrier timed out or an iteration cap was hit
+    int err_code;
+    int size[L_NLISTS];
+    int take[L_NLISTS];
+    unsigned long long total_active;
+    unsigned long long push_tiles, gr_tiles, reach_tiles;
+    int gr_rounds, push_phases, reach_rounds, outer_iters;
+    int global_relabels;
+    int pad[3];
+};
+
+struct Batch {
+    int n_img, n_tiles;
+    const ImgDesc *img;
+    ImgState *ist;
+    const int *tile_img;
+    int4 *cap;
+    int *exc;
+    int *h;
+    unsigned *reach;         // 32 row masks per tile (source-side reachability)
+    int *lists;              // L_NLISTS work queues of tile indices, list_cap each
+    int list_cap;
+    int *mark_push, *mark_gr;
+    Ctl *ctl;
+};
+
+struct SolveParams {
+    int max_outer;     // outer iterations (global relabel + push rounds)
+    int push_rounds;   // checkerboard rounds between global relabels
+    int max_sweeps;    // push/relabel sweeps per tile visit
+    int bfs_every;     // exact local relabel every this many sweeps
+    int max_rounds;    // cap on BFS rounds of one global relabel / reach pass
+};
+
+// Error codes in Ctl::err_code.
+enum {
+    ERRC_BARRIER = 1,
+    ERRC_GR_ROUNDS = 2,
+    ERRC_OUTER = 3,
+    ERRC_REACH_ROUNDS = 4,
+    ERRC_HEIGHT_DECREASE = 5,
+    ERRC_QUEUE = 6
+};
+
+}  // namespace gcfg
+
+namespace gcfg {
+
+// Host launchers (engine.cu).
+int solve_grid_blocks(int n_tiles);
+gcfg_status launch_solve(const Batch &b, const SolveParams &prm, int n_tiles, cudaStream_t st);
+gcfg_status launch_build_arrays(const Batch &b, const int *dp, const int *dn, int penalty, const int *up,
+                                const int *down, const int *left, const int *right, cudaStream_t st);
+gcfg_status launch_extract(const Batch &b, uint8_t *smin, uint8_t *smax, int *label, cudaStream_t st);
+
+}  // namespace gcfg

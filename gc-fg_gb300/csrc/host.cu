@@ -1,0 +1,632 @@
+// host.cu -- the engine's host side and the C ABI (include/gcfg.h).
+//
+// An Engine owns the device buffers of one batch (tile arena, queues,
+// per-image tables) sized for a capacity that only grows, uploads the batch
+// layout, and runs: data term -> build -> persistent solve -> extraction,
+// all on one stream.  The reference-facing graph API, the one-image
+// segmenter and the batch API are thin layers over it.
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "dataterm.cuh"
+#include "engine.cuh"
+
+namespace gcfg {
+
+template <typename T>
+static gcfg_status grow(T *&p, size_t &cap, size_t need) {
+    if (need <= cap && p) return GCFG_OK;
+    cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t n = need < 1 ? 1 : need;
+    if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return GCFG_ERR_OOM;
+    cap = n;
+    return GCFG_OK;
+}
+
+template <typename T>
+static gcfg_status grow_host(T *&p, size_t &cap, size_t need) {
+    if (need <= cap && p) return GCFG_OK;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    size_t n = need < 1 ? 1 : need;
+    if (cudaMallocHost(&p, n * sizeof(T)) != cudaSuccess) return GCFG_ERR_OOM;
+    cap = n;
+    return GCFG_OK;
+}
+
+struct Engine {
+    cudaStream_t st = nullptr;
+    SolveParams prm{64, 4, 64, 16, 1 << 20};
+
+    int n_img = 0, n_tiles = 0;
+    long long n_px = 0, total_chunks = 0;
+
+    // device
+    ImgDesc *d_img = nullptr; size_t c_img = 0;
+    ImgState *d_ist = nullptr; size_t c_ist = 0;
+    long long *d_chunk = nullptr; size_t c_chunk = 0;
+    int *d_tile_img = nullptr; size_t c_timg = 0;
+    int4 *d_cap = nullptr; size_t c_cap = 0;
+    int *d_exc = nullptr; size_t c_exc = 0;
+    int *d_h = nullptr; size_t c_h = 0;
+    unsigned *d_reach = nullptr; size_t c_reach = 0;
+    int *d_lists = nullptr; size_t c_lists = 0; int list_cap = 0;
+    int *d_mpush = nullptr; size_t c_mpush = 0;
+    int *d_mgr = nullptr; size_t c_mgr = 0;
+    Ctl *d_ctl = nullptr; size_t c_ctl = 0;
+    int *d_hist = nullptr; size_t c_hist = 0;
+    int *d_dpl = nullptr; size_t c_dpl = 0;
+    int *d_dnl = nullptr; size_t c_dnl = 0;
+    double *d_raw = nullptr; size_t c_raw = 0;
+    int *d_wlut = nullptr; size_t c_wlut = 0;
+    // staging for host entry points
+    uint8_t *d_rgb = nullptr; size_t c_rgb = 0;
+    uint8_t *d_scrib = nullptr; size_t c_scrib = 0;
+    uint8_t *d_smin = nullptr; size_t c_smin = 0;
+    uint8_t *d_smax = nullptr; size_t c_smax = 0;
+    // host (pinned)
+    ImgDesc *h_img = nullptr; size_t ch_img = 0;
+    ImgState *h_ist = nullptr; size_t ch_ist = 0;
+    long long *h_chunk = nullptr; size_t ch_chunk = 0;
+    int *h_tile_img = nullptr; size_t ch_timg = 0;
+    Ctl *h_ctl = nullptr; size_t ch_ctl = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    ~Engine() { release(); }
+
+    void release() {
+        cudaFree(d_img); cudaFree(d_ist); cudaFree(d_chunk); cudaFree(d_tile_img);
+        cudaFree(d_cap); cudaFree(d_exc); cudaFree(d_h); cudaFree(d_reach);
+        cudaFree(d_lists);
+        cudaFree(d_mpush); cudaFree(d_mgr); cudaFree(d_ctl);
+        cudaFree(d_hist); cudaFree(d_dpl); cudaFree(d_dnl); cudaFree(d_raw); cudaFree(d_wlut);
+        cudaFree(d_rgb); cudaFree(d_scrib); cudaFree(d_smin); cudaFree(d_smax);
+        if (h_img) cudaFreeHost(h_img);
+        if (h_ist) cudaFreeHost(h_ist);
+        if (h_chunk) cudaFreeHost(h_chunk);
+        if (h_tile_img) cudaFreeHost(h_tile_img);
+        if (h_ctl) cudaFreeHost(h_ctl);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        d_img = nullptr; d_ist = nullptr; d_chunk = nullptr; d_tile_img = nullptr;
+        d_cap = nullptr; d_exc = nullptr; d_h = nullptr; d_reach = nullptr;
+        d_lists = nullptr;
+        d_mpush = d_mgr = nullptr; d_ctl = nullptr;
+        d_hist = d_dpl = d_dnl = nullptr; d_raw = nullptr; d_wlut = nullptr;
+        d_rgb = d_scrib = d_smin = d_smax = nullptr;
+        h_img = nullptr; h_ist = nullptr; h_chunk = nullptr; h_tile_img = nullptr; h_ctl = nullptr;
+        ev0 = ev1 = nullptr;
+    }
+
+    gcfg_status init() {
+        GCFG_CK(cudaEventCreate(&ev0));
+        GCFG_CK(cudaEventCreate(&ev1));
+        GCFG_TRY(grow(d_ctl, c_ctl, 1));
+        GCFG_TRY(grow_host(h_ctl, ch_ctl, 1));
+        return GCFG_OK;
+    }
+
+    // Sizes of a batch -> tile count (no allocation).
+    static void count(int n, const int *W, const int *H, int &tiles, long long &px) {
+        tiles = 0;
+        px = 0;
+        for (int i = 0; i < n; ++i) {
+            tiles += div_up(W[i], TILE_W) * div_up(H[i], TILE_H);
+            px += (long long)W[i] * H[i];
+        }
+    }
+
+    gcfg_status reserve(int imgs, int tiles, long long px, bool dataterm, bool staging, bool arena = true) {
+        GCFG_TRY(grow(d_img, c_img, imgs));
+        GCFG_TRY(grow(d_ist, c_ist, imgs));
+        GCFG_TRY(grow(d_chunk, c_chunk, (size_t)imgs + 1));
+        if (arena) {
+            GCFG_TRY(grow(d_tile_img, c_timg, tiles));
+            GCFG_TRY(grow(d_cap, c_cap, (size_t)tiles * TPX));
+            GCFG_TRY(grow(d_exc, c_exc, (size_t)tiles * TPX));
+            GCFG_TRY(grow(d_h, c_h, (size_t)tiles * TPX));
+            GCFG_TRY(grow(d_reach, c_reach, (size_t)tiles * 32));
+            if ((size_t)tiles > (size_t)list_cap || !d_lists) {
+                GCFG_TRY(grow(d_lists, c_lists, (size_t)L_NLISTS * tiles));
+                list_cap = tiles;
+            }
+            GCFG_TRY(grow(d_mpush, c_mpush, tiles));
+            GCFG_TRY(grow(d_mgr, c_mgr, tiles));
+        }
+        GCFG_TRY(grow_host(h_img, ch_img, imgs));
+        GCFG_TRY(grow_host(h_ist, ch_ist, imgs));
+        GCFG_TRY(grow_host(h_chunk, ch_chunk, (size_t)imgs + 1));
+        if (arena) GCFG_TRY(grow_host(h_tile_img, ch_timg, tiles));
+        if (dataterm) {
+            GCFG_TRY(grow(d_hist, c_hist, (size_t)imgs * 2 * NBINS));
+            GCFG_TRY(grow(d_dpl, c_dpl, (size_t)imgs * NBINS));
+            GCFG_TRY(grow(d_dnl, c_dnl, (size_t)imgs * NBINS));
+            GCFG_TRY(grow(d_wlut, c_wlut, (size_t)imgs * WLUT_STRIDE));
+        }
+        if (staging) {
+            GCFG_TRY(grow(d_rgb, c_rgb, (size_t)px * 3));
+            GCFG_TRY(grow(d_scrib, c_scrib, (size_t)px));
+            GCFG_TRY(grow(d_smin, c_smin, (size_t)px));
+            GCFG_TRY(grow(d_smax, c_smax, (size_t)px));
+        }
+        return GCFG_OK;
+    }
+
+    // Lay out a batch: descriptors, tile -> image map, chunk offsets; upload.
+    gcfg_status layout(int n, const int *W, const int *H, const double *lam, bool dataterm, bool staging,
+                       bool arena = true) {
+        if (n < 1) return GCFG_ERR_INVALID;
+        for (int i = 0; i < n; ++i) {
+            if (W[i] < 1 || H[i] < 1 || (long long)W[i] * H[i] > (1LL << 31) - 1) return GCFG_ERR_INVALID;
+            if (lam && !(lam[i] >= 0.0 && lam[i] * 1.0000001 + 1 <= (double)GCFG_MAX_CAP)) return GCFG_ERR_INVALID;
+        }
+        int tiles;
+        long long px;
+        count(n, W, H, tiles, px);
+        if ((long long)tiles * TPX > (1LL << 40)) return GCFG_ERR_INVALID;
+        GCFG_TRY(reserve(n, tiles, px, dataterm, staging, arena));
+        int t = 0;
+        long long p = 0, ch = 0;
+        for (int i = 0; i < n; ++i) {
+            ImgDesc &d = h_img[i];
+            d.W = W[i];
+            d.H = H[i];
+            d.tiles_x = div_up(W[i], TILE_W);
+            d.tiles_y = div_up(H[i], TILE_H);
+            d.tile0 = t;
+            d.n_tiles = d.tiles_x * d.tiles_y;
+            d.pix0 = p;
+            d.lambda = lam ? lam[i] : 0.0;
+            if (arena)
+                for (int k = 0; k < d.n_tiles; ++k) h_tile_img[t + k] = i;
+            h_chunk[i] = ch;
+            t += d.n_tiles;
+            p += (long long)W[i] * H[i];
+            ch += ((long long)W[i] * H[i] + CHUNK_PX - 1) / CHUNK_PX;
+        }
+        h_chunk[n] = ch;
+        n_img = n;
+        n_tiles = t;
+        n_px = p;
+        total_chunks = ch;
+        GCFG_CK(cudaMemcpyAsync(d_img, h_img, n * sizeof(ImgDesc), cudaMemcpyHostToDevice, st));
+        GCFG_CK(cudaMemcpyAsync(d_chunk, h_chunk, (n + 1) * sizeof(long long), cudaMemcpyHostToDevice, st));
+        if (arena)
+            GCFG_CK(cudaMemcpyAsync(d_tile_img, h_tile_img, (size_t)t * sizeof(int), cudaMemcpyHostToDevice, st));
+        GCFG_CK(cudaMemsetAsync(d_ist, 0, n * sizeof(ImgState), st));
+        return GCFG_OK;
+    }
+
+    Batch batch() const {
+        Batch b;
+        b.n_img = n_img;
+        b.n_tiles = n_tiles;
+        b.img = d_img;
+        b.ist = d_ist;
+        b.tile_img = d_tile_img;
+        b.cap = d_cap;
+        b.exc = d_exc;
+        b.h = d_h;
+        b.reach = d_reach;
+        b.lists = d_lists;
+        b.list_cap = list_cap;
+        b.mark_push = d_mpush;
+        b.mark_gr = d_mgr;
+        b.ctl = d_ctl;
+        return b;
+    }
+
+    DtArgs dt(const uint8_t *rgb, const uint8_t *scrib) const {
+        DtArgs a;
+        a.n_img = n_img;
+        a.total_chunks = total_chunks;
+        a.rgb = rgb;
+        a.scrib = scrib;
+        a.img = d_img;
+        a.ist = d_ist;
+        a.chunk_off = d_chunk;
+        a.hist = d_hist;
+        a.dp_lut = d_dpl;
+        a.dn_lut = d_dnl;
+        a.raw_dp = nullptr;
+        a.raw_dn = nullptr;
+        a.wlut = d_wlut;
+        return a;
+    }
+
+    gcfg_status build_images(const uint8_t *rgb, const uint8_t *scrib) {
+        DtArgs a = dt(rgb, scrib);
+        GCFG_TRY(dt_tables(a, st));
+        return dt_build(batch(), a, st);
+    }
+
+    gcfg_status solve() {
+        GCFG_CK(cudaMemsetAsync(d_ctl, 0, sizeof(Ctl), st));
+        return launch_solve(batch(), prm, n_tiles, st);
+    }
+
+    // Read the per-image states and the control block (synchronises).
+    gcfg_status fetch() {
+        GCFG_CK(cudaMemcpyAsync(h_ist, d_ist, n_img * sizeof(ImgState), cudaMemcpyDeviceToHost, st));
+        GCFG_CK(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+        GCFG_CK(cudaStreamSynchronize(st));
+        return GCFG_OK;
+    }
+
+    gcfg_status status() const {
+        if (h_ctl->err) return GCFG_ERR_NOT_CONVERGED;
+        return GCFG_OK;
+    }
+
+    void result(int i, gcfg_result *r, float ms) const {
+        memset(r, 0, sizeof(*r));
+        const ImgState &s = h_ist[i];
+        r->flow = (long long)s.interior_dp - (long long)s.pos_excess;
+        r->ref_energy = (int32_t)((uint32_t)s.ref_init - (uint32_t)s.pos_excess);
+        r->status = status();
+        r->global_relabels = h_ctl->global_relabels;
+        r->gr_sweeps = h_ctl->gr_rounds;
+        r->push_rounds = h_ctl->push_phases;
+        r->cut_sweeps = h_ctl->reach_rounds;
+        r->active_after_first_gr = 0;
+        r->push_tiles = (long long)h_ctl->push_tiles;
+        r->gr_tiles = (long long)h_ctl->gr_tiles;
+        r->ms = ms;
+    }
+};
+
+std::atomic<long long> g_launches{0};
+
+}  // namespace gcfg
+
+using namespace gcfg;
+
+// ---------------------------------------------------------------------------
+// Graph API (drop-in for GraphCut.cu)
+// ---------------------------------------------------------------------------
+
+struct gcfg_graph {
+    Engine e;
+    int W = 0, H = 0;
+    const int32_t *dp = nullptr, *dn = nullptr;
+    const int32_t *up = nullptr, *down = nullptr, *left = nullptr, *right = nullptr;
+    int32_t penalty = 0;
+    bool varying = false;
+    bool built = false;
+    bool solved = false;
+    int32_t *d_label = nullptr;
+};
+
+struct gcfg_segmenter {
+    Engine e;
+    int max_w = 0, max_h = 0;
+};
+
+struct gcfg_batch {
+    Engine e;
+};
+
+extern "C" {
+
+gcfg_status gcfg_set_dataterms(gcfg_graph *g, const int32_t *dp, const int32_t *dn) {
+    if (!g) return GCFG_ERR_INVALID;
+    g->dp = dp;
+    g->dn = dn;
+    g->built = false;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_set_edges(gcfg_graph *g, const int32_t *up, const int32_t *down, const int32_t *left,
+                           const int32_t *right) {
+    if (!g || !up || !down || !left || !right) return GCFG_ERR_INVALID;
+    g->varying = true;
+    g->up = up;
+    g->down = down;
+    g->left = left;
+    g->right = right;
+    g->built = false;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_set_penalty(gcfg_graph *g, int32_t penalty) {
+    if (!g || penalty < 0 || penalty > GCFG_MAX_CAP) return GCFG_ERR_INVALID;
+    g->varying = false;
+    g->penalty = penalty;
+    g->built = false;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_set_graph(gcfg_graph *g) {
+    if (!g) return GCFG_ERR_INVALID;
+    if (!g->dp || !g->dn) return GCFG_ERR_STATE;
+    Engine &e = g->e;
+    GCFG_CK(cudaMemsetAsync(e.d_ist, 0, sizeof(ImgState), e.st));
+    GCFG_CK(cudaMemsetAsync(e.d_ctl, 0, sizeof(Ctl), e.st));
+    GCFG_TRY(launch_build_arrays(e.batch(), g->dp, g->dn, g->penalty, g->varying ? g->up : nullptr, g->down,
+                                 g->left, g->right, e.st));
+    GCFG_TRY(e.fetch());
+    if (e.h_ctl->err) return GCFG_ERR_INVALID;  // capacities out of range
+    g->built = true;
+    g->solved = false;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_init(int w, int h, const int32_t *dp, const int32_t *dn, int32_t penalty, const int32_t *up,
+                      const int32_t *down, const int32_t *left, const int32_t *right, gcfg_graph **out) {
+    if (!out || w <= 0 || h <= 0 || (long long)w * h > (1LL << 31) - 1) return GCFG_ERR_INVALID;
+    if (penalty < 0 || penalty > GCFG_MAX_CAP) return GCFG_ERR_INVALID;
+    gcfg_graph *g = new gcfg_graph();
+    g->W = w;
+    g->H = h;
+    g->penalty = penalty;
+    gcfg_status rc = g->e.init();
+    if (rc == GCFG_OK) rc = g->e.layout(1, &w, &h, nullptr, false, false);
+    if (rc == GCFG_OK && cudaMalloc(&g->d_label, (size_t)w * h * sizeof(int32_t)) != cudaSuccess)
+        rc = GCFG_ERR_OOM;
+    if (rc == GCFG_OK && dp) {
+        gcfg_set_dataterms(g, dp, dn);
+        if (up) rc = gcfg_set_edges(g, up, down, left, right);
+        if (rc == GCFG_OK) rc = gcfg_set_graph(g);
+    }
+    if (rc) {
+        cudaFree(g->d_label);
+        delete g;
+        return rc;
+    }
+    *out = g;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_set_stream(gcfg_graph *g, void *stream) {
+    if (!g) return GCFG_ERR_INVALID;
+    g->e.st = (cudaStream_t)stream;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_set_schedule(gcfg_graph *g, int push_rounds_per_gr, int max_tile_sweeps) {
+    if (!g || push_rounds_per_gr < 1 || max_tile_sweeps < 1) return GCFG_ERR_INVALID;
+    g->e.prm.push_rounds = push_rounds_per_gr;
+    g->e.prm.max_sweeps = max_tile_sweeps;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_optimize(gcfg_graph *g, int32_t *host_label, gcfg_result *res) {
+    if (!g) return GCFG_ERR_INVALID;
+    if (!g->built) return GCFG_ERR_STATE;
+    Engine &e = g->e;
+    GCFG_CK(cudaEventRecord(e.ev0, e.st));
+    GCFG_TRY(e.solve());
+    GCFG_CK(cudaEventRecord(e.ev1, e.st));
+    if (host_label) GCFG_TRY(launch_extract(e.batch(), nullptr, nullptr, g->d_label, e.st));
+    GCFG_TRY(e.fetch());
+    // the graph is consumed in place, as in the reference: re-solving needs
+    // gcfg_set_graph again (GraphCut.cu:385-534 leaves the residual graph)
+    g->built = false;
+    g->solved = true;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e.ev0, e.ev1);
+    if (res) e.result(0, res, ms);
+    GCFG_TRY(e.status());
+    if (host_label) {
+        GCFG_CK(cudaMemcpyAsync(host_label, g->d_label, (size_t)g->W * g->H * sizeof(int32_t),
+                                cudaMemcpyDeviceToHost, e.st));
+        GCFG_CK(cudaStreamSynchronize(e.st));
+    }
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_get_cuts(gcfg_graph *g, uint8_t *d_smin, uint8_t *d_smax) {
+    if (!g) return GCFG_ERR_INVALID;
+    if (!g->solved) return GCFG_ERR_STATE;
+    GCFG_TRY(launch_extract(g->e.batch(), d_smin, d_smax, nullptr, g->e.st));
+    GCFG_CK(cudaStreamSynchronize(g->e.st));
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_end(gcfg_graph *g) {
+    if (!g) return GCFG_ERR_INVALID;
+    cudaFree(g->d_label);
+    delete g;
+    return GCFG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Stand-alone data term and n-links (one image)
+// ---------------------------------------------------------------------------
+
+static gcfg_status one_image_tables(Engine &e, const uint8_t *rgb, const uint8_t *scrib, int w, int h,
+                                    double lambda, double *raw_dp, double *raw_dn, DtArgs &a) {
+    GCFG_TRY(e.init());
+    GCFG_TRY(e.layout(1, &w, &h, &lambda, true, false, false));
+    a = e.dt(rgb, scrib);
+    if (raw_dp || raw_dn) {
+        GCFG_TRY(grow(e.d_raw, e.c_raw, 2 * NBINS));
+        a.raw_dp = e.d_raw;
+        a.raw_dn = e.d_raw + NBINS;
+    }
+    return dt_tables(a, e.st);
+}
+
+gcfg_status gcfg_tlinks(const uint8_t *d_rgb, const uint8_t *d_scrib, int n, int32_t *d_dp, int32_t *d_dn,
+                        double *h_raw_dp, double *h_raw_dn, void *stream) {
+    if (!d_rgb || !d_scrib || !d_dp || !d_dn || n <= 0) return GCFG_ERR_INVALID;
+    Engine e;
+    e.st = (cudaStream_t)stream;
+    DtArgs a;
+    // the image is treated as n x 1: histograms and tables need no geometry
+    GCFG_TRY(one_image_tables(e, d_rgb, d_scrib, n, 1, 0.0, h_raw_dp, h_raw_dn, a));
+    GCFG_TRY(dt_apply_tlinks(a, n, d_dp, d_dn, e.st));
+    if (h_raw_dp)
+        GCFG_CK(cudaMemcpyAsync(h_raw_dp, a.raw_dp, NBINS * sizeof(double), cudaMemcpyDeviceToHost, e.st));
+    if (h_raw_dn)
+        GCFG_CK(cudaMemcpyAsync(h_raw_dn, a.raw_dn, NBINS * sizeof(double), cudaMemcpyDeviceToHost, e.st));
+    GCFG_CK(cudaStreamSynchronize(e.st));
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_nlinks(const uint8_t *d_rgb, int w, int h, double lambda, int32_t *d_up, int32_t *d_down,
+                        int32_t *d_left, int32_t *d_right, void *stream) {
+    if (!d_rgb || !d_up || !d_down || !d_left || !d_right || w <= 0 || h <= 0) return GCFG_ERR_INVALID;
+    if (!(lambda >= 0) || lambda * 1.0000001 + 1 > (double)GCFG_MAX_CAP) return GCFG_ERR_INVALID;
+    Engine e;
+    e.st = (cudaStream_t)stream;
+    DtArgs a;
+    // no scribbles: the colour tables are skipped, only the n-link table is made
+    GCFG_TRY(one_image_tables(e, d_rgb, nullptr, w, h, lambda, nullptr, nullptr, a));
+    GCFG_TRY(dt_apply_nlinks(a, w, h, d_up, d_down, d_left, d_right, e.st));
+    GCFG_CK(cudaStreamSynchronize(e.st));
+    return GCFG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Segmenter (one image) and batch
+// ---------------------------------------------------------------------------
+
+static gcfg_status run_batch(Engine &e, int n, const int *W, const int *H, const double *lam,
+                             const uint8_t *rgb, const uint8_t *scrib, uint8_t *smin, uint8_t *smax,
+                             int64_t *flows, gcfg_result *res, bool staging) {
+    GCFG_CK(cudaEventRecord(e.ev0, e.st));
+    GCFG_TRY(e.layout(n, W, H, lam, true, staging));
+    if (staging) {
+        const uint8_t *h_rgb = rgb, *h_scrib = scrib;
+        GCFG_CK(cudaMemcpyAsync(e.d_rgb, h_rgb, (size_t)e.n_px * 3, cudaMemcpyHostToDevice, e.st));
+        GCFG_CK(cudaMemcpyAsync(e.d_scrib, h_scrib, (size_t)e.n_px, cudaMemcpyHostToDevice, e.st));
+        rgb = e.d_rgb;
+        scrib = e.d_scrib;
+    }
+    GCFG_TRY(e.build_images(rgb, scrib));
+    GCFG_TRY(e.solve());
+    uint8_t *dmin = staging ? (smin ? e.d_smin : nullptr) : smin;
+    uint8_t *dmax = staging ? (smax ? e.d_smax : nullptr) : smax;
+    if (dmin || dmax) GCFG_TRY(launch_extract(e.batch(), dmin, dmax, nullptr, e.st));
+    if (staging) {
+        if (smin) GCFG_CK(cudaMemcpyAsync(smin, e.d_smin, (size_t)e.n_px, cudaMemcpyDeviceToHost, e.st));
+        if (smax) GCFG_CK(cudaMemcpyAsync(smax, e.d_smax, (size_t)e.n_px, cudaMemcpyDeviceToHost, e.st));
+    }
+    GCFG_CK(cudaEventRecord(e.ev1, e.st));
+    GCFG_TRY(e.fetch());
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e.ev0, e.ev1);
+    for (int i = 0; i < n; ++i) {
+        gcfg_result r;
+        e.result(i, &r, ms);
+        if (flows) flows[i] = r.flow;
+        if (res) res[i] = r;
+    }
+    return e.status();
+}
+
+gcfg_status gcfg_seg_create(int max_w, int max_h, gcfg_segmenter **out) {
+    if (!out || max_w < 1 || max_h < 1 || (long long)max_w * max_h > (1LL << 31) - 1) return GCFG_ERR_INVALID;
+    gcfg_segmenter *s = new gcfg_segmenter();
+    s->max_w = max_w;
+    s->max_h = max_h;
+    const double lam = 1.0;
+    gcfg_status rc = s->e.init();
+    if (rc == GCFG_OK) rc = s->e.layout(1, &max_w, &max_h, &lam, true, true);
+    if (rc == GCFG_OK && cudaStreamSynchronize(s->e.st) != cudaSuccess) rc = GCFG_ERR_CUDA;
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_seg_set_stream(gcfg_segmenter *s, void *stream) {
+    if (!s) return GCFG_ERR_INVALID;
+    s->e.st = (cudaStream_t)stream;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_seg_run(gcfg_segmenter *s, const uint8_t *d_rgb, const uint8_t *d_scrib, int w, int h,
+                         double lambda, uint8_t *d_smin, uint8_t *d_smax, gcfg_result *res) {
+    if (!s || !d_rgb || !d_scrib || w < 1 || h < 1 || w > s->max_w || h > s->max_h) return GCFG_ERR_INVALID;
+    return run_batch(s->e, 1, &w, &h, &lambda, d_rgb, d_scrib, d_smin, d_smax, nullptr, res, false);
+}
+
+gcfg_status gcfg_seg_run_host(gcfg_segmenter *s, const uint8_t *h_rgb, const uint8_t *h_scrib, int w, int h,
+                              double lambda, uint8_t *h_smin, uint8_t *h_smax, gcfg_result *res) {
+    if (!s || !h_rgb || !h_scrib || w < 1 || h < 1 || w > s->max_w || h > s->max_h) return GCFG_ERR_INVALID;
+    return run_batch(s->e, 1, &w, &h, &lambda, h_rgb, h_scrib, h_smin, h_smax, nullptr, res, true);
+}
+
+gcfg_status gcfg_seg_destroy(gcfg_segmenter *s) {
+    if (!s) return GCFG_ERR_INVALID;
+    delete s;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_batch_create(int max_images, int64_t max_pixels, gcfg_batch **out) {
+    if (!out || max_images < 1 || max_pixels < 1) return GCFG_ERR_INVALID;
+    gcfg_batch *b = new gcfg_batch();
+    gcfg_status rc = b->e.init();
+    // pre-size for max_images images of average size (tiles grow on demand)
+    const long long tiles = (max_pixels + TPX - 1) / TPX + 2LL * max_images;
+    if (rc == GCFG_OK) rc = b->e.reserve(max_images, (int)(tiles > (1LL << 30) ? (1LL << 30) : tiles),
+                                         max_pixels, true, false);
+    if (rc) {
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_batch_set_stream(gcfg_batch *b, void *stream) {
+    if (!b) return GCFG_ERR_INVALID;
+    b->e.st = (cudaStream_t)stream;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_batch_set_params(gcfg_batch *b, int push_rounds_per_gr, int max_tile_sweeps,
+                                  int sweeps_per_local_relabel) {
+    if (!b || push_rounds_per_gr < 1 || max_tile_sweeps < 1 || sweeps_per_local_relabel < 1)
+        return GCFG_ERR_INVALID;
+    b->e.prm.push_rounds = push_rounds_per_gr;
+    b->e.prm.max_sweeps = max_tile_sweeps;
+    b->e.prm.bfs_every = sweeps_per_local_relabel;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_batch_run(gcfg_batch *b, int n, const int *widths, const int *heights, const double *lambdas,
+                           const uint8_t *d_rgb, const uint8_t *d_scrib, uint8_t *d_smin, uint8_t *d_smax,
+                           int64_t *h_flows, gcfg_result *h_res) {
+    if (!b || n < 1 || !widths || !heights || !lambdas || !d_rgb || !d_scrib) return GCFG_ERR_INVALID;
+    return run_batch(b->e, n, widths, heights, lambdas, d_rgb, d_scrib, d_smin, d_smax, h_flows, h_res, false);
+}
+
+gcfg_status gcfg_batch_run_host(gcfg_batch *b, int n, const int *widths, const int *heights,
+                                const double *lambdas, const uint8_t *h_rgb, const uint8_t *h_scrib,
+                                uint8_t *h_smin, uint8_t *h_smax, int64_t *h_flows, gcfg_result *h_res) {
+    if (!b || n < 1 || !widths || !heights || !lambdas || !h_rgb || !h_scrib) return GCFG_ERR_INVALID;
+    return run_batch(b->e, n, widths, heights, lambdas, h_rgb, h_scrib, h_smin, h_smax, h_flows, h_res, true);
+}
+
+gcfg_status gcfg_batch_destroy(gcfg_batch *b) {
+    if (!b) return GCFG_ERR_INVALID;
+    delete b;
+    return GCFG_OK;
+}
+
+const char *gcfg_strerror(gcfg_status s) {
+    switch (s) {
+    case GCFG_OK: return "ok";
+    case GCFG_ERR_INVALID: return "invalid argument";
+    case GCFG_ERR_OOM: return "out of device memory";
+    case GCFG_ERR_CUDA: return "CUDA error";
+    case GCFG_ERR_NOT_CONVERGED: return "iteration cap reached";
+    case GCFG_ERR_STATE: return "call out of order";
+    case GCFG_ERR_CAPACITY: return "admission refused: memory cap";
+    }
+    return "unknown";
+}
+
+int64_t gcfg_launch_count(void) { return g_launches.load(); }
+
+}  // extern "C"

@@ -31,11 +31,11 @@ EXPORTS = [
     "gcfg_optimize", "gcfg_get_cuts", "gcfg_end", "gcfg_set_stream", "gcfg_set_schedule",
     "gcfg_tlinks", "gcfg_nlinks", "gcfg_seg_create", "gcfg_seg_run", "gcfg_seg_run_host",
     "gcfg_seg_set_stream", "gcfg_seg_destroy", "gcfg_strerror", "gcfg_launch_count",
-    "gcfg_profile_enable", "gcfg_profile_read",
+    "gcfg_profile_enable", "gcfg_profile_read", "gcfg_batch_create", "gcfg_batch_set_stream",
+    "gcfg_batch_set_params", "gcfg_batch_run", "gcfg_batch_run_host", "gcfg_batch_destroy",
 ]
 
-PROF_KINDS = ["hist", "tlut", "sigma", "wlut", "build", "gr_init", "gr_tile", "count", "push",
-              "reach_init", "reach", "extract", "other"]
+PROF_KINDS = ["hist", "tlut", "sigma", "wlut", "build", "solve", "extract", "other"]
 
 
 class GcfgError(RuntimeError):
@@ -93,6 +93,12 @@ def load(path: str = LIB_PATH):
         "gcfg_seg_destroy": (S, [P]),
         "gcfg_strerror": (C.c_char_p, [I]),
         "gcfg_launch_count": (C.c_int64, []),
+        "gcfg_batch_create": (S, [I, C.c_int64, C.POINTER(P)]),
+        "gcfg_batch_set_stream": (S, [P, P]),
+        "gcfg_batch_set_params": (S, [P, I, I, I]),
+        "gcfg_batch_run": (S, [P, I, P, P, P, P, P, P, P, P, P]),
+        "gcfg_batch_run_host": (S, [P, I, P, P, P, P, P, P, P, P, P]),
+        "gcfg_batch_destroy": (S, [P]),
         "gcfg_profile_enable": (S, [I]),
         "gcfg_profile_read": (S, [C.POINTER(ProfEntry), I, C.POINTER(I)]),
     }
@@ -282,6 +288,69 @@ class Segmenter:
     def close(self):
         if self.handle:
             load().gcfg_seg_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BatchSolver:
+    """Many images solved together in one persistent launch (gcfg_batch_*).
+
+    Images are packed back to back, row-major: RGB uint8 (3 bytes/pixel) and
+    scribbles uint8 (0 none, 1 fg, 2 bg); outputs are packed the same way."""
+
+    def __init__(self, max_images, max_pixels):
+        h = C.c_void_p()
+        _check(load().gcfg_batch_create(int(max_images), int(max_pixels), C.byref(h)),
+               "gcfg_batch_create")
+        self.handle = h
+
+    def set_stream(self, stream):
+        _check(load().gcfg_batch_set_stream(self.handle, _stream_ptr(stream)), "gcfg_batch_set_stream")
+
+    def set_params(self, push_rounds_per_gr, max_tile_sweeps, sweeps_per_local_relabel):
+        _check(load().gcfg_batch_set_params(self.handle, int(push_rounds_per_gr), int(max_tile_sweeps),
+                                            int(sweeps_per_local_relabel)), "gcfg_batch_set_params")
+
+    @staticmethod
+    def _arrays(widths, heights, lambdas):
+        import numpy as np
+        w = np.ascontiguousarray(widths, np.int32)
+        h = np.ascontiguousarray(heights, np.int32)
+        lam = np.ascontiguousarray(lambdas, np.float64)
+        return w, h, lam
+
+    def run(self, widths, heights, lambdas, d_rgb, d_scrib, d_smin=None, d_smax=None, results=False):
+        """Device-resident batch.  Returns (flows int64[n], results or None)."""
+        import numpy as np
+        w, h, lam = self._arrays(widths, heights, lambdas)
+        n = len(w)
+        flows = np.empty(n, np.int64)
+        res = (Result * n)() if results else None
+        _check(load().gcfg_batch_run(self.handle, n, _ptr(w), _ptr(h), _ptr(lam), _ptr(d_rgb),
+                                     _ptr(d_scrib), _ptr(d_smin), _ptr(d_smax), _ptr(flows),
+                                     res), "gcfg_batch_run")
+        return flows, ([r.as_dict() for r in res] if results else None)
+
+    def run_host(self, widths, heights, lambdas, h_rgb, h_scrib, h_smin=None, h_smax=None,
+                 results=False):
+        import numpy as np
+        w, h, lam = self._arrays(widths, heights, lambdas)
+        n = len(w)
+        flows = np.empty(n, np.int64)
+        res = (Result * n)() if results else None
+        _check(load().gcfg_batch_run_host(self.handle, n, _ptr(w), _ptr(h), _ptr(lam), _ptr(h_rgb),
+                                          _ptr(h_scrib), _ptr(h_smin), _ptr(h_smax), _ptr(flows),
+                                          res), "gcfg_batch_run_host")
+        return flows, ([r.as_dict() for r in res] if results else None)
+
+    def close(self):
+        if self.handle:
+            load().gcfg_batch_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

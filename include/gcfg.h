@@ -51,12 +51,12 @@ typedef struct {
                                 (GraphCut.cu:456-457): int32, border dp included */
     int32_t status;          /* gcfg_status of the solve */
     int32_t global_relabels; /* exact global relabels run */
-    int32_t gr_sweeps;       /* tile sweeps launched inside global relabels */
-    int32_t push_rounds;     /* checkerboard push/relabel rounds launched */
-    int32_t cut_sweeps;      /* tile sweeps of the source-side reachability pass */
-    int64_t active_after_first_gr; /* active nodes after the first global relabel */
-    int64_t push_tiles;      /* 32x32 tiles processed by push/relabel launches */
-    int64_t gr_tiles;        /* 32x32 tiles processed by global-relabel launches */
+    int32_t gr_sweeps;       /* tile-frontier rounds inside global relabels */
+    int32_t push_rounds;     /* checkerboard push phases (one colour each) */
+    int32_t cut_sweeps;      /* tile-frontier rounds of the source-side reachability */
+    int64_t active_after_first_gr; /* reserved (0) */
+    int64_t push_tiles;      /* 32x32 tile visits by push/relabel */
+    int64_t gr_tiles;        /* 32x32 tile visits by global relabels */
     float ms;                /* device time of the solve (CUDA events) */
 } gcfg_result;
 
@@ -91,7 +91,8 @@ gcfg_status gcfg_get_cuts(gcfg_graph *g, uint8_t *d_smin, uint8_t *d_smax);
 gcfg_status gcfg_end(gcfg_graph *g);
 /* Stream used by every later call on this graph (void* = cudaStream_t). */
 gcfg_status gcfg_set_stream(gcfg_graph *g, void *stream);
-/* Pushes launched per checkerboard colour between global relabels. */
+/* Checkerboard push rounds between global relabels, and push/relabel sweeps
+ * per tile visit (solver schedule; does not change the result). */
 gcfg_status gcfg_set_schedule(gcfg_graph *g, int push_rounds_per_gr, int max_tile_sweeps);
 
 /* ---------------- data term + n-links (spec steps a, b) ---------------- */
@@ -130,13 +131,48 @@ gcfg_status gcfg_seg_run_host(gcfg_segmenter *s, const uint8_t *h_rgb, const uin
 gcfg_status gcfg_seg_set_stream(gcfg_segmenter *s, void *stream);
 gcfg_status gcfg_seg_destroy(gcfg_segmenter *s);
 
+/* ---------------- batched segmentation (many images, one solve) ---------------- */
+
+/* The images of a batch are solved together: one data-term pass, one build,
+ * one persistent solver launch over the tiles of all images, one extraction.
+ * Images are packed back to back in row-major order (image i starts at pixel
+ * offset sum_{j<i} w_j*h_j; RGB at 3x that byte offset). */
+typedef struct gcfg_batch gcfg_batch;
+
+/* Pre-size for max_images images totalling max_pixels pixels (buffers grow
+ * on demand if a later batch is larger). */
+gcfg_status gcfg_batch_create(int max_images, int64_t max_pixels, gcfg_batch **out);
+gcfg_status gcfg_batch_set_stream(gcfg_batch *b, void *stream);
+/* Solver schedule: push rounds between global relabels, sweeps per tile
+ * visit, sweeps between exact local relabels (does not change results). */
+gcfg_status gcfg_batch_set_params(gcfg_batch *b, int push_rounds_per_gr, int max_tile_sweeps,
+                                  int sweeps_per_local_relabel);
+/* Device-resident batch.  d_smin/d_smax (packed, may be NULL) receive the
+ * two canonical cuts; h_flows (n, may be NULL) the exact flow values;
+ * h_res (n, may be NULL) per-image result records. */
+gcfg_status gcfg_batch_run(gcfg_batch *b, int n, const int *widths, const int *heights,
+                           const double *lambdas, const uint8_t *d_rgb, const uint8_t *d_scrib,
+                           uint8_t *d_smin, uint8_t *d_smax, int64_t *h_flows, gcfg_result *h_res);
+/* The same from host memory: inputs copied in and labels copied out. */
+gcfg_status gcfg_batch_run_host(gcfg_batch *b, int n, const int *widths, const int *heights,
+                                const double *lambdas, const uint8_t *h_rgb, const uint8_t *h_scrib,
+                                uint8_t *h_smin, uint8_t *h_smax, int64_t *h_flows,
+                                gcfg_result *h_res);
+gcfg_status gcfg_batch_destroy(gcfg_batch *b);
+
 /* ---------------- profiling (off by default) ---------------- */
 
 /* Kernel kinds reported by gcfg_profile_read (index = kind). */
 typedef enum {
-    GCFG_PK_HIST = 0, GCFG_PK_TLUT, GCFG_PK_SIGMA, GCFG_PK_WLUT, GCFG_PK_BUILD,
-    GCFG_PK_GR_INIT, GCFG_PK_GR_TILE, GCFG_PK_COUNT, GCFG_PK_PUSH, GCFG_PK_REACH_INIT,
-    GCFG_PK_REACH, GCFG_PK_EXTRACT, GCFG_PK_OTHER, GCFG_PK_NKINDS
+    GCFG_PK_HIST = 0,   /* scribble colour histograms */
+    GCFG_PK_TLUT,       /* per-bin t-link tables */
+    GCFG_PK_SIGMA,      /* sum of ||dI||^2 */
+    GCFG_PK_WLUT,       /* n-link weight tables */
+    GCFG_PK_BUILD,      /* residual graph build */
+    GCFG_PK_SOLVE,      /* persistent max-flow kernel (relabel, push, cuts) */
+    GCFG_PK_EXTRACT,    /* label extraction */
+    GCFG_PK_OTHER,
+    GCFG_PK_NKINDS
 } gcfg_prof_kind;
 
 typedef struct {

@@ -61,7 +61,7 @@ def test_random_grids_vs_oracle(seed):
         assert np.array_equal(label, o["smax"].astype(np.int32))
 
 
-@pytest.mark.parametrize("schedule", [(1, 1), (1, 4), (8, 256)])
+@pytest.mark.parametrize("schedule", [(1, 1), (1, 4), (8, 256), (3, 17)])
 def test_schedules_do_not_change_result(schedule):
     rng = np.random.default_rng(11)
     H, W = 97, 131
@@ -174,3 +174,63 @@ def test_optimize_twice_needs_set_graph():
     r2 = gcfg.GC_Optimize(gw)
     assert r1["flow"] == r2["flow"]
     gcfg.GC_End(gw)
+
+
+def _batch_images(n, seed0, max_side=300):
+    """Uneven images from the scaled cfg-0 generator (small, for parity)."""
+    rng = np.random.default_rng(seed0)
+    imgs = []
+    for i in range(n):
+        s = float(np.exp(rng.uniform(np.log(20), np.log(max_side))))
+        a = float(rng.uniform(0.5, 2.0))
+        W = max(3, int(round(s * np.sqrt(a))))
+        H = max(3, int(round(s / np.sqrt(a))))
+        imgs.append(O.generate(3, W, H, seed0 + i))
+    return imgs
+
+
+@pytest.mark.parametrize("n,seed0", [(1, 500), (7, 600), (40, 700)])
+def test_batch_vs_oracle(n, seed0):
+    """Many uneven images in one solve: every image bit-identical to its own
+    oracle solve."""
+    imgs = _batch_images(n, seed0)
+    lams = [(10.0, 50.0, 200.0)[i % 3] for i in range(n)]
+    Ws = [s.shape[1] for _, s in imgs]
+    Hs = [s.shape[0] for _, s in imgs]
+    rgb = np.concatenate([r.reshape(-1) for r, _ in imgs])
+    scrib = np.concatenate([s.reshape(-1) for _, s in imgs])
+    total = scrib.size
+    bs = gcfg.BatchSolver(n, total)
+    smin = torch.zeros(total, dtype=torch.uint8, device="cuda")
+    smax = torch.zeros(total, dtype=torch.uint8, device="cuda")
+    flows, res = bs.run(Ws, Hs, lams, dev(rgb), dev(scrib), smin, smax, results=True)
+    smin = smin.cpu().numpy()
+    smax = smax.cpu().numpy()
+    off = 0
+    for i, ((r, s), lam) in enumerate(zip(imgs, lams)):
+        o = O.segment(r, s, lam)
+        k = s.size
+        assert flows[i] == o["flow"], i
+        assert np.array_equal(smin[off:off + k].reshape(s.shape), o["smin"]), i
+        assert np.array_equal(smax[off:off + k].reshape(s.shape), o["smax"]), i
+        off += k
+    # the host entry point gives the same answer
+    hmin = np.zeros(total, np.uint8)
+    hmax = np.zeros(total, np.uint8)
+    flows_h, _ = bs.run_host(Ws, Hs, lams, rgb, scrib, hmin, hmax)
+    assert np.array_equal(flows_h, flows)
+    assert np.array_equal(hmin, smin) and np.array_equal(hmax, smax)
+
+
+@pytest.mark.parametrize("params", [(1, 1, 1), (1, 8, 2), (2, 64, 16), (8, 256, 64)])
+def test_batch_params_do_not_change_result(params):
+    imgs = _batch_images(12, 900)
+    Ws = [s.shape[1] for _, s in imgs]
+    Hs = [s.shape[0] for _, s in imgs]
+    rgb = np.concatenate([r.reshape(-1) for r, _ in imgs])
+    scrib = np.concatenate([s.reshape(-1) for _, s in imgs])
+    bs = gcfg.BatchSolver(12, scrib.size)
+    bs.set_params(*params)
+    flows, _ = bs.run(Ws, Hs, [50.0] * 12, dev(rgb), dev(scrib))
+    for i, (r, s) in enumerate(imgs):
+        assert flows[i] == O.segment(r, s, 50.0)["flow"]
