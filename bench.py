@@ -5,20 +5,28 @@ synthetic images: colour-histogram t-links, contrast-sensitive n-links,
 graph build, exact max-flow, both canonical cuts.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload plain1080|plain256|plain4096]
+                  [--workload batch256|plain1080|plain256|plain4096]
+
+Default workload (batch256): 256 images of uneven sizes (side log-uniform
+64..1024, aspect uniform 0.5..2, the 256x256 ellipse generator scaled to each
+image, per-image seeds 1000+i, lambda 50) solved as ONE batch: one data-term
+pass, one build, one persistent solver launch, one extraction.  The same
+images solved one at a time by the plain per-image path are timed beside it
+("plain_value").
 
 value : Mpixel/s with the images already resident in HBM (CUDA events per
-        step, L2 flushed before every step).
-e2e   : the same metric through the host entry point (gcfg_seg_run_host):
-        image + scribbles copied in from pinned host memory and both label
-        maps copied back inside the timed region.
+        step; a 256 MB buffer is written before every step to flush L2).
+e2e   : the same metric through the host entry point (gcfg_batch_run_host /
+        gcfg_seg_run_host): images and scribbles copied in from pinned host
+        memory and both label maps copied back inside the timed region.
 roofline: the kernel with the largest device time in a profiled step;
-        achieved = algorithmic bytes / its summed CUDA-event time.
+        achieved = its algorithmic bytes (work counters x bytes per pixel)
+        / its CUDA-event time; peak = MEASURED_PEAKS.json hbm_gbs.
 cpu_baseline: the oracle's Boykov-Kolmogorov solver (oracle/, the CPU
-        checker) on a bounded sample of the same workload, host cores.
+        checker) on a bounded sample of the same images, one host thread.
 --impl reference: the reference has no CPU implementation of this path and
         its CUDA path cannot be built on the GPU host, so this arm times the
-        CPU port (oracle BK) with all host threads, one image per thread.
+        CPU port (oracle BK) on all host threads, one image per thread.
 """
 from __future__ import annotations
 
@@ -38,35 +46,56 @@ import numpy as np  # noqa: E402
 METRIC = "exact-min-cut Mpixel/s"
 UNIT = "Mpixel/s"
 
-# Algorithmic bytes per pixel of each kernel kind (int32 layout):
-#   push    : read 4 caps + excess + height (24 B), write 4 caps + excess (20 B)
-#   gr_tile : read 4 caps + height (20 B), write height (4 B)
-#   build   : read RGB (3 B), write 4 caps + excess (20 B)
-#   reach   : read 4 caps + mark (17 B), write mark (1 B)
-BYTES_PER_PX = {"push": 44, "gr_tile": 24, "build": 23, "reach": 18, "count": 8, "gr_init": 8,
-                "extract": 7, "hist": 4, "sigma": 6, "reach_init": 5}
+# Algorithmic bytes per pixel per unit of work (int32 layout):
+#   global-relabel tile visit: read 4 caps + excess (20 B), write height (4 B)
+#   push tile visit: read 4 caps + excess + height (24 B), write the same (24 B)
+#   reach tile visit: read 4 caps + excess (20 B)
+#   count pass: read excess + height (8 B)
+#   build: read RGB (3 B), write 4 caps + excess (20 B)
+#   extract: read height (4 B) + reach bit, write two label bytes (2 B)
+B_GR, B_PUSH, B_REACH, B_COUNT, B_BUILD, B_EXTRACT = 24, 48, 20, 8, 23, 6
 
-WORKLOADS = {
-    # The plain single-image 1920x1080 configuration: lambda in {10, 50, 200},
-    # seeds 1..3 (one image per lambda).
-    "plain1080": dict(desc="plain per-image, 1920x1080, lambda {10,50,200}, seeds 1-3",
-                      images=[(1, 1920, 1080, 1, 10.0), (1, 1920, 1080, 2, 50.0),
-                              (1, 1920, 1080, 3, 200.0)]),
-    "plain256": dict(desc="plain per-image, 256x256, lambda 50, seed 0",
-                     images=[(0, 256, 256, 0, 50.0)]),
-    "plain4096": dict(desc="plain per-image, 4096x4096, 2000 blobs, lambda 100, seed 2",
-                      images=[(2, 4096, 4096, 2, 100.0)]),
-}
+
+def workload(name):
+    import synth
+    if name == "batch256":
+        shapes = synth.batch_shapes(256, 1000)
+        return dict(kind="batch", desc="256 uneven images (side log-U(64,1024), aspect U(0.5,2)), "
+                                      "scaled 256x256 ellipse generator, seeds 1000+i, lambda 50",
+                    images=[(3, W, H, seed, 50.0) for (W, H, seed) in shapes])
+    if name == "plain1080":
+        return dict(kind="plain", desc="plain per-image, 1920x1080, lambda {10,50,200}, seeds 1-3",
+                    images=[(1, 1920, 1080, 1, 10.0), (1, 1920, 1080, 2, 50.0), (1, 1920, 1080, 3, 200.0)])
+    if name == "plain256":
+        return dict(kind="plain", desc="plain per-image, 256x256, lambda 50, seed 0",
+                    images=[(0, 256, 256, 0, 50.0)])
+    if name == "plain4096":
+        return dict(kind="plain", desc="plain per-image, 4096x4096, 2000 blobs, lambda 100, seed 2",
+                    images=[(2, 4096, 4096, 2, 100.0)])
+    raise SystemExit(f"unknown workload {name}")
+
+
+def make_inputs(spec):
+    import synth
+    rgb, scrib, offs = synth.generate_packed([(c, W, H, s) for (c, W, H, s, _) in spec["images"]])
+    Ws = np.array([W for (_, W, _, _, _) in spec["images"]], np.int32)
+    Hs = np.array([H for (_, _, H, _, _) in spec["images"]], np.int32)
+    lams = np.array([lam for (*_, lam) in spec["images"]], np.float64)
+    return rgb, scrib, offs, Ws, Hs, lams
+
+
+def image_views(rgb, scrib, offs, Ws, Hs):
+    out = []
+    for i in range(len(Ws)):
+        n = int(Ws[i]) * int(Hs[i])
+        o = int(offs[i])
+        out.append((rgb[3 * o:3 * (o + n)].reshape(Hs[i], Ws[i], 3), scrib[o:o + n].reshape(Hs[i], Ws[i])))
+    return out
 
 
 def dist_info():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
             int(os.environ.get("LOCAL_RANK", 0)))
-
-
-def make_images(spec):
-    import oracle as O
-    return [(O.generate(cfg, W, H, seed), lam) for (cfg, W, H, seed, lam) in spec["images"]]
 
 
 class ClockSampler:
@@ -117,17 +146,16 @@ class ClockSampler:
 
 
 def load_peaks():
-    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
-        d = json.load(open(p))
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
 
 
-def ncu_traffic(kind: str, workload: str):
+def ncu_traffic(kind: str, workload_name: str):
     """DRAM bytes per launch from a committed ncu summary, if one exists."""
-    p = os.path.join(ROOT, "profiles", f"{kind}_{workload}.md")
+    p = os.path.join(ROOT, "profiles", f"{kind}_{workload_name}.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -139,20 +167,20 @@ def ncu_traffic(kind: str, workload: str):
     return None
 
 
-def cpu_baseline(images, budget_s=10.0, threads=1):
-    """Oracle BK on a bounded sample of the workload (host cores)."""
+def cpu_baseline(views, lams, budget_s=10.0):
+    """Oracle BK on a bounded sample of the workload, one host thread."""
     import oracle as O
     t0 = time.perf_counter()
-    px = 0
-    flows = []
-    k = 0
-    while True:
-        (rgb, scrib), lam = images[k % len(images)]
-        r = O.segment(rgb, scrib, lam, solver="bk")
-        flows.append((k % len(images), r["flow"]))
+    px, flows, k = 0, [], 0
+    order = sorted(range(len(views)), key=lambda i: views[i][1].size)
+    while k < len(order):
+        i = order[k] if len(views) > 8 else k % len(views)
+        rgb, scrib = views[i]
+        r = O.segment(rgb, scrib, float(lams[i]), solver="bk")
+        flows.append((i, r["flow"]))
         px += scrib.size
         k += 1
-        if time.perf_counter() - t0 > budget_s or k >= 64:
+        if time.perf_counter() - t0 > budget_s or (len(views) <= 8 and k >= 64):
             break
     dt = time.perf_counter() - t0
     return px / dt / 1e6, k, dt, flows
@@ -163,33 +191,29 @@ def run_reference_arm(args, spec, rank, world):
     if rank != 0:
         return 0
     import oracle as O
-    images = make_images(spec)
+    rgb, scrib, offs, Ws, Hs, lams = make_inputs(spec)
+    views = image_views(rgb, scrib, offs, Ws, Hs)
     nthreads = os.cpu_count() or 1
-    lams = [lam for _, lam in images]
-    imgs = [im for im, _ in images]
+    reps = max(1, nthreads // len(views))
     per_step = []
-    total_px = sum(s.size for _, s in imgs)
+    total_px = int(sum(s.size for _, s in views)) * reps
     for i in range(args.warmup + args.steps):
         t = time.perf_counter()
-        # one image per thread; the step's images are replicated so that every
-        # host thread has work (bounded sample of the same workload)
-        reps = max(1, nthreads // len(imgs))
-        flows, _, _, _ = O.segment_batch(imgs * reps, lams * reps, nthreads)
+        O.segment_batch(views * reps, list(lams) * reps, nthreads)
         dt = time.perf_counter() - t
         if i >= args.warmup:
-            per_step.append((dt, total_px * reps))
-    secs = sum(d for d, _ in per_step)
-    px = sum(p for _, p in per_step)
-    value = px / secs / 1e6
+            per_step.append(dt)
+    secs = sum(per_step)
+    value = total_px * len(per_step) / secs / 1e6
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / len(per_step) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded in-repo generator)",
             "config": {"workload": args.workload, "desc": spec["desc"]},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                             "sample": f"{len(imgs)} image(s) x {max(1, nthreads // len(imgs))} replicas per step, "
-                                       "oracle Boykov-Kolmogorov, one image per host thread; the reference "
-                                       "has no CPU solver and its CUDA path is not buildable on the GPU host"},
+                             "sample": f"{len(views)} image(s) x {reps} per step, oracle Boykov-Kolmogorov, "
+                                       "one image per host thread; the reference has no CPU solver and its "
+                                       "CUDA path cannot be built on the GPU host"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -201,12 +225,13 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="plain1080", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="batch256")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--no-plain", action="store_true", help="skip the per-image comparison leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_info()
-    spec = WORKLOADS[args.workload]
+    spec = workload(args.workload)
     if args.impl == "reference":
         return run_reference_arm(args, spec, rank, world)
 
@@ -226,59 +251,81 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
-    images = make_images(spec)
-    maxW = max(s.shape[1] for (_, s), _ in images)
-    maxH = max(s.shape[0] for (_, s), _ in images)
-    seg = gcfg.Segmenter(maxW, maxH)
+    rgb, scrib, offs, Ws, Hs, lams = make_inputs(spec)
+    views = image_views(rgb, scrib, offs, Ws, Hs)
+    n_img = len(Ws)
+    px_per_step = int(scrib.size)
     stream = torch.cuda.current_stream()
-    seg.set_stream(stream)
-    dev = []
-    for (rgb, scrib), lam in images:
-        H, W = scrib.shape
-        dev.append(dict(rgb=torch.from_numpy(rgb).cuda(), scrib=torch.from_numpy(scrib).cuda(),
-                        smin=torch.empty((H, W), dtype=torch.uint8, device="cuda"),
-                        smax=torch.empty((H, W), dtype=torch.uint8, device="cuda"),
-                        W=W, H=H, lam=lam,
-                        h_rgb=torch.from_numpy(rgb).pin_memory(), h_scrib=torch.from_numpy(scrib).pin_memory(),
-                        h_smin=torch.empty((H, W), dtype=torch.uint8).pin_memory(),
-                        h_smax=torch.empty((H, W), dtype=torch.uint8).pin_memory()))
-    px_per_step = sum(d["W"] * d["H"] for d in dev)
+    d_rgb = torch.from_numpy(rgb).cuda()
+    d_scrib = torch.from_numpy(scrib).cuda()
+    d_smin = torch.empty(px_per_step, dtype=torch.uint8, device="cuda")
+    d_smax = torch.empty(px_per_step, dtype=torch.uint8, device="cuda")
+    h_rgb = torch.from_numpy(rgb).pin_memory().numpy()
+    h_scrib = torch.from_numpy(scrib).pin_memory().numpy()
+    h_smin = torch.empty(px_per_step, dtype=torch.uint8).pin_memory().numpy()
+    h_smax = torch.empty(px_per_step, dtype=torch.uint8).pin_memory().numpy()
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
-    def step_device():
-        res = []
-        for d in dev:
-            res.append(seg.run(d["rgb"], d["scrib"], d["W"], d["H"], d["lam"], d["smin"], d["smax"]))
-        return res
+    batched = spec["kind"] == "batch"
+    bs = gcfg.BatchSolver(n_img, px_per_step)
+    bs.set_stream(stream)
+    seg = gcfg.Segmenter(int(Ws.max()), int(Hs.max()))
+    seg.set_stream(stream)
+    offs_l = [int(o) for o in offs]
+
+    def step_batch():
+        flows, res = bs.run(Ws, Hs, lams, d_rgb, d_scrib, d_smin, d_smax, results=True)
+        return flows, res
+
+    def step_plain():
+        flows, res = [], []
+        for i in range(n_img):
+            o, n = offs_l[i], int(Ws[i]) * int(Hs[i])
+            r = seg.run(d_rgb[3 * o:3 * (o + n)], d_scrib[o:o + n], int(Ws[i]), int(Hs[i]), float(lams[i]),
+                        d_smin[o:o + n], d_smax[o:o + n])
+            flows.append(r["flow"])
+            res.append(r)
+        return np.array(flows), res
 
     def step_host():
-        res = []
-        for d in dev:
-            res.append(seg.run_host(d["h_rgb"].numpy(), d["h_scrib"].numpy(), d["W"], d["H"], d["lam"],
-                                    d["h_smin"].numpy(), d["h_smax"].numpy()))
-        return res
+        if batched:
+            return bs.run_host(Ws, Hs, lams, h_rgb, h_scrib, h_smin, h_smax)[0]
+        flows = []
+        for i in range(n_img):
+            o, n = offs_l[i], int(Ws[i]) * int(Hs[i])
+            r = seg.run_host(h_rgb[3 * o:3 * (o + n)], h_scrib[o:o + n], int(Ws[i]), int(Hs[i]),
+                             float(lams[i]), h_smin[o:o + n], h_smax[o:o + n])
+            flows.append(r["flow"])
+        return np.array(flows)
+
+    step = step_batch if batched else step_plain
+
+    def timed(fn, steps):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        out = None
+        for i in range(steps):
+            flush.fill_(i & 0xFF)  # L2 flush (256 MB > 129 MB L2), outside the step's events
+            ev[i][0].record(stream)
+            out = fn()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ev), out
 
     for _ in range(args.warmup):
-        step_device()
+        step()
         step_host()
+    if batched and not args.no_plain:
+        step_plain()
 
     # ---- timed region: device-resident inputs ----
     clocks = ClockSampler(local)
     clocks.start()
     barrier()
     l0 = gcfg.launch_count()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    results = []
-    for i in range(args.steps):
-        flush.fill_(i & 0xFF)  # L2 flush (256 MB > 129 MB L2), outside the step's events
-        ev[i][0].record(stream)
-        results.append(step_device())
-        ev[i][1].record(stream)
+    total_ms, (flows, results) = timed(step, args.steps)
     barrier()
     launches = gcfg.launch_count() - l0
     clk = clocks.stop()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(step_ms)
 
     # ---- e2e through the host entry point ----
     barrier()
@@ -287,10 +334,19 @@ def main():
         flush.fill_(i & 0xFF)
         torch.cuda.synchronize()
         t = time.perf_counter()
-        step_host()
+        flows_h = step_host()
         e2e_ms.append((time.perf_counter() - t) * 1e3)
     barrier()
     e2e_total = sum(e2e_ms)
+
+    # ---- the same images, plain per-image path (batched workload only) ----
+    plain = None
+    if batched and not args.no_plain:
+        psteps = max(1, min(args.steps, 3))
+        plain_ms, (pflows, _) = timed(step_plain, psteps)
+        plain = {"value": px_per_step * psteps / (plain_ms / 1e3) / 1e6, "unit": UNIT,
+                 "ms_per_step": plain_ms / psteps, "steps": psteps,
+                 "flows_equal_batched": bool(np.array_equal(pflows, flows))}
 
     def max_over_ranks(v):
         if dist is None:
@@ -308,50 +364,59 @@ def main():
     gcfg.profile_enable(True)
     gcfg.profile_read()
     flush.fill_(7)
-    prof_res = step_device()
+    pflows2, pres = step()
     prof = gcfg.profile_read()
     gcfg.profile_enable(False)
     dom = max(prof, key=lambda k: prof[k]["ms"])
     peak, peak_kind = load_peaks()
-    if dom == "push":
-        units_px = sum(r["push_tiles"] for r in prof_res) * 1024
-    elif dom == "gr_tile":
-        units_px = sum(r["gr_tiles"] for r in prof_res) * 1024
-    elif dom in ("build", "extract", "hist", "sigma"):
-        units_px = px_per_step
-    else:
-        units_px = sum(((d["W"] + 31) // 32) * ((d["H"] + 31) // 32) * 1024 for d in dev)
+    tiles_total = int(sum(((int(w) + 31) // 32) * ((int(h) + 31) // 32) for w, h in zip(Ws, Hs)))
+    recs = pres if isinstance(pres, list) else [pres]
+    solve_bytes = 0
+    for r in (recs[:1] if batched else recs):
+        solve_bytes += 1024 * (B_GR * r["gr_tiles"] + B_PUSH * r["push_tiles"] + B_REACH * r["reach_tiles"])
+        solve_bytes += 1024 * B_COUNT * r["global_relabels"] * (tiles_total if batched else
+                                                                 ((int(Ws[recs.index(r)]) + 31) // 32) *
+                                                                 ((int(Hs[recs.index(r)]) + 31) // 32))
+    alg = {"solve": solve_bytes, "build": B_BUILD * 1024 * tiles_total, "extract": B_EXTRACT * px_per_step,
+           "hist": 4 * px_per_step, "sigma": 3 * px_per_step}
     launches_dom = max(prof[dom]["launches"], 1)
-    alg_bytes = BYTES_PER_PX.get(dom, 24) * units_px
-    achieved = alg_bytes / (prof[dom]["ms"] / 1e3) / 1e9
+    alg_bytes = alg.get(dom, 0)
+    achieved = alg_bytes / (prof[dom]["ms"] / 1e3) / 1e9 if prof[dom]["ms"] > 0 else 0.0
+    step_prof_ms = sum(v["ms"] for v in prof.values())
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
-                if peak_kind == "measured" else "fallback 6.8 TB/s",
+                "frac": achieved / peak,
+                "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                else "of fallback 6.8 TB/s",
                 "traffic": ncu_traffic(dom, args.workload),
                 "alg_bytes_per_launch": alg_bytes / launches_dom,
                 "avg_launch_us": prof[dom]["ms"] / launches_dom * 1e3,
-                "share_of_step": prof[dom]["ms"] / sum(v["ms"] for v in prof.values()),
+                "share_of_step": prof[dom]["ms"] / step_prof_ms if step_prof_ms else None,
                 "kernels_ms": {k: round(v["ms"], 4) for k, v in prof.items() if v["launches"]}}
 
+    r0 = recs[0]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded in-repo generator; no dataset)",
-            "config": {"workload": args.workload, "desc": spec["desc"], "images_per_step": len(dev),
-                       "pixels_per_step": px_per_step, "l2": "flushed (256 MB write) before every step",
+            "config": {"workload": args.workload, "desc": spec["desc"], "images_per_step": n_img,
+                       "pixels_per_step": px_per_step, "mode": "batched" if batched else "per-image",
+                       "l2": "flushed (256 MB write) before every step",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 4 * px_per_step,
                     "d2h_bytes_per_step": 2 * px_per_step, "ms_per_step": e2e_total / args.steps},
             "roofline": roofline, "clocks": clk, "gpu_launches": launches,
-            "solver": {k: results[-1][0][k] for k in ("global_relabels", "gr_sweeps", "push_rounds",
-                                                       "cut_sweeps")}}
+            "solver": {k: r0[k] for k in ("global_relabels", "gr_sweeps", "push_rounds", "cut_sweeps",
+                                          "push_tiles", "gr_tiles", "reach_tiles")}}
+    if plain is not None:
+        line["plain_per_image"] = plain
+    line["flows_host_equal_device"] = bool(np.array_equal(np.asarray(flows_h), np.asarray(flows)))
     if rank == 0:
-        cpu_v, n_img, secs, flows = cpu_baseline(images, budget_s=args.cpu_budget)
-        ok = all(results[-1][i]["flow"] == f for i, f in flows)
+        cpu_v, n_chk, secs, cflows = cpu_baseline(views, lams, budget_s=args.cpu_budget)
+        ok = all(int(flows[i]) == f for i, f in cflows)
         line["cpu_baseline"] = {"value": cpu_v, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": f"{n_img} image(s) of the workload in {secs:.1f} s, oracle "
+                                "sample": f"{n_chk} image(s) of the workload in {secs:.1f} s, oracle "
                                           "Boykov-Kolmogorov, 1 thread"}
-        line["parity"] = {"flows_equal_oracle": ok, "images_checked": len(set(i for i, _ in flows))}
+        line["parity"] = {"flows_equal_oracle": ok, "images_checked": len(set(i for i, _ in cflows))}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

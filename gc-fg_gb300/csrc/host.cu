@@ -273,7 +273,7 @@ struct Engine {
         r->gr_sweeps = h_ctl->gr_rounds;
         r->push_rounds = h_ctl->push_phases;
         r->cut_sweeps = h_ctl->reach_rounds;
-        r->active_after_first_gr = 0;
+        r->reach_tiles = (long long)h_ctl->reach_tiles;
         r->push_tiles = (long long)h_ctl->push_tiles;
         r->gr_tiles = (long long)h_ctl->gr_tiles;
         r->ms = ms;

@@ -48,7 +48,7 @@ class Result(C.Structure):
     _fields_ = [("flow", C.c_int64), ("ref_energy", C.c_int32), ("status", C.c_int32),
                 ("global_relabels", C.c_int32), ("gr_sweeps", C.c_int32),
                 ("push_rounds", C.c_int32), ("cut_sweeps", C.c_int32),
-                ("active_after_first_gr", C.c_int64), ("push_tiles", C.c_int64),
+                ("reach_tiles", C.c_int64), ("push_tiles", C.c_int64),
                 ("gr_tiles", C.c_int64), ("ms", C.c_float)]
 
     def as_dict(self):

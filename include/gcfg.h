@@ -54,7 +54,7 @@ typedef struct {
     int32_t gr_sweeps;       /* tile-frontier rounds inside global relabels */
     int32_t push_rounds;     /* checkerboard push phases (one colour each) */
     int32_t cut_sweeps;      /* tile-frontier rounds of the source-side reachability */
-    int64_t active_after_first_gr; /* reserved (0) */
+    int64_t reach_tiles;     /* 32x32 tile visits by the source-side reachability */
     int64_t push_tiles;      /* 32x32 tile visits by push/relabel */
     int64_t gr_tiles;        /* 32x32 tile visits by global relabels */
     float ms;                /* device time of the solve (CUDA events) */

@@ -6,7 +6,6 @@
  * leg of bench.py use it, and only as the checker.
  *
  * It restates, in plain C:
- *   - the deterministic synthetic inputs (images + scribbles);
  *   - the colour-histogram data term and the contrast-sensitive n-links;
  *   - the reference's graph construction conventions
  *     (GraphCutKernels.cu:112-214: interior-only nodes, edges into the 1-pixel
@@ -29,34 +28,6 @@
 #ifdef __cplusplus
 extern "C" {
 #endif
-
-/* ---- deterministic PRNG and math (bit-identical on x86-64 and aarch64) ---- */
-uint64_t or_splitmix64(uint64_t *state);
-double or_uniform(uint64_t *state);              /* [0,1), 53-bit */
-double or_normal(uint64_t *state);               /* Box-Muller, own log/cos */
-double or_det_log(double x);
-double or_det_cos(double x);
-
-/* ---- synthetic image families ----
- * family 0: "ellipse" (central ellipse + n_extra random ellipses)
- * family 1: "blobs"   (n_blobs discs on a striped, noisy background)
- * rgb: 3*W*H bytes interleaved, scrib: W*H bytes (0 none, 1 fg, 2 bg). */
-typedef struct {
-    int family;
-    int W, H;
-    uint64_t seed;
-    double ax, ay;           /* central ellipse semi-axes (family 0) */
-    int n_extra;             /* random ellipses (family 0) */
-    double extra_lo, extra_hi;
-    int n_blobs;             /* family 1 */
-    double r_lo, r_hi;       /* blob radii (family 1) */
-    double sd_fg, sd_bg;     /* colour noise per channel */
-    double stripe_amp;       /* family 1: background stripe amplitude */
-    double stripe_period;    /* family 1: stripe period in pixels */
-} or_gen_params;
-
-void or_gen_defaults(int cfg, int W, int H, uint64_t seed, or_gen_params *p);
-int or_generate(const or_gen_params *p, uint8_t *rgb, uint8_t *scrib);
 
 /* ---- data term: 16^3 histograms, +1 Laplace smoothing, round(10*-log p) ---- */
 void or_histograms(const uint8_t *rgb, const uint8_t *scrib, int n,
@@ -131,9 +102,6 @@ int or_segment_batch(int n_img, const int *Ws, const int *Hs, const int64_t *off
                      const uint8_t *rgb, const uint8_t *scrib, const double *lambdas,
                      int solver, int nthreads, uint8_t *smin, uint8_t *smax,
                      int64_t *flows);
-
-/* FNV-1a 64-bit hash of a byte buffer (fixture checks). */
-uint64_t or_fnv1a(const void *data, int64_t n);
 
 #ifdef __cplusplus
 }

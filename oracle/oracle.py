@@ -10,9 +10,15 @@ import ctypes as C
 import os
 import subprocess
 
+import sys
+
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+_PKG = os.path.join(os.path.dirname(HERE), "gc-fg_gb300")
+if _PKG not in sys.path:
+    sys.path.insert(0, _PKG)
+import synth  # noqa: E402  (input generator; the oracle only checks)
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 
 _CFLAGS = ["-O2", "-fPIC", "-shared", "-ffp-contract=off", "-std=c11", "-Wall",
@@ -35,14 +41,6 @@ def build(force: bool = False) -> str:
 _lib = None
 
 
-class GenParams(C.Structure):
-    _fields_ = [("family", C.c_int), ("W", C.c_int), ("H", C.c_int), ("seed", C.c_uint64),
-                ("ax", C.c_double), ("ay", C.c_double), ("n_extra", C.c_int),
-                ("extra_lo", C.c_double), ("extra_hi", C.c_double), ("n_blobs", C.c_int),
-                ("r_lo", C.c_double), ("r_hi", C.c_double), ("sd_fg", C.c_double),
-                ("sd_bg", C.c_double), ("stripe_amp", C.c_double), ("stripe_period", C.c_double)]
-
-
 class Stats(C.Structure):
     _fields_ = [("flow", C.c_int64), ("pushes", C.c_int64), ("relabels", C.c_int64),
                 ("global_relabels", C.c_int64), ("augments", C.c_int64)]
@@ -54,8 +52,6 @@ def lib():
         build()
         _lib = C.CDLL(LIB_PATH)
         P = C.c_void_p
-        _lib.or_gen_defaults.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(GenParams)]
-        _lib.or_generate.argtypes = [C.POINTER(GenParams), P, P]
         _lib.or_histograms.argtypes = [P, P, C.c_int, P, P]
         _lib.or_tlink_lut.argtypes = [P, P, P, P, P, P]
         _lib.or_tlinks.argtypes = [P, C.c_int, P, P, P, P]
@@ -78,12 +74,6 @@ def lib():
         _lib.or_segment.argtypes = [P, P, C.c_int, C.c_int, C.c_double, C.c_int, P, P, P, P, P, P,
                                     P, P, C.POINTER(C.c_int64)]
         _lib.or_segment_batch.argtypes = [C.c_int, P, P, P, P, P, P, C.c_int, C.c_int, P, P, P]
-        _lib.or_fnv1a.argtypes = [P, C.c_int64]
-        _lib.or_fnv1a.restype = C.c_uint64
-        _lib.or_det_log.argtypes = [C.c_double]
-        _lib.or_det_log.restype = C.c_double
-        _lib.or_det_cos.argtypes = [C.c_double]
-        _lib.or_det_cos.restype = C.c_double
     return _lib
 
 
@@ -91,23 +81,9 @@ def _p(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 
 
-def gen_params(cfg: int, W: int, H: int, seed: int) -> GenParams:
-    p = GenParams()
-    lib().or_gen_defaults(cfg, W, H, seed, C.byref(p))
-    return p
-
-
 def generate(cfg: int, W: int, H: int, seed: int):
-    """Synthetic image of one of the workload families.
-
-    Returns (rgb uint8 [H, W, 3], scribbles uint8 [H, W]: 0 none, 1 fg, 2 bg)."""
-    p = gen_params(cfg, W, H, seed)
-    rgb = np.empty((H, W, 3), np.uint8)
-    scrib = np.empty((H, W), np.uint8)
-    rc = lib().or_generate(C.byref(p), _p(rgb), _p(scrib))
-    if rc:
-        raise RuntimeError(f"or_generate failed: {rc}")
-    return rgb, scrib
+    """Synthetic inputs (delegates to the package's generator)."""
+    return synth.generate(cfg, W, H, seed)
 
 
 def histograms(rgb, scrib):
@@ -242,5 +218,4 @@ def segment_batch(images, lambdas, nthreads: int, solver="bk"):
 
 
 def fnv1a(a) -> int:
-    a = np.ascontiguousarray(a)
-    return lib().or_fnv1a(_p(a), a.nbytes)
+    return synth.fnv1a(a)

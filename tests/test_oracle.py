@@ -79,9 +79,10 @@ def test_generator_is_pinned():
 
 def test_det_math():
     xs = np.linspace(1e-6, 1.0, 1001)
-    assert max(abs(O.lib().or_det_log(float(x)) - np.log(x)) for x in xs) < 1e-13
+    import synth
+    assert max(abs(synth.lib().gs_det_log(float(x)) - np.log(x)) for x in xs) < 1e-13
     ts = np.linspace(-7, 7, 1001)
-    assert max(abs(O.lib().or_det_cos(float(t)) - np.cos(t)) for t in ts) < 1e-13
+    assert max(abs(synth.lib().gs_det_cos(float(t)) - np.cos(t)) for t in ts) < 1e-13
 
 
 def test_cfg0_pipeline_solvers_agree():
