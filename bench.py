@@ -405,8 +405,10 @@ def main():
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 4 * px_per_step,
                     "d2h_bytes_per_step": 2 * px_per_step, "ms_per_step": e2e_total / args.steps},
             "roofline": roofline, "clocks": clk, "gpu_launches": launches,
-            "solver": {k: r0[k] for k in ("global_relabels", "gr_sweeps", "push_rounds", "cut_sweeps",
-                                          "push_tiles", "gr_tiles", "reach_tiles")}}
+            "solver": {k: (round(r0[k], 4) if isinstance(r0[k], float) else r0[k])
+                       for k in ("global_relabels", "gr_sweeps", "push_rounds", "cut_sweeps", "push_tiles",
+                                 "gr_tiles", "reach_tiles", "push_sweeps", "push_local_relabels",
+                                 "t_global_relabel_ms", "t_count_ms", "t_push_ms", "t_reach_ms")}}
     if plain is not None:
         line["plain_per_image"] = plain
     line["flows_host_equal_device"] = bool(np.array_equal(np.asarray(flows_h), np.asarray(flows)))

@@ -119,6 +119,28 @@ __device__ bool grid_sync(const Batch &b, unsigned reset_mask) {
 
 __device__ __forceinline__ int vload(const int *p) { return *(volatile const int *)p; }
 
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Phase clock: block 0 / thread 0 charges the time since the last mark to
+// one phase counter (all blocks leave a grid barrier together).
+struct PhaseClock {
+    unsigned long long t;
+    __device__ void start() {
+        if (blockIdx.x == 0 && threadIdx.x == 0) t = gtimer();
+    }
+    __device__ void charge(unsigned long long *slot) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            const unsigned long long now = gtimer();
+            *slot += now - t;
+            t = now;
+        }
+    }
+};
+
 // ---------------------------------------------------------------------------
 // Bit-parallel tile BFS (one warp, lane = row)
 // ---------------------------------------------------------------------------
@@ -336,8 +358,11 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
     __syncthreads();
 
     int any = 1;
+    int sweeps = 0, bfs = 0;
     for (int sw = 0; sw < prm.max_sweeps; ++sw) {
+        ++sweeps;
         if (sw % prm.bfs_every == 0) {
+            ++bfs;
             // exact local relabel against the frozen halo
 #pragma unroll
             for (int k = 0; k < ROWS_PER_WARP; ++k) {
@@ -453,6 +478,10 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
             enqueue(b, b.mark_push, (phase + 1) % 3, phase + 1, nt);
     }
     if (any && threadIdx.x == 0) enqueue(b, b.mark_push, (phase + 2) % 3, phase + 2, t);
+    if (threadIdx.x == 0) {
+        atomicAdd(&b.ctl->push_sweeps, (unsigned long long)sweeps);
+        atomicAdd(&b.ctl->push_bfs, (unsigned long long)bfs);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -466,6 +495,8 @@ __global__ void __launch_bounds__(TILE_THREADS, 2) k_solve(Batch b, SolveParams 
     const int gwarp = blockIdx.x * 8 + warp, nwarps = gridDim.x * 8;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
 
+    PhaseClock clk;
+    clk.start();
     // fresh de-duplication marks and reach bits for this solve
     for (int t = gtid; t < b.n_tiles; t += nthreads) {
         b.mark_push[t] = -1;
@@ -473,6 +504,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 2) k_solve(Batch b, SolveParams 
     }
     for (size_t i = gtid; i < (size_t)b.n_tiles * 32; i += nthreads) b.reach[i] = 0;
     if (!grid_sync(b, 0)) return;
+    clk.charge(&ctl->t_init);
 
     int P = 0;  // push phase counter (even at the start of every outer iteration)
     int G = 0;  // global relabel round counter (tags of the tile frontier)
@@ -513,6 +545,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 2) k_solve(Batch b, SolveParams 
             ++G;
             if (gtid == 0) ctl->gr_rounds++;
         }
+        clk.charge(&ctl->t_gr);
         // ------------------------ count active nodes ------------------------
         for (int t = gwarp; t < b.n_tiles; t += nwarps) {
             const int img = __ldg(b.tile_img + t);
@@ -540,6 +573,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 2) k_solve(Batch b, SolveParams 
             }
         }
         if (!grid_sync(b, 0)) return;
+        clk.charge(&ctl->t_count);
         if (gtid == 0) {
             ctl->global_relabels++;
             ctl->outer_iters = outer + 1;
@@ -580,6 +614,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 2) k_solve(Batch b, SolveParams 
             if (!more) break;
         }
         P = (last + 3) & ~1;
+        clk.charge(&ctl->t_push);
     }
     if (!finished) {
         if (gtid == 0) set_error(b, ERRC_OUTER);
@@ -609,6 +644,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 2) k_solve(Batch b, SolveParams 
         ++G;
         if (gtid == 0) ctl->reach_rounds++;
     }
+    clk.charge(&ctl->t_reach);
 }
 
 // ---------------------------------------------------------------------------

@@ -55,6 +55,9 @@ struct Ctl {
     int gr_rounds, push_phases, reach_rounds, outer_iters;
     int global_relabels;
     int pad[3];
+    // device time per phase (ns, %globaltimer read by block 0 at barriers)
+    unsigned long long t_init, t_gr, t_count, t_push, t_reach;
+    unsigned long long push_sweeps, push_bfs;
 };
 
 struct Batch {

@@ -276,6 +276,12 @@ struct Engine {
         r->reach_tiles = (long long)h_ctl->reach_tiles;
         r->push_tiles = (long long)h_ctl->push_tiles;
         r->gr_tiles = (long long)h_ctl->gr_tiles;
+        r->push_sweeps = (long long)h_ctl->push_sweeps;
+        r->push_local_relabels = (long long)h_ctl->push_bfs;
+        r->t_global_relabel_ms = h_ctl->t_gr * 1e-6f;
+        r->t_count_ms = h_ctl->t_count * 1e-6f;
+        r->t_push_ms = h_ctl->t_push * 1e-6f;
+        r->t_reach_ms = h_ctl->t_reach * 1e-6f;
         r->ms = ms;
     }
 };

@@ -49,7 +49,10 @@ class Result(C.Structure):
                 ("global_relabels", C.c_int32), ("gr_sweeps", C.c_int32),
                 ("push_rounds", C.c_int32), ("cut_sweeps", C.c_int32),
                 ("reach_tiles", C.c_int64), ("push_tiles", C.c_int64),
-                ("gr_tiles", C.c_int64), ("ms", C.c_float)]
+                ("gr_tiles", C.c_int64), ("push_sweeps", C.c_int64),
+                ("push_local_relabels", C.c_int64), ("t_global_relabel_ms", C.c_float),
+                ("t_count_ms", C.c_float), ("t_push_ms", C.c_float), ("t_reach_ms", C.c_float),
+                ("ms", C.c_float)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -57,6 +57,9 @@ typedef struct {
     int64_t reach_tiles;     /* 32x32 tile visits by the source-side reachability */
     int64_t push_tiles;      /* 32x32 tile visits by push/relabel */
     int64_t gr_tiles;        /* 32x32 tile visits by global relabels */
+    int64_t push_sweeps;     /* push/relabel sweeps summed over tile visits */
+    int64_t push_local_relabels; /* exact local (tile BFS) relabels in push visits */
+    float t_global_relabel_ms, t_count_ms, t_push_ms, t_reach_ms; /* device time per phase */
     float ms;                /* device time of the solve (CUDA events) */
 } gcfg_result;
 
