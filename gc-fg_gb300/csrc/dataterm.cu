@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_build_img_b(Batch b, const uin
     const int *dnl = dn_lut + (size_t)im * NBINS;
     const uint8_t *base = rgb + 3 * d.pix0;
     const long long w32 = (long long)((W + 31) / 32) * 32;
-    unsigned long long idp = 0, rinit = 0;
+    unsigned long long idp = 0, rinit = 0, pos = 0;
 #pragma unroll
     for (int k = 0; k < ROWS_PER_WARP; ++k) {
         const int r = warp + 8 * k;
@@ -234,7 +234,10 @@ __global__ void __launch_bounds__(TILE_THREADS) k_build_img_b(Batch b, const uin
         const size_t q = (size_t)t * TPX + r * 32 + lane;
         b.cap[q] = c;
         b.exc[q] = e;
+        write_tile_masks(b, t, r, c, e);
+        if (e > 0) pos += (unsigned)e;
     }
+    block_store_sum(b.tile_pos + t, pos);
     warp_atomic_add_u64(&b.ist[im].interior_dp, idp);
     warp_atomic_add_u64(&b.ist[im].ref_init, rinit);
 }

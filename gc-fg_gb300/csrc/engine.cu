@@ -148,8 +148,9 @@ struct PhaseClock {
 // sink: nodes of this row at level 1 (e < 0).
 // hl/hr: level of this row's left/right halo node; ht/hb: level of the halo
 // node above/below column `lane`.  Levels of the tile are written to
-// hs[row * stride + col]; unreachable nodes get INF.
-__device__ void tile_bfs(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd, unsigned sink, int hl,
+// hs[row * stride + col]; unreachable nodes get INF.  Returns this row's
+// reached set.
+__device__ unsigned tile_bfs(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd, unsigned sink, int hl,
                          int hr, int ht, int hb, int *hs, int stride) {
     const int lane = threadIdx.x & 31;
     int *row = hs + lane * stride;
@@ -183,6 +184,7 @@ __device__ void tile_bfs(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd, uns
             lvl = nxt;
         }
     }
+    return S;
 }
 
 // ---------------------------------------------------------------------------
@@ -195,6 +197,7 @@ struct SmemPush {
     int h[TILE_H + 2][TILE_W + 2];
     int halo_in[4][32];
     unsigned m[5][32];  // left, right, up, down, sink row masks
+    unsigned long long part[8];
     int idx;
     int flag;
 };
@@ -210,63 +213,52 @@ union Smem {
 // Global relabel / reach (warp per tile)
 // ---------------------------------------------------------------------------
 
-// Load the residual row masks of tile t (lane = row after the loop).
-__device__ __forceinline__ void load_masks(const Batch &b, size_t base, unsigned &Rl, unsigned &Rr,
-                                           unsigned &Ru, unsigned &Rd, unsigned &neg, unsigned &pos,
-                                           int &e_row0, int &e_row31) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll 4
-    for (int r = 0; r < 32; ++r) {
-        const int4 c = __ldcg(b.cap + base + r * 32 + lane);
-        const int e = __ldcg(b.exc + base + r * 32 + lane);
-        const unsigned ml = __ballot_sync(FULL, c.x > 0);
-        const unsigned mr = __ballot_sync(FULL, c.y > 0);
-        const unsigned mu = __ballot_sync(FULL, c.z > 0);
-        const unsigned md = __ballot_sync(FULL, c.w > 0);
-        const unsigned mn = __ballot_sync(FULL, e < 0);
-        const unsigned mp = __ballot_sync(FULL, e > 0);
-        if (lane == r) {
-            Rl = ml; Rr = mr; Ru = mu; Rd = md; neg = mn; pos = mp;
-        }
-        if (r == 0) e_row0 = e;
-        if (r == 31) e_row31 = e;
-    }
+// This lane's row of the six mask planes of tile t (lane = row).
+__device__ __forceinline__ void load_tile_masks(const Batch &b, int t, unsigned m[6]) {
+    const unsigned *base = b.tmask + (size_t)t * 6 * 32 + (threadIdx.x & 31);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) m[k] = __ldcg(base + k * 32);
 }
 
-__device__ __forceinline__ int halo_level(const Batch &b, int nt, int px, bool from_exc) {
-    if (nt < 0) return INF_H;
-    const size_t q = (size_t)nt * TPX + px;
-    if (from_exc) return __ldcg(b.exc + q) < 0 ? 1 : INF_H;
-    return __ldcg(b.h + q);
+__device__ __forceinline__ unsigned mask_word(const Batch &b, int t, int k, int row) {
+    return __ldcg(b.tmask + ((size_t)t * 6 + k) * 32 + row);
 }
 
 // Exact distances of tile t given its halo; queues neighbours whose halo
-// (our border) decreased.  round0: heights of every tile are stale, so the
-// halo and "old" border values are derived from the excess instead.
+// (our border) decreased.  round0: the heights of every tile are stale, so
+// the halo and "old" border values come from the sink-connected bits.
 __device__ void gr_tile(const Batch &b, int t, bool round0, int tag_next, int slot_next, int *hs) {
     const int lane = threadIdx.x & 31;
     const TileGeo g = tile_geo(b, t);
     const size_t base = (size_t)t * TPX;
-    unsigned Rl = 0, Rr = 0, Ru = 0, Rd = 0, neg = 0, pos = 0;
-    int e0 = 0, e31 = 0;
-    load_masks(b, base, Rl, Rr, Ru, Rd, neg, pos, e0, e31);
-    int o_top, o_bot, o_lft, o_rgt;
+    unsigned m[6];
+    load_tile_masks(b, t, m);
+    int o_top, o_bot, o_lft, o_rgt, ht, hb, hl, hr;
     if (round0) {
-        o_top = e0 < 0 ? 1 : INF_H;
-        o_bot = e31 < 0 ? 1 : INF_H;
-        o_lft = (neg & 1u) ? 1 : INF_H;
-        o_rgt = (neg >> 31) ? 1 : INF_H;
+        const unsigned n0 = __shfl_sync(FULL, m[4], 0), n31 = __shfl_sync(FULL, m[4], 31);
+        o_top = (n0 >> lane) & 1u ? 1 : INF_H;
+        o_bot = (n31 >> lane) & 1u ? 1 : INF_H;
+        o_lft = (m[4] & 1u) ? 1 : INF_H;
+        o_rgt = (m[4] >> 31) ? 1 : INF_H;
+        ht = g.nb[2] >= 0 && ((mask_word(b, g.nb[2], 4, 31) >> lane) & 1u) ? 1 : INF_H;
+        hb = g.nb[3] >= 0 && ((mask_word(b, g.nb[3], 4, 0) >> lane) & 1u) ? 1 : INF_H;
+        hl = g.nb[0] >= 0 && (mask_word(b, g.nb[0], 4, lane) >> 31) ? 1 : INF_H;
+        hr = g.nb[1] >= 0 && (mask_word(b, g.nb[1], 4, lane) & 1u) ? 1 : INF_H;
     } else {
         o_top = __ldcg(b.h + base + lane);
         o_bot = __ldcg(b.h + base + 31 * 32 + lane);
         o_lft = __ldcg(b.h + base + lane * 32);
         o_rgt = __ldcg(b.h + base + lane * 32 + 31);
+        ht = g.nb[2] >= 0 ? __ldcg(b.h + (size_t)g.nb[2] * TPX + 31 * 32 + lane) : INF_H;
+        hb = g.nb[3] >= 0 ? __ldcg(b.h + (size_t)g.nb[3] * TPX + lane) : INF_H;
+        hl = g.nb[0] >= 0 ? __ldcg(b.h + (size_t)g.nb[0] * TPX + lane * 32 + 31) : INF_H;
+        hr = g.nb[1] >= 0 ? __ldcg(b.h + (size_t)g.nb[1] * TPX + lane * 32) : INF_H;
     }
-    const int ht = halo_level(b, g.nb[2], 31 * 32 + lane, round0);
-    const int hb = halo_level(b, g.nb[3], lane, round0);
-    const int hl = halo_level(b, g.nb[0], lane * 32 + 31, round0);
-    const int hr = halo_level(b, g.nb[1], lane * 32, round0);
-    tile_bfs(Rl, Rr, Ru, Rd, neg, hl, hr, ht, hb, hs, 33);
+    const unsigned reached = tile_bfs(m[0], m[1], m[2], m[3], m[4], hl, hr, ht, hb, hs, 33);
+    int act = __popc(m[5] & reached);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) act += __shfl_down_sync(FULL, act, o);
+    if (lane == 0) b.tile_act[t] = act;
     __syncwarp();
 #pragma unroll 4
     for (int r = 0; r < 32; ++r) b.h[base + r * 32 + lane] = hs[r * 33 + lane];
@@ -285,35 +277,18 @@ __device__ void gr_tile(const Batch &b, int t, bool round0, int tag_next, int sl
 __device__ void reach_tile(const Batch &b, int t, bool round0, int tag_next, int slot_next) {
     const int lane = threadIdx.x & 31;
     const TileGeo g = tile_geo(b, t);
-    const size_t base = (size_t)t * TPX;
-    unsigned Rl = 0, Rr = 0, Ru = 0, Rd = 0, neg = 0, pos = 0;
-    int e0, e31;
-    load_masks(b, base, Rl, Rr, Ru, Rd, neg, pos, e0, e31);
+    unsigned m[6];
+    load_tile_masks(b, t, m);
     const unsigned old = round0 ? 0u : __ldcg(b.reach + (size_t)t * 32 + lane);
-    // halo nodes that are reached and have residual capacity into the tile
-    unsigned Tin = 0, Bin = 0;
-    unsigned lbit = 0, rbit = 0;
-    if (g.nb[2] >= 0) {
-        const unsigned rr = __ldcg(b.reach + (size_t)g.nb[2] * 32 + 31);
-        const int4 c = __ldcg(b.cap + (size_t)g.nb[2] * TPX + 31 * 32 + lane);
-        Tin = rr & __ballot_sync(FULL, c.w > 0);
-    }
-    if (g.nb[3] >= 0) {
-        const unsigned rr = __ldcg(b.reach + (size_t)g.nb[3] * 32 + 0);
-        const int4 c = __ldcg(b.cap + (size_t)g.nb[3] * TPX + lane);
-        Bin = rr & __ballot_sync(FULL, c.z > 0);
-    }
-    if (g.nb[0] >= 0) {
-        const unsigned rr = __ldcg(b.reach + (size_t)g.nb[0] * 32 + lane);
-        const int4 c = __ldcg(b.cap + (size_t)g.nb[0] * TPX + lane * 32 + 31);
-        lbit = ((rr >> 31) & 1u) && c.y > 0 ? 1u : 0u;
-    }
-    if (g.nb[1] >= 0) {
-        const unsigned rr = __ldcg(b.reach + (size_t)g.nb[1] * 32 + lane);
-        const int4 c = __ldcg(b.cap + (size_t)g.nb[1] * TPX + lane * 32);
-        rbit = (rr & 1u) && c.x > 0 ? 0x80000000u : 0u;
-    }
-    unsigned S = pos | old;
+    // halo pixels that are reached and have residual capacity into the tile
+    const unsigned Tin = g.nb[2] >= 0 ? __ldcg(b.reach + (size_t)g.nb[2] * 32 + 31) & mask_word(b, g.nb[2], 3, 31) : 0u;
+    const unsigned Bin = g.nb[3] >= 0 ? __ldcg(b.reach + (size_t)g.nb[3] * 32) & mask_word(b, g.nb[3], 2, 0) : 0u;
+    const unsigned lbit =
+        g.nb[0] >= 0 ? ((__ldcg(b.reach + (size_t)g.nb[0] * 32 + lane) & mask_word(b, g.nb[0], 1, lane)) >> 31) : 0u;
+    const unsigned rbit =
+        g.nb[1] >= 0 ? ((__ldcg(b.reach + (size_t)g.nb[1] * 32 + lane) & mask_word(b, g.nb[1], 0, lane) & 1u) << 31) : 0u;
+    const unsigned Rl = m[0], Rr = m[1], Ru = m[2], Rd = m[3];
+    unsigned S = m[5] | old;
     for (int it = 0; it < BFS_MAX_ITERS; ++it) {
         unsigned up = __shfl_up_sync(FULL, S & Rd, 1);
         unsigned dn = __shfl_down_sync(FULL, S & Ru, 1);
@@ -450,13 +425,27 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
         any = __syncthreads_or(act);
         if (!any) break;
     }
-    // ---- write back ----
+    // ---- write back (and refresh the tile's mask planes and excess sum) ----
+    unsigned long long pos = 0;
 #pragma unroll
     for (int k = 0; k < ROWS_PER_WARP; ++k) {
         const int r = warp + 8 * k;
-        b.cap[base + r * 32 + lane] = s.c[r][lane];
-        b.exc[base + r * 32 + lane] = s.e[r][lane];
+        const int4 c = s.c[r][lane];
+        const int e = s.e[r][lane];
+        b.cap[base + r * 32 + lane] = c;
+        b.exc[base + r * 32 + lane] = e;
         b.h[base + r * 32 + lane] = s.h[r + 1][lane + 1];
+        write_tile_masks(b, t, r, c, e);
+        if (e > 0) pos += (unsigned)e;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) pos += __shfl_down_sync(FULL, pos, o);
+    if (lane == 0) s.part[warp] = pos;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long tot = 0;
+        for (int w = 0; w < 8; ++w) tot += s.part[w];
+        b.tile_pos[t] = tot;
     }
     // ---- hand halo flow to the (idle) neighbour tiles ----
     if (warp < 4) {
@@ -470,8 +459,18 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
             else if (warp == 2) { px = 31 * 32 + lane; comp = 3; }  // upper tile, its DOWN edge
             else { px = lane; comp = 2; }                           // lower tile, its UP edge
             const size_t q = (size_t)nt * TPX + px;
-            atomicAdd(b.exc + q, f);
-            atomicAdd(reinterpret_cast<int *>(b.cap + q) + comp, f);
+            const int old_e = atomicAdd(b.exc + q, f);
+            const int new_e = old_e + f;
+            const int old_c = atomicAdd(reinterpret_cast<int *>(b.cap + q) + comp, f);
+            // keep the receiving tile's mask planes and excess sum exact
+            unsigned *mt = b.tmask + (size_t)nt * 6 * 32;
+            const int row = px >> 5;
+            const unsigned bit = 1u << (px & 31);
+            if (old_c == 0) atomicOr(mt + comp * 32 + row, bit);
+            if (old_e < 0 && new_e >= 0) atomicAnd(mt + 4 * 32 + row, ~bit);
+            if (old_e <= 0 && new_e > 0) atomicOr(mt + 5 * 32 + row, bit);
+            const int dpos = max(new_e, 0) - max(old_e, 0);
+            if (dpos) atomicAdd(b.tile_pos + nt, (unsigned long long)dpos);
             sent = true;
         }
         if (__any_sync(FULL, sent) && lane == 0)
@@ -547,29 +546,17 @@ __global__ void __launch_bounds__(TILE_THREADS, 2) k_solve(Batch b, SolveParams 
         }
         clk.charge(&ctl->t_gr);
         // ------------------------ count active nodes ------------------------
-        for (int t = gwarp; t < b.n_tiles; t += nwarps) {
+        for (int t = gtid; t < b.n_tiles; t += nthreads) {
             const int img = __ldg(b.tile_img + t);
             if (vload(&b.ist[img].done)) continue;
-            const size_t base = (size_t)t * TPX;
-            unsigned long long pos = 0;
-            int nact = 0;
-#pragma unroll 4
-            for (int r = 0; r < 32; ++r) {
-                const int e = __ldcg(b.exc + base + r * 32 + lane);
-                const int hh = __ldcg(b.h + base + r * 32 + lane);
-                if (e > 0) pos += (unsigned)e;
-                nact += __popc(__ballot_sync(FULL, e > 0 && hh < INF_H));
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) pos += __shfl_down_sync(FULL, pos, o);
-            if (lane == 0) {
-                if (pos) atomicAdd(&b.ist[img].pos_excess, pos);
-                if (nact) {
-                    atomicAdd(&b.ist[img].active, (unsigned long long)nact);
-                    atomicAdd(&ctl->total_active, (unsigned long long)nact);
-                    const TileGeo g = tile_geo(b, t);
-                    enqueue(b, b.mark_push, (P + g.color) % 3, P + g.color, t);
-                }
+            const int nact = vload(b.tile_act + t);
+            const unsigned long long pos = __ldcg(b.tile_pos + t);
+            if (pos) atomicAdd(&b.ist[img].pos_excess, pos);
+            if (nact) {
+                atomicAdd(&b.ist[img].active, (unsigned long long)nact);
+                atomicAdd(&ctl->total_active, (unsigned long long)nact);
+                const TileGeo g = tile_geo(b, t);
+                enqueue(b, b.mark_push, (P + g.color) % 3, P + g.color, t);
             }
         }
         if (!grid_sync(b, 0)) return;
@@ -664,7 +651,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_build_arrays(Batch b, const in
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const TileGeo g = tile_geo(b, t);
     const int W = b.img[g.img].W, H = b.img[g.img].H;
-    unsigned long long idp = 0, rinit = 0;
+    unsigned long long idp = 0, rinit = 0, pos = 0;
     int bad = 0;
     const long long w32 = (long long)((W + 31) / 32) * 32;
 #pragma unroll
@@ -697,7 +684,10 @@ __global__ void __launch_bounds__(TILE_THREADS) k_build_arrays(Batch b, const in
         const size_t p = (size_t)t * TPX + r * 32 + lane;
         b.cap[p] = c;
         b.exc[p] = e;
+        write_tile_masks(b, t, r, c, e);
+        if (e > 0) pos += (unsigned)e;
     }
+    block_store_sum(b.tile_pos + t, pos);
     if (bad) set_error(b, 100);
     warp_atomic_add_u64(&b.ist[g.img].interior_dp, idp);
     warp_atomic_add_u64(&b.ist[g.img].ref_init, rinit);

@@ -69,6 +69,12 @@ struct Batch {
     int *exc;
     int *h;
     unsigned *reach;         // 32 row masks per tile (source-side reachability)
+    // Per-tile row bitmask planes, kept exact by every writer of cap/exc:
+    // tmask[(t*6 + k)*32 + row], k = 0..3 residual capacity toward left,
+    // right, up, down; 4: e < 0 (sink-connected); 5: e > 0 (excess).
+    unsigned *tmask;
+    int *tile_act;                  // active pixels of the tile at its last relabel visit
+    unsigned long long *tile_pos;   // sum of positive excess of the tile
     int *lists;              // L_NLISTS work queues of tile indices, list_cap each
     int list_cap;
     int *mark_push, *mark_gr;
@@ -103,5 +109,41 @@ gcfg_status launch_solve(const Batch &b, const SolveParams &prm, int n_tiles, cu
 gcfg_status launch_build_arrays(const Batch &b, const int *dp, const int *dn, int penalty, const int *up,
                                 const int *down, const int *left, const int *right, cudaStream_t st);
 gcfg_status launch_extract(const Batch &b, uint8_t *smin, uint8_t *smax, int *label, cudaStream_t st);
+
+}  // namespace gcfg
+
+namespace gcfg {
+
+// ---- device helpers shared by the build kernels and the solver ----
+
+// Mask planes and positive-excess sum of one tile from per-pixel values held
+// by a block (warp w owns rows w, w+8, w+16, w+24; lane = column).
+__device__ __forceinline__ void write_tile_masks(const Batch &b, int t, int r, int4 c, int e) {
+    const unsigned ml = __ballot_sync(0xffffffffu, c.x > 0);
+    const unsigned mr = __ballot_sync(0xffffffffu, c.y > 0);
+    const unsigned mu = __ballot_sync(0xffffffffu, c.z > 0);
+    const unsigned md = __ballot_sync(0xffffffffu, c.w > 0);
+    const unsigned mn = __ballot_sync(0xffffffffu, e < 0);
+    const unsigned mp = __ballot_sync(0xffffffffu, e > 0);
+    const int lane = threadIdx.x & 31;
+    if (lane < 6) {
+        const unsigned v = lane == 0 ? ml : lane == 1 ? mr : lane == 2 ? mu : lane == 3 ? md : lane == 4 ? mn : mp;
+        b.tmask[((size_t)t * 6 + lane) * 32 + r] = v;
+    }
+}
+
+// Sum of v over the block, stored by thread 0 (blocks of TILE_THREADS).
+__device__ __forceinline__ void block_store_sum(unsigned long long *dst, unsigned long long v) {
+    __shared__ unsigned long long part[TILE_THREADS / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long tot = 0;
+        for (int w = 0; w < TILE_THREADS / 32; ++w) tot += part[w];
+        *dst = tot;
+    }
+}
 
 }  // namespace gcfg

@@ -55,6 +55,9 @@ struct Engine {
     int *d_exc = nullptr; size_t c_exc = 0;
     int *d_h = nullptr; size_t c_h = 0;
     unsigned *d_reach = nullptr; size_t c_reach = 0;
+    unsigned *d_tmask = nullptr; size_t c_tmask = 0;
+    int *d_tact = nullptr; size_t c_tact = 0;
+    unsigned long long *d_tpos = nullptr; size_t c_tpos = 0;
     int *d_lists = nullptr; size_t c_lists = 0; int list_cap = 0;
     int *d_mpush = nullptr; size_t c_mpush = 0;
     int *d_mgr = nullptr; size_t c_mgr = 0;
@@ -82,6 +85,7 @@ struct Engine {
     void release() {
         cudaFree(d_img); cudaFree(d_ist); cudaFree(d_chunk); cudaFree(d_tile_img);
         cudaFree(d_cap); cudaFree(d_exc); cudaFree(d_h); cudaFree(d_reach);
+        cudaFree(d_tmask); cudaFree(d_tact); cudaFree(d_tpos);
         cudaFree(d_lists);
         cudaFree(d_mpush); cudaFree(d_mgr); cudaFree(d_ctl);
         cudaFree(d_hist); cudaFree(d_dpl); cudaFree(d_dnl); cudaFree(d_raw); cudaFree(d_wlut);
@@ -95,6 +99,7 @@ struct Engine {
         if (ev1) cudaEventDestroy(ev1);
         d_img = nullptr; d_ist = nullptr; d_chunk = nullptr; d_tile_img = nullptr;
         d_cap = nullptr; d_exc = nullptr; d_h = nullptr; d_reach = nullptr;
+        d_tmask = nullptr; d_tact = nullptr; d_tpos = nullptr;
         d_lists = nullptr;
         d_mpush = d_mgr = nullptr; d_ctl = nullptr;
         d_hist = d_dpl = d_dnl = nullptr; d_raw = nullptr; d_wlut = nullptr;
@@ -131,6 +136,9 @@ struct Engine {
             GCFG_TRY(grow(d_exc, c_exc, (size_t)tiles * TPX));
             GCFG_TRY(grow(d_h, c_h, (size_t)tiles * TPX));
             GCFG_TRY(grow(d_reach, c_reach, (size_t)tiles * 32));
+            GCFG_TRY(grow(d_tmask, c_tmask, (size_t)tiles * 6 * 32));
+            GCFG_TRY(grow(d_tact, c_tact, tiles));
+            GCFG_TRY(grow(d_tpos, c_tpos, tiles));
             if ((size_t)tiles > (size_t)list_cap || !d_lists) {
                 GCFG_TRY(grow(d_lists, c_lists, (size_t)L_NLISTS * tiles));
                 list_cap = tiles;
@@ -213,6 +221,9 @@ struct Engine {
         b.exc = d_exc;
         b.h = d_h;
         b.reach = d_reach;
+        b.tmask = d_tmask;
+        b.tile_act = d_tact;
+        b.tile_pos = d_tpos;
         b.lists = d_lists;
         b.list_cap = list_cap;
         b.mark_push = d_mpush;
