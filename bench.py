@@ -408,7 +408,9 @@ def main():
             "solver": {k: (round(r0[k], 4) if isinstance(r0[k], float) else r0[k])
                        for k in ("global_relabels", "gr_sweeps", "push_rounds", "cut_sweeps", "push_tiles",
                                  "gr_tiles", "reach_tiles", "push_sweeps", "push_local_relabels",
-                                 "t_global_relabel_ms", "t_count_ms", "t_push_ms", "t_reach_ms")}}
+                                 "t_global_relabel_ms", "t_count_ms", "t_push_ms", "t_reach_ms",
+                                 "cyc_load", "cyc_local_relabel", "cyc_sweeps", "cyc_writeback",
+                                 "cyc_take")}}
     if plain is not None:
         line["plain_per_image"] = plain
     line["flows_host_equal_device"] = bool(np.array_equal(np.asarray(flows_h), np.asarray(flows)))

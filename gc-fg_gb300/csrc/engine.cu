@@ -316,6 +316,7 @@ __device__ void reach_tile(const Batch &b, int t, bool round0, int tag_next, int
 
 __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int phase, SmemPush &s) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    long long c0 = clock64(), c1, cb = 0, cs = 0;
     const TileGeo g = tile_geo(b, t);
     const size_t base = (size_t)t * TPX;
 #pragma unroll
@@ -330,15 +331,23 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
     if (warp == 2) s.h[lane + 1][0] = g.nb[0] >= 0 ? __ldcg(b.h + (size_t)g.nb[0] * TPX + lane * 32 + 31) : INF_H;
     if (warp == 3) s.h[lane + 1][TILE_W + 1] = g.nb[1] >= 0 ? __ldcg(b.h + (size_t)g.nb[1] * TPX + lane * 32) : INF_H;
     if (warp < 4) s.halo_in[warp][lane] = 0;
+    if (threadIdx.x == 0) s.flag = 0;  // "pushed in sweep sw" marker: sw + 1
     __syncthreads();
+    c1 = clock64();
+    const long long c_load = c1 - c0;
 
     int any = 1;
     int sweeps = 0, bfs = 0;
+    // The exact local relabel (tile BFS) runs at the first sweep when
+    // prm.bfs_first is set, after a sweep that pushed nothing while active
+    // pixels remain, and at least every prm.bfs_every sweeps.
+    bool need_bfs = prm.bfs_first != 0;
+    int since_bfs = 0;
     for (int sw = 0; sw < prm.max_sweeps; ++sw) {
         ++sweeps;
-        if (sw % prm.bfs_every == 0) {
+        if (need_bfs || since_bfs >= prm.bfs_every) {
             ++bfs;
-            // exact local relabel against the frozen halo
+            since_bfs = 0;
 #pragma unroll
             for (int k = 0; k < ROWS_PER_WARP; ++k) {
                 const int r = warp + 8 * k;
@@ -354,67 +363,107 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
                 }
             }
             __syncthreads();
+            const long long cb0 = clock64();
             if (warp == 0)
                 tile_bfs(s.m[0][lane], s.m[1][lane], s.m[2][lane], s.m[3][lane], s.m[4][lane],
                          s.h[lane + 1][0], s.h[lane + 1][TILE_W + 1], s.h[0][lane + 1],
                          s.h[TILE_H + 1][lane + 1], &s.h[1][1], TILE_W + 2);
             __syncthreads();
+            cb += clock64() - cb0;
         }
-        // ---- push phase: heights fixed ----
+        ++since_bfs;
+        // ---- push phase: heights fixed.  All loads first, flows in
+        // registers, then fire-and-forget shared atomics. ----
+        int ev[ROWS_PER_WARP], hv[ROWS_PER_WARP];
 #pragma unroll
         for (int k = 0; k < ROWS_PER_WARP; ++k) {
             const int r = warp + 8 * k;
-            int e = s.e[r][lane];
-            const int hh = s.h[r + 1][lane + 1];
-            if (e > 0 && hh < INF_H) {
+            ev[k] = s.e[r][lane];
+            hv[k] = s.h[r + 1][lane + 1];
+        }
+        bool pushed = false;
+#pragma unroll
+        for (int k = 0; k < ROWS_PER_WARP; ++k) {
+            const int r = warp + 8 * k;
+            const int hh = hv[k];
+            if (ev[k] > 0 && hh < INF_H) {
                 const int4 c = s.c[r][lane];
-                const int e0 = e;
-                if (c.x > 0 && hh == s.h[r + 1][lane] + 1) {
-                    const int f = min(e, c.x);
-                    e -= f;
-                    s.c[r][lane].x = c.x - f;
-                    if (lane > 0) { s.c[r][lane - 1].y += f; atomicAdd(&s.e[r][lane - 1], f); }
-                    else atomicAdd(&s.halo_in[0][r], f);
+                const int hl = s.h[r + 1][lane], hr = s.h[r + 1][lane + 2];
+                const int hu = s.h[r][lane + 1], hd = s.h[r + 2][lane + 1];
+                int e = ev[k];
+                const int fl = (c.x > 0 && hh == hl + 1) ? min(e, c.x) : 0;
+                e -= fl;
+                const int fr = (c.y > 0 && hh == hr + 1) ? min(e, c.y) : 0;
+                e -= fr;
+                const int fu = (c.z > 0 && hh == hu + 1) ? min(e, c.z) : 0;
+                e -= fu;
+                const int fd = (c.w > 0 && hh == hd + 1) ? min(e, c.w) : 0;
+                e -= fd;
+                if (fl) {
+                    s.c[r][lane].x = c.x - fl;
+                    if (lane > 0) {
+                        atomicAdd(reinterpret_cast<int *>(&s.c[r][lane - 1]) + 1, fl);
+                        atomicAdd(&s.e[r][lane - 1], fl);
+                    } else {
+                        atomicAdd(&s.halo_in[0][r], fl);
+                    }
                 }
-                if (e > 0 && c.y > 0 && hh == s.h[r + 1][lane + 2] + 1) {
-                    const int f = min(e, c.y);
-                    e -= f;
-                    s.c[r][lane].y = c.y - f;
-                    if (lane < TILE_W - 1) { s.c[r][lane + 1].x += f; atomicAdd(&s.e[r][lane + 1], f); }
-                    else atomicAdd(&s.halo_in[1][r], f);
+                if (fr) {
+                    s.c[r][lane].y = c.y - fr;
+                    if (lane < TILE_W - 1) {
+                        atomicAdd(reinterpret_cast<int *>(&s.c[r][lane + 1]) + 0, fr);
+                        atomicAdd(&s.e[r][lane + 1], fr);
+                    } else {
+                        atomicAdd(&s.halo_in[1][r], fr);
+                    }
                 }
-                if (e > 0 && c.z > 0 && hh == s.h[r][lane + 1] + 1) {
-                    const int f = min(e, c.z);
-                    e -= f;
-                    s.c[r][lane].z = c.z - f;
-                    if (r > 0) { s.c[r - 1][lane].w += f; atomicAdd(&s.e[r - 1][lane], f); }
-                    else atomicAdd(&s.halo_in[2][lane], f);
+                if (fu) {
+                    s.c[r][lane].z = c.z - fu;
+                    if (r > 0) {
+                        atomicAdd(reinterpret_cast<int *>(&s.c[r - 1][lane]) + 3, fu);
+                        atomicAdd(&s.e[r - 1][lane], fu);
+                    } else {
+                        atomicAdd(&s.halo_in[2][lane], fu);
+                    }
                 }
-                if (e > 0 && c.w > 0 && hh == s.h[r + 2][lane + 1] + 1) {
-                    const int f = min(e, c.w);
-                    e -= f;
-                    s.c[r][lane].w = c.w - f;
-                    if (r < TILE_H - 1) { s.c[r + 1][lane].z += f; atomicAdd(&s.e[r + 1][lane], f); }
-                    else atomicAdd(&s.halo_in[3][lane], f);
+                if (fd) {
+                    s.c[r][lane].w = c.w - fd;
+                    if (r < TILE_H - 1) {
+                        atomicAdd(reinterpret_cast<int *>(&s.c[r + 1][lane]) + 2, fd);
+                        atomicAdd(&s.e[r + 1][lane], fd);
+                    } else {
+                        atomicAdd(&s.halo_in[3][lane], fd);
+                    }
                 }
-                if (e != e0) atomicSub(&s.e[r][lane], e0 - e);
+                if (e != ev[k]) {
+                    atomicSub(&s.e[r][lane], ev[k] - e);
+                    pushed = true;
+                }
             }
         }
+        if (pushed) s.flag = sw + 1;  // benign race: every writer stores the same value
         __syncthreads();
         // ---- relabel phase: capacities and excess fixed ----
         int act = 0;
 #pragma unroll
         for (int k = 0; k < ROWS_PER_WARP; ++k) {
             const int r = warp + 8 * k;
-            const int e = s.e[r][lane];
-            int hh = s.h[r + 1][lane + 1];
-            if (e > 0 && hh < INF_H) {
+            ev[k] = s.e[r][lane];
+            hv[k] = s.h[r + 1][lane + 1];
+        }
+#pragma unroll
+        for (int k = 0; k < ROWS_PER_WARP; ++k) {
+            const int r = warp + 8 * k;
+            int hh = hv[k];
+            if (ev[k] > 0 && hh < INF_H) {
                 const int4 c = s.c[r][lane];
+                const int hl = s.h[r + 1][lane], hr = s.h[r + 1][lane + 2];
+                const int hu = s.h[r][lane + 1], hd = s.h[r + 2][lane + 1];
                 int m = INF_H;
-                if (c.x > 0) m = min(m, s.h[r + 1][lane]);
-                if (c.y > 0) m = min(m, s.h[r + 1][lane + 2]);
-                if (c.z > 0) m = min(m, s.h[r][lane + 1]);
-                if (c.w > 0) m = min(m, s.h[r + 2][lane + 1]);
+                if (c.x > 0) m = min(m, hl);
+                if (c.y > 0) m = min(m, hr);
+                if (c.z > 0) m = min(m, hu);
+                if (c.w > 0) m = min(m, hd);
                 if (m >= hh) {
                     hh = m >= INF_H - 1 ? INF_H : m + 1;
                     s.h[r + 1][lane + 1] = hh;
@@ -424,7 +473,10 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
         }
         any = __syncthreads_or(act);
         if (!any) break;
+        need_bfs = s.flag != sw + 1;  // stalled: nothing was pushed in this sweep
     }
+    const long long c2 = clock64();
+    cs = c2 - c1 - cb;
     // ---- write back (and refresh the tile's mask planes and excess sum) ----
     unsigned long long pos = 0;
 #pragma unroll
@@ -477,9 +529,14 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
             enqueue(b, b.mark_push, (phase + 1) % 3, phase + 1, nt);
     }
     if (any && threadIdx.x == 0) enqueue(b, b.mark_push, (phase + 2) % 3, phase + 2, t);
+    __syncthreads();
     if (threadIdx.x == 0) {
         atomicAdd(&b.ctl->push_sweeps, (unsigned long long)sweeps);
         atomicAdd(&b.ctl->push_bfs, (unsigned long long)bfs);
+        atomicAdd(&b.ctl->cyc_load, (unsigned long long)c_load);
+        atomicAdd(&b.ctl->cyc_bfs, (unsigned long long)cb);
+        atomicAdd(&b.ctl->cyc_sweep, (unsigned long long)cs);
+        atomicAdd(&b.ctl->cyc_wb, (unsigned long long)(clock64() - c2));
     }
 }
 
@@ -582,10 +639,12 @@ __global__ void __launch_bounds__(TILE_THREADS, 2) k_solve(Batch b, SolveParams 
                 last = p;
                 const int n = vload(&ctl->size[slot]);
                 for (;;) {
+                    const long long ct = clock64();
                     if (threadIdx.x == 0) sm.p.idx = atomicAdd(&ctl->take[slot], 1);
                     __syncthreads();
                     const int idx = sm.p.idx;
                     __syncthreads();
+                    if (threadIdx.x == 0) atomicAdd(&ctl->cyc_take, (unsigned long long)(clock64() - ct));
                     if (idx >= n) break;
                     push_tile(b, b.lists[(size_t)slot * b.list_cap + idx], prm, p, sm.p);
                     if (threadIdx.x == 0) atomicAdd(&ctl->push_tiles, 1ull);

@@ -58,6 +58,8 @@ struct Ctl {
     // device time per phase (ns, %globaltimer read by block 0 at barriers)
     unsigned long long t_init, t_gr, t_count, t_push, t_reach;
     unsigned long long push_sweeps, push_bfs;
+    // SM cycles per section of the push visits, summed over visits
+    unsigned long long cyc_load, cyc_bfs, cyc_sweep, cyc_wb, cyc_take;
 };
 
 struct Batch {
@@ -85,7 +87,8 @@ struct SolveParams {
     int max_outer;     // outer iterations (global relabel + push rounds)
     int push_rounds;   // checkerboard rounds between global relabels
     int max_sweeps;    // push/relabel sweeps per tile visit
-    int bfs_every;     // exact local relabel every this many sweeps
+    int bfs_every;     // exact local relabel at least every this many sweeps
+    int bfs_first;     // exact local relabel at the start of every tile visit
     int max_rounds;    // cap on BFS rounds of one global relabel / reach pass
 };
 

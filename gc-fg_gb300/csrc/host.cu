@@ -41,7 +41,7 @@ static gcfg_status grow_host(T *&p, size_t &cap, size_t need) {
 
 struct Engine {
     cudaStream_t st = nullptr;
-    SolveParams prm{64, 4, 64, 16, 1 << 20};
+    SolveParams prm{64, 4, 64, 16, 0, 1 << 20};
 
     int n_img = 0, n_tiles = 0;
     long long n_px = 0, total_chunks = 0;
@@ -293,6 +293,11 @@ struct Engine {
         r->t_count_ms = h_ctl->t_count * 1e-6f;
         r->t_push_ms = h_ctl->t_push * 1e-6f;
         r->t_reach_ms = h_ctl->t_reach * 1e-6f;
+        r->cyc_load = (long long)h_ctl->cyc_load;
+        r->cyc_local_relabel = (long long)h_ctl->cyc_bfs;
+        r->cyc_sweeps = (long long)h_ctl->cyc_sweep;
+        r->cyc_writeback = (long long)h_ctl->cyc_wb;
+        r->cyc_take = (long long)h_ctl->cyc_take;
         r->ms = ms;
     }
 };

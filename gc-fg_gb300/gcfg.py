@@ -52,7 +52,8 @@ class Result(C.Structure):
                 ("gr_tiles", C.c_int64), ("push_sweeps", C.c_int64),
                 ("push_local_relabels", C.c_int64), ("t_global_relabel_ms", C.c_float),
                 ("t_count_ms", C.c_float), ("t_push_ms", C.c_float), ("t_reach_ms", C.c_float),
-                ("ms", C.c_float)]
+                ("cyc_load", C.c_int64), ("cyc_local_relabel", C.c_int64), ("cyc_sweeps", C.c_int64),
+                ("cyc_writeback", C.c_int64), ("cyc_take", C.c_int64), ("ms", C.c_float)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -60,6 +60,9 @@ typedef struct {
     int64_t push_sweeps;     /* push/relabel sweeps summed over tile visits */
     int64_t push_local_relabels; /* exact local (tile BFS) relabels in push visits */
     float t_global_relabel_ms, t_count_ms, t_push_ms, t_reach_ms; /* device time per phase */
+    /* SM cycles summed over push tile visits, per section (load, local
+     * relabel, sweeps, write-back + hand-over, queue take) */
+    int64_t cyc_load, cyc_local_relabel, cyc_sweeps, cyc_writeback, cyc_take;
     float ms;                /* device time of the solve (CUDA events) */
 } gcfg_result;
 
