@@ -17,6 +17,8 @@ OBJ_DIR = os.path.join(HERE, "_build")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# extra nvcc flags for experiments (e.g. -DGCFG_SOLVE_MIN_BLOCKS=4)
+FLAGS += os.environ.get("GCFG_NVCC_EXTRA", "").split()
 
 
 def sources():

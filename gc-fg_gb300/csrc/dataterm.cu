@@ -13,10 +13,11 @@
 // (solveMRF.cu:87-90) that InitGraphVarEdges consumes
 // (GraphCutKernels.cu:165-214).
 //
-// Exactness: per image, the -log values of the 4096 bins and the weights of
-// every ||dI||^2 that can round to a non-zero capacity are evaluated once in
-// double precision into small tables; the per-pixel passes are integer
-// gathers, so the int32 capacities match the CPU oracle bit for bit.
+// Exactness: the CPU oracle evaluates these expressions in double precision.
+// Here the 4096 per-bin t-links of an image go into a table, and the n-link
+// of every pixel pair is evaluated directly; both use a float evaluation
+// whenever it is provably far from a rounding boundary and the oracle's
+// double expression otherwise, so every int32 capacity matches bit for bit.
 #include "dataterm.cuh"
 
 namespace gcfg {
@@ -42,57 +43,136 @@ __device__ __forceinline__ int chunk_image(const long long *__restrict__ chunk_o
     return lo;
 }
 
-// Scribble histograms: privatised per block in shared memory, with warp
-// aggregation of equal bins (__match_any_sync) before the shared atomics.
-__global__ void __launch_bounds__(256) k_hist_b(const uint8_t *__restrict__ rgb,
-                                                const uint8_t *__restrict__ scrib,
-                                                const ImgDesc *__restrict__ img,
-                                                const long long *__restrict__ chunk_off, int n_img,
-                                                int *__restrict__ hist) {
-    __shared__ int sh[2 * NBINS];
-    const int im = chunk_image(chunk_off, n_img, blockIdx.x);
-    const long long n = (long long)img[im].W * img[im].H;
-    const long long first = ((long long)blockIdx.x - chunk_off[im]) * CHUNK_PX;
-    const long long last = min(n, first + CHUNK_PX);
-    const long long pix0 = img[im].pix0;
-    for (int i = threadIdx.x; i < 2 * NBINS; i += blockDim.x) sh[i] = 0;
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    for (long long base = first + (threadIdx.x & ~31); base < last; base += blockDim.x) {
-        const long long i = base + lane;
-        int key = -1;
-        if (i < last) {
-            const int s = scrib[pix0 + i];
-            if (s == 1 || s == 2) key = (s - 1) * NBINS + color_bin3(rgb + 3 * (pix0 + i));
-        }
-        const unsigned same = __match_any_sync(0xffffffffu, key);
-        if (key >= 0 && lane == __ffs(same) - 1) atomicAdd(&sh[key], __popc(same));
-    }
-    __syncthreads();
-    int *dst = hist + (size_t)im * 2 * NBINS;
-    for (int i = threadIdx.x; i < 2 * NBINS; i += blockDim.x)
-        if (sh[i]) atomicAdd(dst + i, sh[i]);
+// ---------------------------------------------------------------------------
+// Quantised table entries.  The reference value is the double expression
+// the CPU oracle evaluates; a float evaluation decides the rounding whenever
+// it lies farther from a .5 boundary than its proven error, and the double
+// expression is evaluated only for the near-ties that remain.
+// ---------------------------------------------------------------------------
+
+// 10 * -ln((h + 1) / N) in double (the oracle's expression).  Not inlined,
+// so that the compiler cannot speculate it into the float fast path.
+__device__ __noinline__ double tlink_raw(int h, long long N) {
+    const double p = (double)(h + 1) / (double)N;
+    return 10.0 * -log(p);
 }
 
-// Sum of ||dI||^2 over all right and down neighbour pairs, exact int64.
-__global__ void __launch_bounds__(256) k_sigma_b(const uint8_t *__restrict__ rgb,
-                                                 const ImgDesc *__restrict__ img,
-                                                 const long long *__restrict__ chunk_off, int n_img,
-                                                 ImgState *ist) {
+// round(10 * -ln((h+1)/N)).  Float error: the ratio carries <= 3 ulp
+// (conversions and division, 1.8e-7 relative), which moves the log by
+// <= 1.8e-7; logf adds <= 1 ulp of a result <= 22 (2.7e-6); times 10:
+// < 3e-5.  Margin used: 1e-3.
+__device__ __forceinline__ int tlink_quant(int h, long long N) {
+    const float pf = (float)(h + 1) / (float)N;
+    const float v = -10.0f * logf(pf);
+    const float fr = v - floorf(v);
+    if (fabsf(fr - 0.5f) > 1e-3f) return (int)floorf(v + 0.5f);
+    return (int)round(tlink_raw(h, N));
+}
+
+// round(lambda * exp(-d2 / (2 s2))).  Float error: the exponent a carries
+// <= 3 ulp relative (1.8e-7 * |a|), expf <= 2 ulp, the product <= 1 ulp, so
+// the float value v is off by < v * 2e-7 * (|a| + 4).  A wrong rounding needs
+// v within that error of some k + 0.5, where |a| = ln(lambda / (k + 0.5))
+// <= ln(2 lambda): the error is then < lambda * 2e-7 * (ln(2 lambda) + 4),
+// below the margin 1e-5 * lambda + 1e-5 for every lambda up to 2^28.
+// (Large |a| only make v smaller: it underflows toward 0 and rounds to 0.)
+struct NlinkParams {
+    float lf, inv;       // (float)lambda, (float)(1 / (2 sigma^2))
+    int constant;        // constant image: every weight is const_w = round(lambda)
+    int const_w;
+    double lambda, s2;   // only read on the exact (near-tie) path
+};
+
+// round(lambda * exp(-d2 / (2 s2))) in double: the oracle's expression.  Not
+// inlined, so that it cannot be speculated into the float fast path.
+__device__ __noinline__ int nlink_exact(int d2, double lambda, double s2) {
+    const double a = -(double)d2 / (2.0 * s2);
+    return (int)round(lambda * exp(a));
+}
+
+// sigma^2 and 1 / (2 sigma^2) of each image, once per image.
+__global__ void k_img_params(const ImgDesc *__restrict__ img, int n_img, ImgState *ist) {
+    const int im = blockIdx.x * blockDim.x + threadIdx.x;
+    if (im >= n_img) return;
+    const unsigned long long s = ist[im].sigma_sum;
+    const long long count = (long long)(img[im].W - 1) * img[im].H + (long long)img[im].W * (img[im].H - 1);
+    const double s2 = (s == 0 || count == 0) ? 0.0 : (double)s / (double)count;
+    ist[im].s2 = s2;
+    ist[im].inv2s2 = s2 > 0.0 ? (float)(1.0 / (2.0 * s2)) : 0.f;
+    ist[im].lambda_f = (float)img[im].lambda;
+    ist[im].const_w = (int)round(img[im].lambda);
+}
+
+__device__ __forceinline__ NlinkParams nlink_params(double lambda, const ImgState &st) {
+    NlinkParams q;
+    q.lambda = lambda;
+    q.s2 = st.s2;
+    q.lf = st.lambda_f;
+    q.inv = st.inv2s2;
+    q.constant = st.inv2s2 == 0.f;
+    q.const_w = st.const_w;
+    return q;
+}
+
+__device__ __forceinline__ int nlink_quant(int d2, const NlinkParams &q) {
+    const float v = q.lf * expf(-(float)d2 * q.inv);
+    const float fr = v - floorf(v);
+    if (fabsf(fr - 0.5f) > 1e-5f * q.lf + 1e-5f) return (int)floorf(v + 0.5f);
+    return nlink_exact(d2, q.lambda, q.s2);
+}
+
+// One pass over a chunk of an image: the scribble colour histograms
+// (privatised per block in shared memory, equal bins of a warp aggregated
+// with __match_any_sync before the shared atomics) and the exact sum of
+// ||dI||^2 over right and down neighbour pairs (for sigma^2).
+__global__ void __launch_bounds__(256) k_hist_sigma_b(const uint8_t *__restrict__ rgb,
+                                                      const uint8_t *__restrict__ scrib,
+                                                      const ImgDesc *__restrict__ img,
+                                                      const long long *__restrict__ chunk_off, int n_img,
+                                                      int *__restrict__ hist, ImgState *ist) {
+    __shared__ int sh[2 * NBINS];
     const int im = chunk_image(chunk_off, n_img, blockIdx.x);
     const int W = img[im].W, H = img[im].H;
-    const long long n = (long long)W * H;
-    const long long first = ((long long)blockIdx.x - chunk_off[im]) * CHUNK_PX;
-    const long long last = min(n, first + CHUNK_PX);
-    const uint8_t *base = rgb + 3 * img[im].pix0;
+    const int rows = img[im].rows_per_chunk;
+    const int y0 = (int)((long long)blockIdx.x - chunk_off[im]) * rows;
+    const int y1 = min(H, y0 + rows);
+    const long long pix0 = img[im].pix0;
+    const uint8_t *base = rgb + 3 * pix0;
+    const bool do_hist = scrib != nullptr;
+    if (do_hist)
+        for (int i = threadIdx.x; i < 2 * NBINS; i += blockDim.x) sh[i] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned long long acc = 0;
-    for (long long i = first + threadIdx.x; i < last; i += blockDim.x) {
-        const int x = (int)(i % W), y = (int)(i / W);
-        const uint8_t *p = base + 3 * i;
-        if (x + 1 < W) acc += (unsigned)diff2p(p, p + 3);
-        if (y + 1 < H) acc += (unsigned)diff2p(p, p + 3 * (long long)W);
+    // warps take rows, lanes take columns: no per-pixel division, and every
+    // lane of a warp runs the same iterations (full-warp collectives)
+    for (int y = y0 + warp; y < y1; y += blockDim.x >> 5) {
+        for (int xb = 0; xb < W; xb += 32) {
+            const int x = xb + lane;
+            int key = -1;
+            if (x < W) {
+                const long long i = (long long)y * W + x;
+                const uint8_t *p = base + 3 * i;
+                if (x + 1 < W) acc += (unsigned)diff2p(p, p + 3);
+                if (y + 1 < H) acc += (unsigned)diff2p(p, p + 3 * (long long)W);
+                if (do_hist) {
+                    const int sc = scrib[pix0 + i];
+                    if (sc == 1 || sc == 2) key = (sc - 1) * NBINS + color_bin3(p);
+                }
+            }
+            if (do_hist) {
+                const unsigned same = __match_any_sync(0xffffffffu, key);
+                if (key >= 0 && lane == __ffs(same) - 1) atomicAdd(&sh[key], __popc(same));
+            }
+        }
     }
     warp_atomic_add_u64(&ist[im].sigma_sum, acc);
+    if (do_hist) {
+        __syncthreads();
+        int *dst = hist + (size_t)im * 2 * NBINS;
+        for (int i = threadIdx.x; i < 2 * NBINS; i += blockDim.x)
+            if (sh[i]) atomicAdd(dst + i, sh[i]);
+    }
 }
 
 // Per-bin t-link tables (one block per image, double precision).
@@ -132,70 +212,35 @@ __global__ void __launch_bounds__(1024) k_tlut_b(const int *__restrict__ hist, i
         }
     }
     __syncthreads();
-    const double df = (double)(part[0][0] + NBINS), db = (double)(part[1][0] + NBINS);
+    const long long Nf = part[0][0] + NBINS, Nb = part[1][0] + NBINS;
     for (int b = threadIdx.x; b < NBINS; b += blockDim.x) {
-        const double pf = (double)(hf[b] + 1) / df;
-        const double pb = (double)(hb[b] + 1) / db;
-        const double rdn = 10.0 * -log(pf);
-        const double rdp = 10.0 * -log(pb);
-        dp_lut[(size_t)im * NBINS + b] = (int)round(rdp);
-        dn_lut[(size_t)im * NBINS + b] = (int)round(rdn);
-        if (raw_dp) raw_dp[(size_t)im * NBINS + b] = rdp;
-        if (raw_dn) raw_dn[(size_t)im * NBINS + b] = rdn;
+        int qdp, qdn;
+        if (raw_dp || raw_dn) {
+            const double rdp = tlink_raw(hb[b], Nb), rdn = tlink_raw(hf[b], Nf);
+            qdp = (int)round(rdp);
+            qdn = (int)round(rdn);
+            if (raw_dp) raw_dp[(size_t)im * NBINS + b] = rdp;
+            if (raw_dn) raw_dn[(size_t)im * NBINS + b] = rdn;
+        } else {
+            qdp = tlink_quant(hb[b], Nb);
+            qdn = tlink_quant(hf[b], Nf);
+        }
+        dp_lut[(size_t)im * NBINS + b] = qdp;
+        dn_lut[(size_t)im * NBINS + b] = qdn;
     }
 }
 
-// Length of each image's n-link table: beyond d2lim every weight rounds to 0
-// (lambda * exp(-d2 / 2 sigma^2) < 0.5 with a margin far above rounding error).
-__global__ void k_d2lim_b(const ImgDesc *__restrict__ img, int n_img, ImgState *ist) {
-    const int im = blockIdx.x * blockDim.x + threadIdx.x;
-    if (im >= n_img) return;
-    const int W = img[im].W, H = img[im].H;
-    const double lambda = img[im].lambda;
-    const unsigned long long s = ist[im].sigma_sum;
-    const long long count = (long long)(W - 1) * H + (long long)W * (H - 1);
-    int lim;
-    if (s == 0 || count == 0 || lambda < 0.5) {
-        lim = 0;
-    } else {
-        const double s2 = (double)s / (double)count;
-        const double x = 2.0 * s2 * (log(2.0 * lambda) + 1e-9) + 2.0;
-        lim = x >= (double)MAX_D2 ? MAX_D2 : (int)ceil(x);
-    }
-    ist[im].d2lim = lim;
-}
-
-// N-link weight for every ||dI||^2 up to d2lim (double precision).
-__global__ void k_wlut_b(const ImgDesc *__restrict__ img, const ImgState *__restrict__ ist,
-                         int *__restrict__ wlut) {
-    const int im = blockIdx.y;
-    const int d2 = blockIdx.x * blockDim.x + threadIdx.x;
-    if (d2 > ist[im].d2lim) return;
-    const int W = img[im].W, H = img[im].H;
-    const unsigned long long s = ist[im].sigma_sum;
-    const long long count = (long long)(W - 1) * H + (long long)W * (H - 1);
-    const double lambda = img[im].lambda;
-    double w;
-    if (s == 0 || count == 0) {
-        w = lambda;
-    } else {
-        const double s2 = (double)s / (double)count;
-        const double a = -(double)d2 / (2.0 * s2);
-        w = lambda * exp(a);
-    }
-    wlut[(size_t)im * WLUT_STRIDE + d2] = (int)round(w);
-}
-
-__device__ __forceinline__ int nlink_w(const int *__restrict__ wl, int lim, int d2) {
-    return d2 <= lim ? __ldg(wl + d2) : 0;
+// N-link weight of a pair at squared colour distance d2 (s2 = sigma^2,
+// 0 for a constant image, whose weights are all lambda).
+__device__ __forceinline__ int nlink_w(int d2, const NlinkParams &q) {
+    return q.constant ? q.const_w : nlink_quant(d2, q);
 }
 
 // Fused image -> residual graph of one tile: t-link gather, n-link gather,
 // the reference's interior/border conventions, tile-major output.
 __global__ void __launch_bounds__(TILE_THREADS) k_build_img_b(Batch b, const uint8_t *__restrict__ rgb,
                                                                const int *__restrict__ dp_lut,
-                                                               const int *__restrict__ dn_lut,
-                                                               const int *__restrict__ wlut) {
+                                                               const int *__restrict__ dn_lut) {
     const int t = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int im = __ldg(b.tile_img + t);
@@ -203,8 +248,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_build_img_b(Batch b, const uin
     const int lt = t - d.tile0;
     const int tx = lt % d.tiles_x, ty = lt / d.tiles_x;
     const int W = d.W, H = d.H;
-    const int lim = b.ist[im].d2lim;
-    const int *wl = wlut + (size_t)im * WLUT_STRIDE;
+    const NlinkParams q = nlink_params(d.lambda, b.ist[im]);
     const int *dpl = dp_lut + (size_t)im * NBINS;
     const int *dnl = dn_lut + (size_t)im * NBINS;
     const uint8_t *base = rgb + 3 * d.pix0;
@@ -223,10 +267,10 @@ __global__ void __launch_bounds__(TILE_THREADS) k_build_img_b(Batch b, const uin
             const int vdp = __ldg(dpl + bin);
             if ((long long)x + (long long)y * w32 < (long long)W * H && vdp > 0) rinit += (unsigned)vdp;
             if (x > 0 && y > 0 && x < W - 1 && y < H - 1) {
-                c.x = x == 1 ? 0 : nlink_w(wl, lim, diff2p(p, p - 3));
-                c.y = x == W - 2 ? 0 : nlink_w(wl, lim, diff2p(p, p + 3));
-                c.z = y == 1 ? 0 : nlink_w(wl, lim, diff2p(p, p - 3 * (long long)W));
-                c.w = y == H - 2 ? 0 : nlink_w(wl, lim, diff2p(p, p + 3 * (long long)W));
+                c.x = x == 1 ? 0 : nlink_w(diff2p(p, p - 3), q);
+                c.y = x == W - 2 ? 0 : nlink_w(diff2p(p, p + 3), q);
+                c.z = y == 1 ? 0 : nlink_w(diff2p(p, p - 3 * (long long)W), q);
+                c.w = y == H - 2 ? 0 : nlink_w(diff2p(p, p + 3 * (long long)W), q);
                 e = vdp - __ldg(dnl + bin);
                 idp += (unsigned)vdp;
             }
@@ -253,20 +297,21 @@ __global__ void k_tlinks_apply(const uint8_t *__restrict__ rgb, long long n,
     dn[i] = __ldg(dn_lut + bin);
 }
 
-__global__ void k_nlinks_apply(const uint8_t *__restrict__ rgb, int W, int H, const ImgState *ist,
-                               const int *__restrict__ wl, int *__restrict__ up,
-                               int *__restrict__ down, int *__restrict__ left,
-                               int *__restrict__ right) {
+__global__ void k_nlinks_apply(const uint8_t *__restrict__ rgb, const ImgDesc *__restrict__ img,
+                               const ImgState *ist, int *__restrict__ up, int *__restrict__ down,
+                               int *__restrict__ left, int *__restrict__ right) {
+    const ImgDesc d = img[0];
+    const int W = d.W, H = d.H;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= W || y >= H) return;
-    const int lim = ist[0].d2lim;
+    const NlinkParams q = nlink_params(d.lambda, ist[0]);
     const long long i = (long long)y * W + x;
     const uint8_t *p = rgb + 3 * i;
-    left[i] = x > 0 ? nlink_w(wl, lim, diff2p(p, p - 3)) : 0;
-    right[i] = x + 1 < W ? nlink_w(wl, lim, diff2p(p, p + 3)) : 0;
-    up[i] = y > 0 ? nlink_w(wl, lim, diff2p(p, p - 3 * (long long)W)) : 0;
-    down[i] = y + 1 < H ? nlink_w(wl, lim, diff2p(p, p + 3 * (long long)W)) : 0;
+    left[i] = x > 0 ? nlink_w(diff2p(p, p - 3), q) : 0;
+    right[i] = x + 1 < W ? nlink_w(diff2p(p, p + 3), q) : 0;
+    up[i] = y > 0 ? nlink_w(diff2p(p, p - 3 * (long long)W), q) : 0;
+    down[i] = y + 1 < H ? nlink_w(diff2p(p, p + 3 * (long long)W), q) : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -275,25 +320,21 @@ __global__ void k_nlinks_apply(const uint8_t *__restrict__ rgb, int W, int H, co
 
 gcfg_status dt_tables(const DtArgs &a, cudaStream_t st) {
     // a.scrib == NULL: n-link tables only (the colour histograms need scribbles)
-    if (a.scrib) {
-        GCFG_CK(cudaMemsetAsync(a.hist, 0, (size_t)a.n_img * 2 * NBINS * sizeof(int), st));
-        GCFG_LAUNCH(GCFG_PK_HIST, st,
-                    k_hist_b<<<a.total_chunks, 256, 0, st>>>(a.rgb, a.scrib, a.img, a.chunk_off, a.n_img, a.hist));
+    if (a.scrib) GCFG_CK(cudaMemsetAsync(a.hist, 0, (size_t)a.n_img * 2 * NBINS * sizeof(int), st));
+    GCFG_LAUNCH(GCFG_PK_HIST, st,
+                k_hist_sigma_b<<<a.total_chunks, 256, 0, st>>>(a.rgb, a.scrib, a.img, a.chunk_off, a.n_img,
+                                                               a.hist, a.ist));
+    GCFG_LAUNCH(GCFG_PK_TLUT, st, k_img_params<<<div_up(a.n_img, 128), 128, 0, st>>>(a.img, a.n_img, a.ist));
+    if (a.scrib)
         GCFG_LAUNCH(GCFG_PK_TLUT, st,
                     k_tlut_b<<<a.n_img, 1024, 0, st>>>(a.hist, a.dp_lut, a.dn_lut, a.raw_dp, a.raw_dn));
-    }
-    GCFG_LAUNCH(GCFG_PK_SIGMA, st,
-                k_sigma_b<<<a.total_chunks, 256, 0, st>>>(a.rgb, a.img, a.chunk_off, a.n_img, a.ist));
-    GCFG_LAUNCH(GCFG_PK_WLUT, st, k_d2lim_b<<<div_up(a.n_img, 128), 128, 0, st>>>(a.img, a.n_img, a.ist));
-    GCFG_LAUNCH(GCFG_PK_WLUT, st,
-                k_wlut_b<<<dim3(div_up(MAX_D2 + 1, 256), a.n_img), 256, 0, st>>>(a.img, a.ist, a.wlut));
     GCFG_CK(cudaGetLastError());
     return GCFG_OK;
 }
 
 gcfg_status dt_build(const Batch &b, const DtArgs &a, cudaStream_t st) {
     GCFG_LAUNCH(GCFG_PK_BUILD, st,
-                k_build_img_b<<<b.n_tiles, TILE_THREADS, 0, st>>>(b, a.rgb, a.dp_lut, a.dn_lut, a.wlut));
+                k_build_img_b<<<b.n_tiles, TILE_THREADS, 0, st>>>(b, a.rgb, a.dp_lut, a.dn_lut));
     GCFG_CK(cudaGetLastError());
     return GCFG_OK;
 }
@@ -309,7 +350,7 @@ gcfg_status dt_apply_nlinks(const DtArgs &a, int W, int H, int *up, int *down, i
                             cudaStream_t st) {
     dim3 blk(32, 8), grd(div_up(W, 32), div_up(H, 8));
     GCFG_LAUNCH(GCFG_PK_OTHER, st,
-                k_nlinks_apply<<<grd, blk, 0, st>>>(a.rgb, W, H, a.ist, a.wlut, up, down, left, right));
+                k_nlinks_apply<<<grd, blk, 0, st>>>(a.rgb, a.img, a.ist, up, down, left, right));
     GCFG_CK(cudaGetLastError());
     return GCFG_OK;
 }

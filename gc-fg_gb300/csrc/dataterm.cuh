@@ -6,12 +6,10 @@
 namespace gcfg {
 
 constexpr int NBINS = 4096;                   // 16^3 colour bins per class
-constexpr int MAX_D2 = 3 * 255 * 255;         // largest ||dI||^2 of two RGB pixels
-constexpr int WLUT_STRIDE = MAX_D2 + 1;       // n-link table entries per image
-constexpr int CHUNK_PX = 8192;                // pixels per block in per-image passes
+constexpr int CHUNK_PX = 8192;                // pixels per block in per-image passes (about)
 
 // Device buffers of the data term for a batch (per image: 2*4096 histogram
-// bins, 4096 dp and dn entries, WLUT_STRIDE n-link weights).
+// bins, 4096 dp and dn entries).
 struct DtArgs {
     int n_img;
     long long total_chunks;
@@ -23,7 +21,6 @@ struct DtArgs {
     int *hist;
     int *dp_lut, *dn_lut;
     double *raw_dp, *raw_dn;  // optional (NULL): pre-rounding per-bin values
-    int *wlut;
 };
 
 gcfg_status dt_tables(const DtArgs &a, cudaStream_t st);

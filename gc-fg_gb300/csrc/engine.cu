@@ -544,7 +544,11 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
 // The persistent solve kernel
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(TILE_THREADS, 2) k_solve(Batch b, SolveParams prm) {
+#ifndef GCFG_SOLVE_MIN_BLOCKS
+#define GCFG_SOLVE_MIN_BLOCKS 4   // blocks of the persistent kernel per SM (register budget)
+#endif
+
+__global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(Batch b, SolveParams prm) {
     __shared__ Smem sm;
     Ctl *ctl = b.ctl;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

@@ -26,6 +26,8 @@ struct ImgDesc {
     int tile0, n_tiles;
     long long pix0;   // offset of the image in packed row-major inputs/outputs
     double lambda;
+    int rows_per_chunk;  // rows of the image per block in the per-image passes
+    int pad;
 };
 
 // Per-image state written by the device.
@@ -35,9 +37,11 @@ struct ImgState {
     unsigned long long pos_excess;   // sum of positive excess (last count)
     unsigned long long active;       // active nodes (last count)
     unsigned long long sigma_sum;    // sum of ||dI||^2 over neighbour pairs
+    double s2;                       // sigma^2 = sigma_sum / pairs (0: constant image)
+    float inv2s2;                    // (float)(1 / (2 sigma^2))
+    float lambda_f;                  // (float)lambda
+    int const_w;                     // round(lambda): every weight of a constant image
     int done;
-    int d2lim;                       // n-link table length - 1
-    int pad[2];
 };
 
 enum { L_PUSH0 = 0, L_PUSH1, L_PUSH2, L_GR0, L_GR1, L_NLISTS };

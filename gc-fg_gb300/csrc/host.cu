@@ -66,7 +66,6 @@ struct Engine {
     int *d_dpl = nullptr; size_t c_dpl = 0;
     int *d_dnl = nullptr; size_t c_dnl = 0;
     double *d_raw = nullptr; size_t c_raw = 0;
-    int *d_wlut = nullptr; size_t c_wlut = 0;
     // staging for host entry points
     uint8_t *d_rgb = nullptr; size_t c_rgb = 0;
     uint8_t *d_scrib = nullptr; size_t c_scrib = 0;
@@ -88,7 +87,7 @@ struct Engine {
         cudaFree(d_tmask); cudaFree(d_tact); cudaFree(d_tpos);
         cudaFree(d_lists);
         cudaFree(d_mpush); cudaFree(d_mgr); cudaFree(d_ctl);
-        cudaFree(d_hist); cudaFree(d_dpl); cudaFree(d_dnl); cudaFree(d_raw); cudaFree(d_wlut);
+        cudaFree(d_hist); cudaFree(d_dpl); cudaFree(d_dnl); cudaFree(d_raw);
         cudaFree(d_rgb); cudaFree(d_scrib); cudaFree(d_smin); cudaFree(d_smax);
         if (h_img) cudaFreeHost(h_img);
         if (h_ist) cudaFreeHost(h_ist);
@@ -102,7 +101,7 @@ struct Engine {
         d_tmask = nullptr; d_tact = nullptr; d_tpos = nullptr;
         d_lists = nullptr;
         d_mpush = d_mgr = nullptr; d_ctl = nullptr;
-        d_hist = d_dpl = d_dnl = nullptr; d_raw = nullptr; d_wlut = nullptr;
+        d_hist = d_dpl = d_dnl = nullptr; d_raw = nullptr;
         d_rgb = d_scrib = d_smin = d_smax = nullptr;
         h_img = nullptr; h_ist = nullptr; h_chunk = nullptr; h_tile_img = nullptr; h_ctl = nullptr;
         ev0 = ev1 = nullptr;
@@ -154,7 +153,6 @@ struct Engine {
             GCFG_TRY(grow(d_hist, c_hist, (size_t)imgs * 2 * NBINS));
             GCFG_TRY(grow(d_dpl, c_dpl, (size_t)imgs * NBINS));
             GCFG_TRY(grow(d_dnl, c_dnl, (size_t)imgs * NBINS));
-            GCFG_TRY(grow(d_wlut, c_wlut, (size_t)imgs * WLUT_STRIDE));
         }
         if (staging) {
             GCFG_TRY(grow(d_rgb, c_rgb, (size_t)px * 3));
@@ -192,10 +190,11 @@ struct Engine {
             d.lambda = lam ? lam[i] : 0.0;
             if (arena)
                 for (int k = 0; k < d.n_tiles; ++k) h_tile_img[t + k] = i;
+            d.rows_per_chunk = W[i] >= CHUNK_PX ? 1 : CHUNK_PX / W[i];
             h_chunk[i] = ch;
             t += d.n_tiles;
             p += (long long)W[i] * H[i];
-            ch += ((long long)W[i] * H[i] + CHUNK_PX - 1) / CHUNK_PX;
+            ch += (H[i] + d.rows_per_chunk - 1) / d.rows_per_chunk;
         }
         h_chunk[n] = ch;
         n_img = n;
@@ -246,7 +245,6 @@ struct Engine {
         a.dn_lut = d_dnl;
         a.raw_dp = nullptr;
         a.raw_dn = nullptr;
-        a.wlut = d_wlut;
         return a;
     }
 

@@ -234,3 +234,25 @@ def test_batch_params_do_not_change_result(params):
     flows, _ = bs.run(Ws, Hs, [50.0] * 12, dev(rgb), dev(scrib))
     for i, (r, s) in enumerate(imgs):
         assert flows[i] == O.segment(r, s, 50.0)["flow"]
+
+
+@pytest.mark.parametrize("cfg,W,H,seed", [(0, 256, 256, 0), (1, 400, 300, 11), (2, 512, 512, 2), (3, 97, 61, 1003)])
+@pytest.mark.parametrize("lam", [0.3, 0.5, 1.0, 7.7, 37.3, 50.0, 200.0, 1000.0, 12345.6])
+def test_nlinks_bit_exact_many(cfg, W, H, seed, lam):
+    """The n-link table (float fast path, double fallback near .5) equals
+    the oracle's double evaluation for every weight."""
+    rgb, _ = O.generate(cfg, W, H, seed)
+    outs = [torch.empty((H, W), dtype=torch.int32, device="cuda") for _ in range(4)]
+    gcfg.nlinks(dev(rgb), W, H, lam, *outs)
+    for a, b in zip(outs, O.nlinks(rgb, lam)):
+        assert np.array_equal(a.cpu().numpy(), b)
+
+
+@pytest.mark.parametrize("cfg,W,H,seed", [(0, 256, 256, 0), (1, 640, 360, 4), (2, 700, 500, 9), (3, 40, 120, 1010)])
+def test_tlinks_bit_exact_many(cfg, W, H, seed):
+    rgb, scrib = O.generate(cfg, W, H, seed)
+    dp = torch.empty((H, W), dtype=torch.int32, device="cuda")
+    dn = torch.empty_like(dp)
+    gcfg.tlinks(dev(rgb), dev(scrib), dp, dn)
+    odp, odn = O.tlinks(rgb, scrib)
+    assert np.array_equal(dp.cpu().numpy(), odp) and np.array_equal(dn.cpu().numpy(), odn)
