@@ -643,6 +643,7 @@ const char *gcfg_strerror(gcfg_status s) {
     case GCFG_ERR_NOT_CONVERGED: return "iteration cap reached";
     case GCFG_ERR_STATE: return "call out of order";
     case GCFG_ERR_CAPACITY: return "admission refused: memory cap";
+    case GCFG_ERR_TOO_LARGE: return "image larger than the fixed working memory of the allocation-free solve";
     }
     return "unknown";
 }

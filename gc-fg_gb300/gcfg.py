@@ -23,7 +23,9 @@ GCFG_ERR_CUDA = 3
 GCFG_ERR_NOT_CONVERGED = 4
 GCFG_ERR_STATE = 5
 GCFG_ERR_CAPACITY = 6
+GCFG_ERR_TOO_LARGE = 7
 GCFG_MAX_CAP = (1 << 28) - 1
+GCFG_NOALLOC_MAX_TILES = 640
 
 # Every function declared in include/gcfg.h (checked by the CPU test suite).
 EXPORTS = [
@@ -33,6 +35,7 @@ EXPORTS = [
     "gcfg_seg_set_stream", "gcfg_seg_destroy", "gcfg_strerror", "gcfg_launch_count",
     "gcfg_profile_enable", "gcfg_profile_read", "gcfg_batch_create", "gcfg_batch_set_stream",
     "gcfg_batch_set_params", "gcfg_batch_run", "gcfg_batch_run_host", "gcfg_batch_destroy",
+    "gcfg_solve_noalloc",
 ]
 
 PROF_KINDS = ["hist", "tlut", "sigma", "wlut", "build", "solve", "extract", "other"]
@@ -103,6 +106,7 @@ def load(path: str = LIB_PATH):
         "gcfg_batch_run": (S, [P, I, P, P, P, P, P, P, P, P, P]),
         "gcfg_batch_run_host": (S, [P, I, P, P, P, P, P, P, P, P, P]),
         "gcfg_batch_destroy": (S, [P]),
+        "gcfg_solve_noalloc": (S, [I, I, P, P, C.c_int32, P, P, P, P, P, C.POINTER(C.c_int64), P]),
         "gcfg_profile_enable": (S, [I]),
         "gcfg_profile_read": (S, [C.POINTER(ProfEntry), I, C.POINTER(I)]),
     }

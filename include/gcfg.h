@@ -36,7 +36,8 @@ typedef enum {
     GCFG_ERR_CUDA = 3,            /* a CUDA call failed */
     GCFG_ERR_NOT_CONVERGED = 4,   /* an iteration cap was reached */
     GCFG_ERR_STATE = 5,           /* call out of order (e.g. optimize before set_graph) */
-    GCFG_ERR_CAPACITY = 6         /* admission refused: over the memory cap */
+    GCFG_ERR_CAPACITY = 6,        /* admission refused: over the memory cap */
+    GCFG_ERR_TOO_LARGE = 7        /* larger than the fixed working memory of gcfg_solve_noalloc */
 } gcfg_status;
 
 /* Largest accepted capacity (t-links and n-links).  Keeps every excess and
@@ -165,6 +166,40 @@ gcfg_status gcfg_batch_run_host(gcfg_batch *b, int n, const int *widths, const i
                                 uint8_t *h_smin, uint8_t *h_smax, int64_t *h_flows,
                                 gcfg_result *h_res);
 gcfg_status gcfg_batch_destroy(gcfg_batch *b);
+
+/* ---------------- allocation-free solve ---------------- */
+
+/* Largest image of gcfg_solve_noalloc, in 32x32 tiles, and the size of the
+ * fixed device array that holds its working memory. */
+#define GCFG_NOALLOC_MAX_TILES 640
+#define GCFG_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* Solves one graph like gcfg_init + gcfg_optimize, but allocates nothing:
+ * no cudaMalloc, cudaFree or other allocating call.  It has no counterpart in
+ * the reference.  It is for callers that cannot allocate device memory at
+ * solve time: a host framework that owns all of the GPU's memory and forbids
+ * plug-ins to allocate, a process already at its device-memory limit, or a
+ * latency-bound loop that cannot afford the device-wide synchronisation that
+ * cudaMalloc/cudaFree can cause.  Its working memory is one fixed file-scope
+ * device array of GCFG_NOALLOC_SCRATCH_BYTES (16 MiB) that every GPU loading
+ * this library holds until the process exits.
+ *
+ * Inputs as in gcfg_init (device arrays, caller-owned; up == NULL selects the
+ * constant penalty).  Outputs: d_label (device, W*H int32) receives the
+ * labels gcfg_optimize returns; *h_flow (host, may be NULL) the exact flow.
+ * Limits: ceil(w/32) * ceil(h/32) <= GCFG_NOALLOC_MAX_TILES (e.g. 1024x640 or
+ * 800x800 pixels), else GCFG_ERR_TOO_LARGE before any GPU work.
+ * All calls share the array and it keeps the last call's contents (each call
+ * clears what must start at zero); calls whose GPU work overlaps, e.g. on two
+ * streams, race on it and must be serialised.  The first call on a device
+ * looks up the array's device address with that device current
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * stream: cudaStream_t as void* (NULL = legacy default stream).  The call
+ * returns after the solve has finished. */
+gcfg_status gcfg_solve_noalloc(int w, int h, const int32_t *d_dp, const int32_t *d_dn, int32_t penalty,
+                               const int32_t *d_up, const int32_t *d_down, const int32_t *d_left,
+                               const int32_t *d_right, int32_t *d_label, int64_t *h_flow,
+                               void *stream);
 
 /* ---------------- profiling (off by default) ---------------- */
 
