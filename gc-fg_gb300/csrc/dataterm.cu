@@ -91,9 +91,11 @@ __device__ __noinline__ int nlink_exact(int d2, double lambda, double s2) {
 }
 
 // sigma^2 and 1 / (2 sigma^2) of each image, once per image.
-__global__ void k_img_params(const ImgDesc *__restrict__ img, int n_img, ImgState *ist) {
-    const int im = blockIdx.x * blockDim.x + threadIdx.x;
-    if (im >= n_img) return;
+__global__ void k_img_params(const int *__restrict__ ilist, const ImgDesc *__restrict__ img, int n_img,
+                             ImgState *ist) {
+    const int li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= n_img) return;
+    const int im = ilist ? ilist[li] : li;
     const unsigned long long s = ist[im].sigma_sum;
     const long long count = (long long)(img[im].W - 1) * img[im].H + (long long)img[im].W * (img[im].H - 1);
     const double s2 = (s == 0 || count == 0) ? 0.0 : (double)s / (double)count;
@@ -129,12 +131,14 @@ __global__ void __launch_bounds__(256) k_hist_sigma_b(const uint8_t *__restrict_
                                                       const uint8_t *__restrict__ scrib,
                                                       const ImgDesc *__restrict__ img,
                                                       const long long *__restrict__ chunk_off, int n_img,
-                                                      int *__restrict__ hist, ImgState *ist) {
+                                                      const int *__restrict__ ilist, int *__restrict__ hist,
+                                                      ImgState *ist) {
     __shared__ int sh[2 * NBINS];
-    const int im = chunk_image(chunk_off, n_img, blockIdx.x);
+    const int li = chunk_image(chunk_off, n_img, blockIdx.x);
+    const int im = ilist ? ilist[li] : li;
     const int W = img[im].W, H = img[im].H;
     const int rows = img[im].rows_per_chunk;
-    const int y0 = (int)((long long)blockIdx.x - chunk_off[im]) * rows;
+    const int y0 = (int)((long long)blockIdx.x - chunk_off[li]) * rows;
     const int y1 = min(H, y0 + rows);
     const long long pix0 = img[im].pix0;
     const uint8_t *base = rgb + 3 * pix0;
@@ -176,11 +180,11 @@ __global__ void __launch_bounds__(256) k_hist_sigma_b(const uint8_t *__restrict_
 }
 
 // Per-bin t-link tables (one block per image, double precision).
-__global__ void __launch_bounds__(1024) k_tlut_b(const int *__restrict__ hist, int *__restrict__ dp_lut,
-                                                 int *__restrict__ dn_lut, double *raw_dp,
-                                                 double *raw_dn) {
+__global__ void __launch_bounds__(1024) k_tlut_b(const int *__restrict__ ilist, const int *__restrict__ hist,
+                                                 int *__restrict__ dp_lut, int *__restrict__ dn_lut,
+                                                 double *raw_dp, double *raw_dn) {
     __shared__ long long part[2][32];
-    const int im = blockIdx.x;
+    const int im = ilist ? ilist[blockIdx.x] : blockIdx.x;
     const int *hf = hist + (size_t)im * 2 * NBINS;
     const int *hb = hf + NBINS;
     long long nf = 0, nb = 0;
@@ -241,7 +245,7 @@ __device__ __forceinline__ int nlink_w(int d2, const NlinkParams &q) {
 __global__ void __launch_bounds__(TILE_THREADS) k_build_img_b(Batch b, const uint8_t *__restrict__ rgb,
                                                                const int *__restrict__ dp_lut,
                                                                const int *__restrict__ dn_lut) {
-    const int t = blockIdx.x;
+    const int t = batch_tile(b, blockIdx.x);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int im = __ldg(b.tile_img + t);
     const ImgDesc d = b.img[im];
@@ -320,21 +324,22 @@ __global__ void k_nlinks_apply(const uint8_t *__restrict__ rgb, const ImgDesc *_
 
 gcfg_status dt_tables(const DtArgs &a, cudaStream_t st) {
     // a.scrib == NULL: n-link tables only (the colour histograms need scribbles)
-    if (a.scrib) GCFG_CK(cudaMemsetAsync(a.hist, 0, (size_t)a.n_img * 2 * NBINS * sizeof(int), st));
+    // (with an image list the caller clears the histograms of those images)
+    if (a.scrib && !a.ilist) GCFG_CK(cudaMemsetAsync(a.hist, 0, (size_t)a.n_img * 2 * NBINS * sizeof(int), st));
     GCFG_LAUNCH(GCFG_PK_HIST, st,
                 k_hist_sigma_b<<<a.total_chunks, 256, 0, st>>>(a.rgb, a.scrib, a.img, a.chunk_off, a.n_img,
-                                                               a.hist, a.ist));
-    GCFG_LAUNCH(GCFG_PK_TLUT, st, k_img_params<<<div_up(a.n_img, 128), 128, 0, st>>>(a.img, a.n_img, a.ist));
+                                                               a.ilist, a.hist, a.ist));
+    GCFG_LAUNCH(GCFG_PK_TLUT, st, k_img_params<<<div_up(a.n_img, 128), 128, 0, st>>>(a.ilist, a.img, a.n_img, a.ist));
     if (a.scrib)
         GCFG_LAUNCH(GCFG_PK_TLUT, st,
-                    k_tlut_b<<<a.n_img, 1024, 0, st>>>(a.hist, a.dp_lut, a.dn_lut, a.raw_dp, a.raw_dn));
+                    k_tlut_b<<<a.n_img, 1024, 0, st>>>(a.ilist, a.hist, a.dp_lut, a.dn_lut, a.raw_dp, a.raw_dn));
     GCFG_CK(cudaGetLastError());
     return GCFG_OK;
 }
 
 gcfg_status dt_build(const Batch &b, const DtArgs &a, cudaStream_t st) {
     GCFG_LAUNCH(GCFG_PK_BUILD, st,
-                k_build_img_b<<<b.n_tiles, TILE_THREADS, 0, st>>>(b, a.rgb, a.dp_lut, a.dn_lut));
+                k_build_img_b<<<batch_ntiles(b), TILE_THREADS, 0, st>>>(b, a.rgb, a.dp_lut, a.dn_lut));
     GCFG_CK(cudaGetLastError());
     return GCFG_OK;
 }

@@ -11,7 +11,8 @@ constexpr int CHUNK_PX = 8192;                // pixels per block in per-image p
 // Device buffers of the data term for a batch (per image: 2*4096 histogram
 // bins, 4096 dp and dn entries).
 struct DtArgs {
-    int n_img;
+    int n_img;                // images of this pass (local index k)
+    const int *ilist;         // local image k -> image (slot) index; NULL: k itself
     long long total_chunks;
     const uint8_t *rgb;       // packed row-major RGB of all images
     const uint8_t *scrib;     // packed row-major scribbles (0 none, 1 fg, 2 bg)

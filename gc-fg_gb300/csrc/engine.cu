@@ -558,11 +558,13 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
     PhaseClock clk;
     clk.start();
     // fresh de-duplication marks and reach bits for this solve
-    for (int t = gtid; t < b.n_tiles; t += nthreads) {
+    const int nt = batch_ntiles(b);
+    for (int k = gtid; k < nt; k += nthreads) {
+        const int t = batch_tile(b, k);
         b.mark_push[t] = -1;
         b.mark_gr[t] = -1;
     }
-    for (size_t i = gtid; i < (size_t)b.n_tiles * 32; i += nthreads) b.reach[i] = 0;
+    for (size_t i = gtid; i < (size_t)nt * 32; i += nthreads) b.reach[(size_t)batch_tile(b, (int)(i >> 5)) * 32 + (i & 31)] = 0;
     if (!grid_sync(b, 0)) return;
     clk.charge(&ctl->t_init);
 
@@ -571,13 +573,16 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
     bool finished = false;
     for (int outer = 0; outer < prm.max_outer; ++outer) {
         // ------------------------ exact global relabel ------------------------
-        for (int i = gtid; i < b.n_img; i += nthreads)
+        for (int k = gtid; k < batch_nimg(b); k += nthreads) {
+            const int i = batch_img(b, k);
             if (!b.ist[i].done) {
                 b.ist[i].pos_excess = 0;
                 b.ist[i].active = 0;
             }
+        }
         if (gtid == 0) ctl->total_active = 0;
-        for (int t = gwarp; t < b.n_tiles; t += nwarps) {
+        for (int k = gwarp; k < nt; k += nwarps) {
+            const int t = batch_tile(b, k);
             if (vload(&b.ist[__ldg(b.tile_img + t)].done)) continue;
             gr_tile(b, t, true, G + 1, L_GR0 + ((G + 1) & 1), sm.w.hs[warp]);
             if (lane == 0) atomicAdd(&ctl->gr_tiles, 1ull);
@@ -607,7 +612,8 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
         }
         clk.charge(&ctl->t_gr);
         // ------------------------ count active nodes ------------------------
-        for (int t = gtid; t < b.n_tiles; t += nthreads) {
+        for (int k = gtid; k < nt; k += nthreads) {
+            const int t = batch_tile(b, k);
             const int img = __ldg(b.tile_img + t);
             if (vload(&b.ist[img].done)) continue;
             const int nact = vload(b.tile_act + t);
@@ -627,8 +633,10 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
             ctl->outer_iters = outer + 1;
         }
         const unsigned long long total = *(volatile unsigned long long *)&ctl->total_active;
-        for (int i = gtid; i < b.n_img; i += nthreads)
+        for (int k = gtid; k < batch_nimg(b); k += nthreads) {
+            const int i = batch_img(b, k);
             if (!b.ist[i].done && *(volatile unsigned long long *)&b.ist[i].active == 0) b.ist[i].done = 1;
+        }
         if (total == 0) {
             finished = true;
             break;
@@ -671,7 +679,7 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
         return;
     }
     // ------------------------ source-side reachability ------------------------
-    for (int t = gwarp; t < b.n_tiles; t += nwarps) reach_tile(b, t, true, G + 1, L_GR0 + ((G + 1) & 1));
+    for (int k = gwarp; k < nt; k += nwarps) reach_tile(b, batch_tile(b, k), true, G + 1, L_GR0 + ((G + 1) & 1));
     if (!grid_sync(b, 0)) return;
     ++G;
     for (int k = 1;; ++k) {
@@ -710,7 +718,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_build_arrays(Batch b, const in
                                                                 const int *__restrict__ down,
                                                                 const int *__restrict__ left,
                                                                 const int *__restrict__ right) {
-    const int t = blockIdx.x;
+    const int t = batch_tile(b, blockIdx.x);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const TileGeo g = tile_geo(b, t);
     const int W = b.img[g.img].W, H = b.img[g.img].H;
@@ -756,23 +764,23 @@ __global__ void __launch_bounds__(TILE_THREADS) k_build_arrays(Batch b, const in
     warp_atomic_add_u64(&b.ist[g.img].ref_init, rinit);
 }
 
-// Labels of every image, row-major, at each image's pix0 offset:
+// Labels of every image, row-major, at each image's out0 offset:
 // smin = source-reachable, smax = interior and cannot reach the sink,
 // label = smax as int32 (the reference's GC_Optimize output).
 __global__ void __launch_bounds__(TILE_THREADS) k_extract(Batch b, uint8_t *smin, uint8_t *smax,
                                                            int *label) {
-    const int t = blockIdx.x;
+    const int t = batch_tile(b, blockIdx.x);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const TileGeo g = tile_geo(b, t);
     const int W = b.img[g.img].W, H = b.img[g.img].H;
-    const long long pix0 = b.img[g.img].pix0;
+    const long long out0 = b.img[g.img].out0;
 #pragma unroll
     for (int k = 0; k < ROWS_PER_WARP; ++k) {
         const int r = warp + 8 * k;
         const int x = g.tx * TILE_W + lane, y = g.ty * TILE_H + r;
         if (x >= W || y >= H) continue;
         const size_t p = (size_t)t * TPX + r * 32 + lane;
-        const size_t i = (size_t)pix0 + (size_t)y * W + x;
+        const size_t i = (size_t)out0 + (size_t)y * W + x;
         const bool inside = x > 0 && y > 0 && x < W - 1 && y < H - 1;
         const uint8_t sm = inside && b.h[p] >= INF_H;
         if (smin) smin[i] = (uint8_t)((b.reach[(size_t)t * 32 + r] >> lane) & 1u);
@@ -785,7 +793,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_extract(Batch b, uint8_t *smin
 
 namespace gcfg {
 
-int solve_grid_blocks(int n_tiles) {
+int solve_grid_blocks(int n_tiles, int max_grid) {
     static int cached = 0;
     if (!cached) {
         int dev = 0, sms = 0, per_sm = 0;
@@ -796,12 +804,14 @@ int solve_grid_blocks(int n_tiles) {
     }
     // half the tiles run in a push phase; more blocks than that only make
     // the grid barrier slower
+    int cap = cached;
+    if (max_grid > 0 && max_grid < cap) cap = max_grid;
     const int want = (n_tiles + 1) / 2;
-    return want < 1 ? 1 : (want < cached ? want : cached);
+    return want < 1 ? 1 : (want < cap ? want : cap);
 }
 
-gcfg_status launch_solve(const Batch &b, const SolveParams &prm, int n_tiles, cudaStream_t st) {
-    const int grid = solve_grid_blocks(n_tiles);
+gcfg_status launch_solve(const Batch &b, const SolveParams &prm, int n_tiles, cudaStream_t st, int max_grid) {
+    const int grid = solve_grid_blocks(n_tiles, max_grid);
     Batch bb = b;
     SolveParams pp = prm;
     void *args[] = {&bb, &pp};
@@ -816,13 +826,13 @@ gcfg_status launch_solve(const Batch &b, const SolveParams &prm, int n_tiles, cu
 gcfg_status launch_build_arrays(const Batch &b, const int *dp, const int *dn, int penalty, const int *up,
                                 const int *down, const int *left, const int *right, cudaStream_t st) {
     GCFG_LAUNCH(GCFG_PK_BUILD, st,
-                k_build_arrays<<<b.n_tiles, TILE_THREADS, 0, st>>>(b, dp, dn, penalty, up, down, left, right));
+                k_build_arrays<<<batch_ntiles(b), TILE_THREADS, 0, st>>>(b, dp, dn, penalty, up, down, left, right));
     GCFG_CK(cudaGetLastError());
     return GCFG_OK;
 }
 
 gcfg_status launch_extract(const Batch &b, uint8_t *smin, uint8_t *smax, int *label, cudaStream_t st) {
-    GCFG_LAUNCH(GCFG_PK_EXTRACT, st, k_extract<<<b.n_tiles, TILE_THREADS, 0, st>>>(b, smin, smax, label));
+    GCFG_LAUNCH(GCFG_PK_EXTRACT, st, k_extract<<<batch_ntiles(b), TILE_THREADS, 0, st>>>(b, smin, smax, label));
     GCFG_CK(cudaGetLastError());
     return GCFG_OK;
 }

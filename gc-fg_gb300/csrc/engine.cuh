@@ -28,6 +28,7 @@ struct ImgDesc {
     double lambda;
     int rows_per_chunk;  // rows of the image per block in the per-image passes
     int pad;
+    long long out0;   // offset of the image in the packed output label arrays
 };
 
 // Per-image state written by the device.
@@ -68,6 +69,14 @@ struct Ctl {
 
 struct Batch {
     int n_img, n_tiles;
+    // Optional subset of the arena to solve: tiles tlist[0..n_tlist) (images
+    // outside the subset must be marked done).  NULL: every tile 0..n_tiles.
+    const int *tlist;
+    int n_tlist;
+    // Optional list of the images being solved (per-image loops visit only
+    // these); NULL: every image 0..n_img.
+    const int *ilist;
+    int n_ilist;
     const ImgDesc *img;
     ImgState *ist;
     const int *tile_img;
@@ -96,6 +105,11 @@ struct SolveParams {
     int max_rounds;    // cap on BFS rounds of one global relabel / reach pass
 };
 
+__host__ __device__ __forceinline__ int batch_ntiles(const Batch &b) { return b.tlist ? b.n_tlist : b.n_tiles; }
+__device__ __forceinline__ int batch_tile(const Batch &b, int k) { return b.tlist ? __ldg(b.tlist + k) : k; }
+__host__ __device__ __forceinline__ int batch_nimg(const Batch &b) { return b.ilist ? b.n_ilist : b.n_img; }
+__device__ __forceinline__ int batch_img(const Batch &b, int k) { return b.ilist ? __ldg(b.ilist + k) : k; }
+
 // Error codes in Ctl::err_code.
 enum {
     ERRC_BARRIER = 1,
@@ -111,8 +125,10 @@ enum {
 namespace gcfg {
 
 // Host launchers (engine.cu).
-int solve_grid_blocks(int n_tiles);
-gcfg_status launch_solve(const Batch &b, const SolveParams &prm, int n_tiles, cudaStream_t st);
+// Co-resident blocks of the persistent kernel (capped by max_grid when > 0).
+int solve_grid_blocks(int n_tiles, int max_grid = 0);
+gcfg_status launch_solve(const Batch &b, const SolveParams &prm, int n_tiles, cudaStream_t st,
+                         int max_grid = 0);
 gcfg_status launch_build_arrays(const Batch &b, const int *dp, const int *dn, int penalty, const int *up,
                                 const int *down, const int *left, const int *right, cudaStream_t st);
 gcfg_status launch_extract(const Batch &b, uint8_t *smin, uint8_t *smax, int *label, cudaStream_t st);

@@ -188,6 +188,7 @@ struct Engine {
             d.n_tiles = d.tiles_x * d.tiles_y;
             d.pix0 = p;
             d.lambda = lam ? lam[i] : 0.0;
+            d.out0 = p;
             if (arena)
                 for (int k = 0; k < d.n_tiles; ++k) h_tile_img[t + k] = i;
             d.rows_per_chunk = W[i] >= CHUNK_PX ? 1 : CHUNK_PX / W[i];
@@ -213,6 +214,10 @@ struct Engine {
         Batch b;
         b.n_img = n_img;
         b.n_tiles = n_tiles;
+        b.tlist = nullptr;
+        b.n_tlist = 0;
+        b.ilist = nullptr;
+        b.n_ilist = 0;
         b.img = d_img;
         b.ist = d_ist;
         b.tile_img = d_tile_img;
@@ -234,6 +239,7 @@ struct Engine {
     DtArgs dt(const uint8_t *rgb, const uint8_t *scrib) const {
         DtArgs a;
         a.n_img = n_img;
+        a.ilist = nullptr;
         a.total_chunks = total_chunks;
         a.rgb = rgb;
         a.scrib = scrib;

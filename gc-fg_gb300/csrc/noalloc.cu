@@ -91,6 +91,7 @@ __global__ void k_noalloc_layout(ImgDesc *img, int *tile_img, int W, int H) {
         d.lambda = 0.0;
         d.rows_per_chunk = 1;
         d.pad = 0;
+        d.out0 = 0;
         *img = d;
     }
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) tile_img[t] = 0;
@@ -117,6 +118,10 @@ extern "C" gcfg_status gcfg_solve_noalloc(int w, int h, const int32_t *d_dp, con
     Batch b;
     b.n_img = 1;
     b.n_tiles = (int)tiles;
+    b.tlist = nullptr;
+    b.n_tlist = 0;
+    b.ilist = nullptr;
+    b.n_ilist = 0;
     b.img = reinterpret_cast<const ImgDesc *>(base + OFF_IMG);
     b.ist = reinterpret_cast<ImgState *>(base + OFF_IST);
     b.tile_img = reinterpret_cast<const int *>(base + OFF_TIMG);

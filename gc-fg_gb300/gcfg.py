@@ -366,3 +366,135 @@ class BatchSolver:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------
+# Serving
+# ---------------------------------------------------------------------------
+
+class ServeConfig(C.Structure):
+    _fields_ = [("mem_cap_bytes", C.c_int64), ("lanes", C.c_int32), ("max_batch_images", C.c_int32),
+                ("max_batch_tiles", C.c_int64), ("max_sessions", C.c_int32), ("pad", C.c_int32)]
+
+
+class ServeRequest(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("pad0", C.c_int32), ("session", C.c_int64), ("w", C.c_int32),
+                ("h", C.c_int32), ("lam", C.c_double), ("h_rgb", C.c_void_p), ("h_scrib", C.c_void_p),
+                ("edit_x", C.c_int32), ("edit_y", C.c_int32), ("edit_size", C.c_int32),
+                ("edit_class", C.c_int32), ("h_smin", C.c_void_p), ("h_smax", C.c_void_p)]
+
+
+class ServeResult(C.Structure):
+    _fields_ = [("status", C.c_int32), ("warm", C.c_int32), ("session", C.c_int64), ("flow", C.c_int64),
+                ("batch_images", C.c_int32), ("lane", C.c_int32), ("t_submit", C.c_double),
+                ("t_start", C.c_double), ("t_done", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServeStats(C.Structure):
+    _fields_ = [(k, C.c_int64) for k in ("submitted", "admitted", "completed", "evicted", "batches",
+                                          "bytes_in_use", "sessions", "queued")]
+
+
+REQ_NEW, REQ_EDIT = 0, 1
+
+
+def _serve_sigs(lib):
+    P = C.c_void_p
+    sig = {
+        "gcfg_serve_create": (C.c_int, [C.POINTER(ServeConfig), C.POINTER(P)]),
+        "gcfg_serve_submit": (C.c_int, [P, C.POINTER(ServeRequest), C.POINTER(C.c_int64),
+                                        C.POINTER(C.c_int64)]),
+        "gcfg_serve_wait": (C.c_int, [P, C.c_int64, C.POINTER(ServeResult), C.c_int]),
+        "gcfg_serve_release": (C.c_int, [P, C.c_int64]),
+        "gcfg_serve_get_stats": (C.c_int, [P, C.POINTER(ServeStats)]),
+        "gcfg_serve_destroy": (C.c_int, [P]),
+        "gcfg_serve_now": (C.c_double, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+
+
+EXPORTS += ["gcfg_serve_create", "gcfg_serve_submit", "gcfg_serve_wait", "gcfg_serve_release",
+            "gcfg_serve_get_stats", "gcfg_serve_destroy", "gcfg_serve_now"]
+
+
+class Server:
+    """Continuous-batching segmentation server (gcfg_serve_*).
+
+    Host buffers passed to submit_* must stay alive until the request is
+    waited for; this object keeps references to them until then."""
+
+    def __init__(self, mem_cap_bytes=60 << 30, lanes=2, max_batch_images=256, max_batch_tiles=1 << 16,
+                 max_sessions=4096):
+        lib = load()
+        if not getattr(lib, "_serve_sigs", False):
+            _serve_sigs(lib)
+            lib._serve_sigs = True
+        cfg = ServeConfig(int(mem_cap_bytes), int(lanes), int(max_batch_images), int(max_batch_tiles),
+                          int(max_sessions), 0)
+        h = C.c_void_p()
+        _check(lib.gcfg_serve_create(C.byref(cfg), C.byref(h)), "gcfg_serve_create")
+        self.handle = h
+        self._refs = {}
+
+    def _submit(self, req, refs):
+        t = C.c_int64()
+        sid = C.c_int64()
+        _check(load().gcfg_serve_submit(self.handle, C.byref(req), C.byref(t), C.byref(sid)),
+               "gcfg_serve_submit")
+        self._refs[t.value] = refs
+        return t.value, sid.value
+
+    def submit_new(self, rgb, scrib, lam, smin=None, smax=None):
+        """Returns (ticket, session).  rgb: uint8 [H, W, 3], scrib: uint8 [H, W]."""
+        H, W = scrib.shape
+        req = ServeRequest(kind=REQ_NEW, w=W, h=H, lam=float(lam), h_rgb=_ptr(rgb).value,
+                           h_scrib=_ptr(scrib).value,
+                           h_smin=None if smin is None else _ptr(smin).value,
+                           h_smax=None if smax is None else _ptr(smax).value)
+        return self._submit(req, (rgb, scrib, smin, smax))
+
+    def submit_edit(self, session, x, y, size, cls, smin=None, smax=None):
+        req = ServeRequest(kind=REQ_EDIT, session=int(session), edit_x=int(x), edit_y=int(y),
+                           edit_size=int(size), edit_class=int(cls),
+                           h_smin=None if smin is None else _ptr(smin).value,
+                           h_smax=None if smax is None else _ptr(smax).value)
+        return self._submit(req, (smin, smax))
+
+    def wait(self, ticket, timeout_ms=-1) -> dict:
+        res = ServeResult()
+        load().gcfg_serve_wait(self.handle, int(ticket), C.byref(res), int(timeout_ms))
+        self._refs.pop(ticket, None)
+        return res.as_dict()
+
+    def release(self, session):
+        _check(load().gcfg_serve_release(self.handle, int(session)), "gcfg_serve_release")
+
+    def stats(self) -> dict:
+        st = ServeStats()
+        _check(load().gcfg_serve_get_stats(self.handle, C.byref(st)), "gcfg_serve_get_stats")
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    @staticmethod
+    def now() -> float:
+        lib = load()
+        if not getattr(lib, "_serve_sigs", False):
+            _serve_sigs(lib)
+            lib._serve_sigs = True
+        return lib.gcfg_serve_now()
+
+    def close(self):
+        if self.handle:
+            load().gcfg_serve_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -167,6 +167,75 @@ gcfg_status gcfg_batch_run_host(gcfg_batch *b, int n, const int *widths, const i
                                 gcfg_result *h_res);
 gcfg_status gcfg_batch_destroy(gcfg_batch *b);
 
+/* ---------------- serving (continuous batching, resident images) ---------------- */
+
+/* A server keeps every admitted image resident on the device (pixels,
+ * scribbles, residual graph, histograms, t-link tables) and solves waiting
+ * requests in batches on `lanes` worker lanes (host thread + stream each);
+ * requests that arrive while lanes are busy join the next free lane's batch,
+ * and with two lanes two batches run on the device at once.  New images are
+ * admitted while their device footprint fits under mem_cap_bytes (idle
+ * resident images are evicted least-recently-used first).  A scribble edit of
+ * a resident image is re-solved warm from its stored flow with the t-links
+ * reparametrised; its result equals a cold solve of the edited image. */
+typedef struct gcfg_server gcfg_server;
+
+typedef struct {
+    int64_t mem_cap_bytes;    /* device footprint cap of resident images */
+    int32_t lanes;            /* worker lanes (1..8) */
+    int32_t max_batch_images; /* images per batch */
+    int64_t max_batch_tiles;  /* 32x32 tiles per batch (also the largest image) */
+    int32_t max_sessions;     /* resident images */
+    int32_t pad;
+} gcfg_serve_config;
+
+enum { GCFG_REQ_NEW = 0, GCFG_REQ_EDIT = 1 };
+
+typedef struct {
+    int32_t kind;             /* GCFG_REQ_NEW or GCFG_REQ_EDIT */
+    int32_t pad0;
+    int64_t session;          /* GCFG_REQ_EDIT: the resident image to edit */
+    int32_t w, h;             /* GCFG_REQ_NEW: image size */
+    double lambda;            /* GCFG_REQ_NEW: n-link weight */
+    const uint8_t *h_rgb;     /* GCFG_REQ_NEW: host RGB (3*w*h), valid until completion */
+    const uint8_t *h_scrib;   /* GCFG_REQ_NEW: host scribbles (w*h: 0/1 fg/2 bg) */
+    int32_t edit_x, edit_y;   /* GCFG_REQ_EDIT: top-left corner of the scribble square */
+    int32_t edit_size;        /* GCFG_REQ_EDIT: side of the square */
+    int32_t edit_class;       /* GCFG_REQ_EDIT: 1 = foreground, 2 = background */
+    uint8_t *h_smin, *h_smax; /* host outputs (w*h each) or NULL */
+} gcfg_serve_request;
+
+typedef struct {
+    int32_t status;           /* gcfg_status of the request */
+    int32_t warm;             /* 1: solved warm (scribble edit) */
+    int64_t session;          /* resident image id (new for GCFG_REQ_NEW) */
+    int64_t flow;             /* exact flow value */
+    int32_t batch_images;     /* images in the batch that solved it */
+    int32_t lane;
+    double t_submit, t_start, t_done; /* host clock (gcfg_serve_now), seconds */
+} gcfg_serve_result;
+
+typedef struct {
+    int64_t submitted, admitted, completed, evicted, batches;
+    int64_t bytes_in_use, sessions, queued;
+} gcfg_serve_stats;
+
+gcfg_status gcfg_serve_create(const gcfg_serve_config *cfg, gcfg_server **out);
+/* Non-blocking; returns a ticket for gcfg_serve_wait and the id of the
+ * resident image (a new one for GCFG_REQ_NEW; edits may be submitted for it
+ * at once and run after its first solve).  A new image larger than
+ * max_batch_tiles or than the whole cap is refused (GCFG_ERR_CAPACITY). */
+gcfg_status gcfg_serve_submit(gcfg_server *s, const gcfg_serve_request *req, int64_t *ticket,
+                              int64_t *session);
+/* Wait for a ticket (timeout_ms < 0: no limit).  Returns the request's status. */
+gcfg_status gcfg_serve_wait(gcfg_server *s, int64_t ticket, gcfg_serve_result *res, int timeout_ms);
+/* Drop a resident image (not while a request uses it). */
+gcfg_status gcfg_serve_release(gcfg_server *s, int64_t session);
+gcfg_status gcfg_serve_get_stats(gcfg_server *s, gcfg_serve_stats *out);
+gcfg_status gcfg_serve_destroy(gcfg_server *s);
+/* The host clock of the result timestamps (seconds). */
+double gcfg_serve_now(void);
+
 /* ---------------- allocation-free solve ---------------- */
 
 /* Largest image of gcfg_solve_noalloc, in 32x32 tiles, and the size of the
