@@ -186,6 +186,164 @@ def cpu_baseline(views, lams, budget_s=10.0):
     return px / dt / 1e6, k, dt, flows
 
 
+def _sleep_until(now, ta):
+    while True:
+        d = ta - now()
+        if d <= 0:
+            return
+        if d > 1e-3:
+            time.sleep(d - 5e-4)
+
+
+def _lane_overlap(results):
+    """Fraction of the lanes' busy time during which two or more lanes ran."""
+    ev = sorted({(r["lane"], r["t_start"], r["t_done"]) for r in results}, key=lambda b: b[1])
+    pts = sorted([(b[1], 1) for b in ev] + [(b[2], -1) for b in ev])
+    busy = multi = 0.0
+    depth, last = 0, None
+    for t, d in pts:
+        if last is not None and depth > 0:
+            busy += t - last
+            if depth > 1:
+                multi += t - last
+        depth += d
+        last = t
+    return multi / busy if busy > 0 else 0.0
+
+
+def serve_bench(torch, gcfg, n_req=1200, rate=500.0, lanes=2, cap=60 << 30, seed=4):
+    """Serving workload: a Poisson request trace replayed through the server
+    (continuous batching, resident images, warm edits) and through a plain
+    cold-solve loop (one gcfg_seg_run_host per request, edits re-solved cold
+    from the edited scribbles).  Both take host buffers (pinned) and return
+    both label maps to the host.  Every request's flow and cuts must be equal
+    across the served run, a saturated served run (all requests at once) and
+    the plain loop."""
+    import zlib
+    import synth
+    pool_specs, reqs = synth.serve_trace(n_req, rate, seed)
+    rgb, scrib, offs = synth.generate_packed(pool_specs)
+    p_rgb = torch.from_numpy(rgb).pin_memory().numpy()
+    p_scrib = torch.from_numpy(scrib).pin_memory().numpy()
+    sides = [W for (_, W, _, _) in pool_specs]
+
+    def pool_view(i):
+        o, s = int(offs[i]), sides[i]
+        return p_rgb[3 * o:3 * (o + s * s)].reshape(s, s, 3), p_scrib[o:o + s * s].reshape(s, s)
+
+    new_img = [q["img"] for q in reqs if q["kind"] == "new"]
+    img_of = [q["img"] if q["kind"] == "new" else new_img[q["target"]] for q in reqs]
+    npx = np.array([sides[i] ** 2 for i in img_of], np.int64)
+    ooff = np.zeros(len(reqs), np.int64)
+    ooff[1:] = np.cumsum(npx)[:-1]
+    total_px = int(npx.sum())
+    out_min = torch.empty(total_px, dtype=torch.uint8).pin_memory().numpy()
+    out_max = torch.empty(total_px, dtype=torch.uint8).pin_memory().numpy()
+    now = gcfg.Server.now
+
+    def outs(k):
+        o, n, s = int(ooff[k]), int(npx[k]), sides[img_of[k]]
+        return out_min[o:o + n].reshape(s, s), out_max[o:o + n].reshape(s, s)
+
+    def digest(k, flow):
+        a, b = outs(k)
+        return (int(flow), zlib.crc32(a), zlib.crc32(b))
+
+    def served(open_loop, n=None):
+        rq = reqs if n is None else reqs[:n]
+        srv = gcfg.Server(mem_cap_bytes=cap, lanes=lanes, max_batch_images=256, max_batch_tiles=1 << 16,
+                          max_sessions=len(new_img) + 16)
+        sids, tick = [], []
+        t0 = now() + 0.02
+        for k, q in enumerate(rq):
+            ta = t0 + (q["t"] if open_loop else 0.0)
+            if open_loop:
+                _sleep_until(now, ta)
+            smin, smax = outs(k)
+            if q["kind"] == "new":
+                r, s = pool_view(q["img"])
+                t, sid = srv.submit_new(r, s, q["lam"], smin, smax)
+                sids.append(sid)
+            else:
+                t, _ = srv.submit_edit(sids[q["target"]], q["x"], q["y"], q["size"], q["cls"], smin, smax)
+            tick.append((t, ta))
+        res = [srv.wait(t, timeout_ms=600000) for t, _ in tick]
+        st = srv.stats()
+        srv.close()
+        assert all(r["status"] == 0 for r in res), "served request failed"
+        return res, np.array([ta for _, ta in tick]), st, [digest(k, r["flow"]) for k, r in enumerate(res)]
+
+    served(True, n=60)  # warm-up
+    res, tarr, st, dig_served = served(True)
+    done = np.array([r["t_done"] for r in res])
+    lat = done - tarr
+    is_edit = np.array([q["kind"] == "edit" for q in reqs])
+    res_sat, tarr_sat, st_sat, dig_sat = served(False)
+    make_sat = max(r["t_done"] for r in res_sat) - tarr_sat[0]
+
+    # plain cold-solve loop on the same schedule
+    seg = gcfg.Segmenter(max(sides), max(sides))
+    edited = {q["target"] for q in reqs if q["kind"] == "edit"}
+    sess_scrib = {}
+    n_new = 0
+    for q in reqs:
+        if q["kind"] == "new":
+            if n_new in edited:
+                sess_scrib[n_new] = torch.from_numpy(pool_view(q["img"])[1].copy()).pin_memory().numpy()
+            n_new += 1
+    p_lat, p_svc, dig_plain = [], [], []
+    for warm in (True, False):
+        n_new = 0
+        t0 = now() + 0.02
+        for k, q in enumerate(reqs[:60] if warm else reqs):
+            ta = t0 + q["t"]
+            _sleep_until(now, ta)
+            ts = now()
+            if q["kind"] == "new":
+                r, s = pool_view(q["img"])
+                if not warm and n_new in sess_scrib:
+                    s = sess_scrib[n_new]
+                n_new += 1
+            else:
+                r = pool_view(new_img[q["target"]])[0]
+                s = sess_scrib[q["target"]] if not warm else pool_view(new_img[q["target"]])[1].copy()
+                s[q["y"]:q["y"] + q["size"], q["x"]:q["x"] + q["size"]] = q["cls"]
+            smin, smax = outs(k)
+            out = seg.run_host(r, s, s.shape[1], s.shape[0], 50.0, smin, smax)
+            td = now()
+            if not warm:
+                p_lat.append(td - ta)
+                p_svc.append(td - ts)
+                dig_plain.append(out["flow"])
+    seg.close()
+    dig_plain = [digest(k, f) for k, f in enumerate(dig_plain)]
+    p_lat = np.array(p_lat)
+
+    def ms(a, p):
+        return round(float(np.percentile(a, p)) * 1e3, 3)
+
+    return {
+        "workload": f"Poisson {rate:g} req/s, {len(reqs)} requests ({int((~is_edit).sum())} new images "
+                    f"256^2/1024^2/2048^2 at 60/30/10%, {int(is_edit.sum())} scribble edits 15x15 of earlier "
+                    f"images), 1920x1080-family generator, lambda 50, trace seed {seed}; host buffers (pinned) "
+                    f"in and both label maps out",
+        "pixels": total_px, "lanes": lanes, "mem_cap_gb": cap / 2 ** 30,
+        "served": {"p50_ms": ms(lat, 50), "p99_ms": ms(lat, 99),
+                   "p50_new_ms": ms(lat[~is_edit], 50), "p99_new_ms": ms(lat[~is_edit], 99),
+                   "p50_edit_ms": ms(lat[is_edit], 50), "p99_edit_ms": ms(lat[is_edit], 99),
+                   "mpixel_s": total_px / (done.max() - tarr[0]) / 1e6,
+                   "batches": st["batches"], "mean_batch_images": len(reqs) / max(st["batches"], 1),
+                   "lane_overlap_frac": round(_lane_overlap(res), 4),
+                   "resident_gb_at_end": st["bytes_in_use"] / 2 ** 30, "evicted": st["evicted"]},
+        "served_saturated": {"mpixel_s": total_px / make_sat / 1e6, "makespan_ms": make_sat * 1e3,
+                             "batches": st_sat["batches"]},
+        "plain_cold_loop": {"p50_ms": ms(p_lat, 50), "p99_ms": ms(p_lat, 99),
+                            "mpixel_s": total_px / float(np.sum(p_svc)) / 1e6,
+                            "mean_service_ms": float(np.mean(p_svc)) * 1e3},
+        "results_equal": bool(dig_served == dig_plain and dig_sat == dig_plain),
+    }
+
+
 def run_reference_arm(args, spec, rank, world):
     """--impl reference: CPU port of the path on all host threads."""
     if rank != 0:
@@ -228,6 +386,8 @@ def main():
     ap.add_argument("--workload", default="batch256")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-plain", action="store_true", help="skip the per-image comparison leg")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--serve-requests", type=int, default=1200)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_info()
@@ -413,6 +573,8 @@ def main():
                                  "cyc_take")}}
     if plain is not None:
         line["plain_per_image"] = plain
+    if batched and not args.no_serve and rank == 0:
+        line["serving"] = serve_bench(torch, gcfg, n_req=args.serve_requests)
     line["flows_host_equal_device"] = bool(np.array_equal(np.asarray(flows_h), np.asarray(flows)))
     if rank == 0:
         cpu_v, n_chk, secs, cflows = cpu_baseline(views, lams, budget_s=args.cpu_budget)

@@ -121,3 +121,53 @@ def _u(st):
     z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
     z ^= z >> 31
     return (z >> 11) * (1.0 / 9007199254740992.0)
+
+
+SERVE_SIZES = ((256, 0.6), (1024, 0.3), (2048, 0.1))
+
+
+def serve_trace(n_req: int = 1200, rate: float = 500.0, seed: int = 4, edit_frac: float = 0.3,
+                pool=(48, 24, 8), edit_size: int = 15, lam: float = 50.0):
+    """Request trace of the serving workload.
+
+    Poisson arrivals at `rate` requests/s.  A request is a scribble edit with
+    probability `edit_frac` (once an image exists): a `edit_size` square of
+    class 1 (foreground) or 2 (background) at a uniform position of a uniformly
+    chosen earlier image.  Otherwise it is a new square image whose side is
+    256 / 1024 / 2048 with probability 0.6 / 0.3 / 0.1, drawn from the
+    1920x1080-family generator (cfg 4).  New images of one side cycle through
+    a pool of `pool[c]` distinct generated images (seeds 4000 + 100*c + k), so
+    that the inputs stay small; every new request is still its own resident
+    session.
+
+    Returns (pool_specs, requests): pool_specs = [(4, side, side, seed)], and
+    each request a dict with 't' (arrival, seconds from the start), 'kind'
+    ('new' | 'edit'), and for new: 'img' (pool index), 'lam'; for edit: 'target'
+    (ordinal of the new request it edits), 'x', 'y', 'size', 'cls'.
+    """
+    st = [seed * 104729 + 3]
+    pool_specs, pool_base = [], []
+    for c, (side, _) in enumerate(SERVE_SIZES):
+        pool_base.append(len(pool_specs))
+        pool_specs += [(4, side, side, 4000 + 100 * c + k) for k in range(pool[c])]
+    cum = np.cumsum([p for _, p in SERVE_SIZES])
+    t = 0.0
+    reqs, news, used = [], [], [0] * len(SERVE_SIZES)
+    for _ in range(n_req):
+        t += float(-np.log(1.0 - _u(st)) / rate)
+        if news and _u(st) < edit_frac:
+            k = min(int(_u(st) * len(news)), len(news) - 1)
+            side = news[k]
+            span = max(1, side - edit_size + 1)
+            x = min(int(_u(st) * span), span - 1)
+            y = min(int(_u(st) * span), span - 1)
+            cls = 1 if _u(st) < 0.5 else 2
+            reqs.append(dict(t=t, kind="edit", target=k, x=x, y=y, size=edit_size, cls=cls))
+        else:
+            c = int(np.searchsorted(cum, _u(st), side="right"))
+            c = min(c, len(SERVE_SIZES) - 1)
+            img = pool_base[c] + used[c] % pool[c]
+            used[c] += 1
+            news.append(SERVE_SIZES[c][0])
+            reqs.append(dict(t=t, kind="new", img=img, lam=lam))
+    return pool_specs, reqs
