@@ -1,0 +1,210 @@
+// dterm_api.cu -- the DataTerm interface (DataTerm.h:9-19) over the
+// colour-histogram data term.
+//
+// The reference keeps one global data-term state per process: an image, a
+// selection map and a kernel-density colour model that selectOnMap() splats
+// into (DataTerm.cpp:28-165).  Here the state lives in a handle: the image
+// (3 bytes per pixel, as given), the selection map (one byte per pixel: 0 none,
+// 1 foreground, 2 background) and the two t-link arrays.  The colour model is
+// the 16^3-bin histogram pair of the selected pixels, rebuilt from the current
+// image and map whenever the t-links are computed (gcfg_dt_compute), so a
+// selection made by selectOnMap() and one made by setSelection() both act on
+// the model.
+#include "engine.cuh"
+
+namespace gcfg {
+namespace {
+
+// setSelection: int map -> byte map (K_SetMap, DataTermKernels.cu:86-94).
+__global__ void k_sel_from_int(const int32_t *__restrict__ in, uint8_t *__restrict__ map, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        map[i] = (uint8_t)in[i];
+}
+
+// selectOnMap: mark a size x size square with corner (x0, y0), clipped to the
+// image (DataTerm.cpp:111-123 marks x..x+4, y..y+4 without clipping).
+__global__ void k_sel_square(uint8_t *map, int W, int H, int x0, int y0, int size, int cls) {
+    const int dx = threadIdx.x, dy = threadIdx.y;
+    if (dx >= size || dy >= size) return;
+    const int x = x0 + dx, y = y0 + dy;
+    if (x < 0 || y < 0 || x >= W || y >= H) return;
+    map[(long long)y * W + x] = (uint8_t)cls;
+}
+
+// drawSelection: class-1 pixels become (0, 0, 255) as in K_DrawMap
+// (DataTermKernels.cu:96-113); class-2 pixels (no counterpart) become
+// (255, 0, 0).
+__global__ void k_draw_sel(const uint8_t *__restrict__ map, const uint8_t *__restrict__ img,
+                           uint8_t *__restrict__ out, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const uint8_t m = map[i];
+        uint8_t c0 = img[3 * i + 0], c1 = img[3 * i + 1], c2 = img[3 * i + 2];
+        if (m == 1) {
+            c0 = 0;
+            c1 = 0;
+            c2 = 255;
+        } else if (m == 2) {
+            c0 = 255;
+            c1 = 0;
+            c2 = 0;
+        }
+        out[3 * i + 0] = c0;
+        out[3 * i + 1] = c1;
+        out[3 * i + 2] = c2;
+    }
+}
+
+int grid_for(long long n) {
+    long long b = (n + 255) / 256;
+    return (int)(b < 4096 ? (b > 0 ? b : 1) : 4096);
+}
+
+}  // namespace
+}  // namespace gcfg
+
+using namespace gcfg;
+
+struct gcfg_dataterm {
+    int W = 0, H = 0;
+    int sigma = 5;
+    uint8_t *d_img = nullptr, *d_sel = nullptr;
+    int32_t *d_pos = nullptr, *d_neg = nullptr;
+    int32_t *d_tmp = nullptr;  // setSelection staging (allocated on first use)
+    uint8_t *d_draw = nullptr; // drawSelection output (allocated on first use)
+    cudaStream_t st = nullptr;
+};
+
+extern "C" {
+
+gcfg_status gcfg_dt_create(int w, int h, gcfg_dataterm **out) {
+    if (!out || w <= 0 || h <= 0 || (long long)w * h > (1LL << 31) - 1) return GCFG_ERR_INVALID;
+    gcfg_dataterm *d = new gcfg_dataterm();
+    d->W = w;
+    d->H = h;
+    const size_t n = (size_t)w * h;
+    if (cudaMalloc(&d->d_img, 3 * n) != cudaSuccess || cudaMalloc(&d->d_sel, n) != cudaSuccess ||
+        cudaMalloc(&d->d_pos, n * sizeof(int32_t)) != cudaSuccess ||
+        cudaMalloc(&d->d_neg, n * sizeof(int32_t)) != cudaSuccess) {
+        cudaFree(d->d_img);
+        cudaFree(d->d_sel);
+        cudaFree(d->d_pos);
+        cudaFree(d->d_neg);
+        delete d;
+        return GCFG_ERR_OOM;
+    }
+    // a fresh state has an empty selection (init_data_term calls reset())
+    if (cudaMemset(d->d_sel, 0, n) != cudaSuccess || cudaMemset(d->d_img, 0, 3 * n) != cudaSuccess) {
+        cudaFree(d->d_img);
+        cudaFree(d->d_sel);
+        cudaFree(d->d_pos);
+        cudaFree(d->d_neg);
+        delete d;
+        return GCFG_ERR_CUDA;
+    }
+    *out = d;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_dt_destroy(gcfg_dataterm *d) {
+    if (!d) return GCFG_ERR_INVALID;
+    cudaStreamSynchronize(d->st);
+    cudaFree(d->d_img);
+    cudaFree(d->d_sel);
+    cudaFree(d->d_pos);
+    cudaFree(d->d_neg);
+    cudaFree(d->d_tmp);
+    cudaFree(d->d_draw);
+    delete d;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_dt_set_stream(gcfg_dataterm *d, void *stream) {
+    if (!d) return GCFG_ERR_INVALID;
+    d->st = (cudaStream_t)stream;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_dt_set_image(gcfg_dataterm *d, const uint8_t *h_img) {
+    if (!d || !h_img) return GCFG_ERR_INVALID;
+    GCFG_CK(cudaMemcpyAsync(d->d_img, h_img, (size_t)3 * d->W * d->H, cudaMemcpyHostToDevice, d->st));
+    GCFG_CK(cudaStreamSynchronize(d->st));
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_dt_set_image_device(gcfg_dataterm *d, const uint8_t *d_img) {
+    if (!d || !d_img) return GCFG_ERR_INVALID;
+    GCFG_CK(cudaMemcpyAsync(d->d_img, d_img, (size_t)3 * d->W * d->H, cudaMemcpyDeviceToDevice, d->st));
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_dt_set_selection(gcfg_dataterm *d, const int32_t *h_select) {
+    if (!d || !h_select) return GCFG_ERR_INVALID;
+    const long long n = (long long)d->W * d->H;
+    if (!d->d_tmp && cudaMalloc(&d->d_tmp, (size_t)n * sizeof(int32_t)) != cudaSuccess) return GCFG_ERR_OOM;
+    GCFG_CK(cudaMemcpyAsync(d->d_tmp, h_select, (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice, d->st));
+    k_sel_from_int<<<grid_for(n), 256, 0, d->st>>>(d->d_tmp, d->d_sel, n);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    GCFG_CK(cudaGetLastError());
+    GCFG_CK(cudaStreamSynchronize(d->st));
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_dt_set_scribbles_device(gcfg_dataterm *d, const uint8_t *d_scrib) {
+    if (!d || !d_scrib) return GCFG_ERR_INVALID;
+    GCFG_CK(cudaMemcpyAsync(d->d_sel, d_scrib, (size_t)d->W * d->H, cudaMemcpyDeviceToDevice, d->st));
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_dt_reset(gcfg_dataterm *d) {
+    if (!d) return GCFG_ERR_INVALID;
+    GCFG_CK(cudaMemsetAsync(d->d_sel, 0, (size_t)d->W * d->H, d->st));
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_dt_select_on_map(gcfg_dataterm *d, int x, int y, int cls) {
+    if (!d || (cls != 1 && cls != 2)) return GCFG_ERR_INVALID;
+    k_sel_square<<<1, dim3(GCFG_DT_SELECT_SIZE, GCFG_DT_SELECT_SIZE), 0, d->st>>>(d->d_sel, d->W, d->H, x, y,
+                                                                               GCFG_DT_SELECT_SIZE, cls);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    GCFG_CK(cudaGetLastError());
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_dt_set_sigma(gcfg_dataterm *d, int sigma) {
+    if (!d || sigma <= 0) return GCFG_ERR_INVALID;
+    d->sigma = sigma;  // kept for the interface; the histogram model has no kernel width
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_dt_compute(gcfg_dataterm *d) {
+    if (!d) return GCFG_ERR_INVALID;
+    return gcfg_tlinks(d->d_img, d->d_sel, d->W * d->H, d->d_pos, d->d_neg, nullptr, nullptr, d->st);
+}
+
+gcfg_status gcfg_dt_nlinks(gcfg_dataterm *d, double lambda, int32_t *d_up, int32_t *d_down, int32_t *d_left,
+                           int32_t *d_right) {
+    if (!d) return GCFG_ERR_INVALID;
+    return gcfg_nlinks(d->d_img, d->W, d->H, lambda, d_up, d_down, d_left, d_right, d->st);
+}
+
+int32_t *gcfg_dt_pos(gcfg_dataterm *d) { return d ? d->d_pos : nullptr; }
+int32_t *gcfg_dt_neg(gcfg_dataterm *d) { return d ? d->d_neg : nullptr; }
+uint8_t *gcfg_dt_image(gcfg_dataterm *d) { return d ? d->d_img : nullptr; }
+uint8_t *gcfg_dt_selection(gcfg_dataterm *d) { return d ? d->d_sel : nullptr; }
+
+gcfg_status gcfg_dt_draw_selection(gcfg_dataterm *d, const uint8_t *h_in, uint8_t *h_out) {
+    if (!d || !h_in || !h_out) return GCFG_ERR_INVALID;
+    const long long n = (long long)d->W * d->H;
+    if (!d->d_draw && cudaMalloc(&d->d_draw, (size_t)3 * n) != cudaSuccess) return GCFG_ERR_OOM;
+    // as in the reference, the input becomes the current image; the marks go
+    // only to the output (the reference also leaves them in its image buffer)
+    GCFG_CK(cudaMemcpyAsync(d->d_img, h_in, (size_t)3 * n, cudaMemcpyHostToDevice, d->st));
+    k_draw_sel<<<grid_for(n), 256, 0, d->st>>>(d->d_sel, d->d_img, d->d_draw, n);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    GCFG_CK(cudaGetLastError());
+    GCFG_CK(cudaMemcpyAsync(h_out, d->d_draw, (size_t)3 * n, cudaMemcpyDeviceToHost, d->st));
+    GCFG_CK(cudaStreamSynchronize(d->st));
+    return GCFG_OK;
+}
+
+}  // extern "C"

@@ -13,6 +13,8 @@ from __future__ import annotations
 import ctypes as C
 import os
 
+import numpy as np
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libgcfg.so")
 
@@ -498,3 +500,208 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------
+# DataTerm (DataTerm.h:9-19): gcfg_dt_* handle and the reference's names
+# ---------------------------------------------------------------------------
+
+EXPORTS += ["gcfg_dt_create", "gcfg_dt_destroy", "gcfg_dt_set_stream", "gcfg_dt_set_image",
+            "gcfg_dt_set_image_device", "gcfg_dt_set_selection", "gcfg_dt_set_scribbles_device",
+            "gcfg_dt_reset", "gcfg_dt_select_on_map", "gcfg_dt_set_sigma", "gcfg_dt_compute",
+            "gcfg_dt_pos", "gcfg_dt_neg", "gcfg_dt_image", "gcfg_dt_selection",
+            "gcfg_dt_draw_selection", "gcfg_dt_nlinks"]
+
+
+def _dt_lib():
+    lib = load()
+    if not getattr(lib, "_dt_sigs", False):
+        P = C.c_void_p
+        sig = {
+            "gcfg_dt_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(P)]),
+            "gcfg_dt_destroy": (C.c_int, [P]),
+            "gcfg_dt_set_stream": (C.c_int, [P, P]),
+            "gcfg_dt_set_image": (C.c_int, [P, P]),
+            "gcfg_dt_set_image_device": (C.c_int, [P, P]),
+            "gcfg_dt_set_selection": (C.c_int, [P, P]),
+            "gcfg_dt_set_scribbles_device": (C.c_int, [P, P]),
+            "gcfg_dt_reset": (C.c_int, [P]),
+            "gcfg_dt_select_on_map": (C.c_int, [P, C.c_int, C.c_int, C.c_int]),
+            "gcfg_dt_set_sigma": (C.c_int, [P, C.c_int]),
+            "gcfg_dt_compute": (C.c_int, [P]),
+            "gcfg_dt_pos": (P, [P]),
+            "gcfg_dt_neg": (P, [P]),
+            "gcfg_dt_image": (P, [P]),
+            "gcfg_dt_selection": (P, [P]),
+            "gcfg_dt_draw_selection": (C.c_int, [P, P, P]),
+            "gcfg_dt_nlinks": (C.c_int, [P, C.c_double, P, P, P, P]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        lib._dt_sigs = True
+    return lib
+
+
+class DeviceArray:
+    """A device array owned by the library, seen through
+    __cuda_array_interface__ (torch.as_tensor(a, device="cuda") is a view)."""
+
+    def __init__(self, ptr, n, typestr):
+        self.ptr, self.n, self.typestr = int(ptr or 0), int(n), typestr
+
+    def data_ptr(self):
+        return self.ptr
+
+    @property
+    def __cuda_array_interface__(self):
+        return {"shape": (self.n,), "typestr": self.typestr, "data": (self.ptr, False), "version": 2}
+
+
+class DataTermState:
+    """gcfg_dt_* handle: image, selection map and t-link arrays of one image."""
+
+    def __init__(self, width, height):
+        lib = _dt_lib()
+        h = C.c_void_p()
+        _check(lib.gcfg_dt_create(int(width), int(height), C.byref(h)), "gcfg_dt_create")
+        self.handle, self.width, self.height = h, int(width), int(height)
+
+    def _lib(self):
+        if not self.handle:
+            raise GcfgError(GCFG_ERR_STATE, "DataTerm used after free")
+        return _dt_lib()
+
+    def set_stream(self, stream):
+        _check(self._lib().gcfg_dt_set_stream(self.handle, _stream_ptr(stream)), "gcfg_dt_set_stream")
+
+    def set_image(self, h_img):
+        a = np.ascontiguousarray(h_img, dtype=np.uint8)
+        assert a.size == 3 * self.width * self.height
+        _check(self._lib().gcfg_dt_set_image(self.handle, _ptr(a)), "gcfg_dt_set_image")
+
+    def set_image_device(self, d_img):
+        _check(self._lib().gcfg_dt_set_image_device(self.handle, _ptr(d_img)), "gcfg_dt_set_image_device")
+
+    def set_selection(self, h_select):
+        a = np.ascontiguousarray(h_select, dtype=np.int32)
+        assert a.size == self.width * self.height
+        _check(self._lib().gcfg_dt_set_selection(self.handle, _ptr(a)), "gcfg_dt_set_selection")
+
+    def set_scribbles_device(self, d_scrib):
+        _check(self._lib().gcfg_dt_set_scribbles_device(self.handle, _ptr(d_scrib)),
+               "gcfg_dt_set_scribbles_device")
+
+    def reset(self):
+        _check(self._lib().gcfg_dt_reset(self.handle), "gcfg_dt_reset")
+
+    def select_on_map(self, x, y, cls=1):
+        _check(self._lib().gcfg_dt_select_on_map(self.handle, int(x), int(y), int(cls)),
+               "gcfg_dt_select_on_map")
+
+    def set_sigma(self, sigma):
+        _check(self._lib().gcfg_dt_set_sigma(self.handle, int(sigma)), "gcfg_dt_set_sigma")
+
+    def compute(self):
+        _check(self._lib().gcfg_dt_compute(self.handle), "gcfg_dt_compute")
+
+    def pos(self) -> DeviceArray:
+        return DeviceArray(self._lib().gcfg_dt_pos(self.handle), self.width * self.height, "<i4")
+
+    def neg(self) -> DeviceArray:
+        return DeviceArray(self._lib().gcfg_dt_neg(self.handle), self.width * self.height, "<i4")
+
+    def image(self) -> DeviceArray:
+        return DeviceArray(self._lib().gcfg_dt_image(self.handle), 3 * self.width * self.height, "|u1")
+
+    def selection(self) -> DeviceArray:
+        return DeviceArray(self._lib().gcfg_dt_selection(self.handle), self.width * self.height, "|u1")
+
+    def draw_selection(self, h_in, h_out=None):
+        a = np.ascontiguousarray(h_in, dtype=np.uint8)
+        out = np.empty_like(a) if h_out is None else h_out
+        _check(self._lib().gcfg_dt_draw_selection(self.handle, _ptr(a), _ptr(out)), "gcfg_dt_draw_selection")
+        return out
+
+    def nlinks(self, lam, d_up, d_down, d_left, d_right):
+        _check(self._lib().gcfg_dt_nlinks(self.handle, float(lam), _ptr(d_up), _ptr(d_down), _ptr(d_left),
+                                          _ptr(d_right)), "gcfg_dt_nlinks")
+
+    def close(self):
+        if self.handle:
+            _dt_lib().gcfg_dt_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DataTerm:
+    """The reference's DataTerm namespace (one process-wide state,
+    DataTerm.h:7-39) with its function names."""
+
+    _state = None
+    width = 0
+    height = 0
+
+    @classmethod
+    def _s(cls) -> DataTermState:
+        if cls._state is None:
+            raise GcfgError(GCFG_ERR_STATE, "DataTerm.init_data_term was not called")
+        return cls._state
+
+    @classmethod
+    def init_data_term(cls, w, h):
+        if cls._state is not None:
+            cls._state.close()
+        cls._state = DataTermState(w, h)
+        cls.width, cls.height = int(w), int(h)
+
+    @classmethod
+    def free_data_term(cls):
+        cls._s().close()
+        cls._state = None
+
+    @classmethod
+    def setImage(cls, h_img):
+        cls._s().set_image(h_img)
+
+    @classmethod
+    def setSelection(cls, h_select):
+        cls._s().set_selection(h_select)
+
+    @classmethod
+    def reset(cls):
+        cls._s().reset()
+
+    @classmethod
+    def selectOnMap(cls, x, y, sigma=None):
+        cls._s().select_on_map(x, y, 1)
+
+    @classmethod
+    def selectBackgroundOnMap(cls, x, y):
+        cls._s().select_on_map(x, y, 2)
+
+    @classmethod
+    def drawSelection(cls, inp, out=None):
+        return cls._s().draw_selection(inp, out)
+
+    @classmethod
+    def getDataTermsMixture(cls):
+        cls._s().compute()
+
+    @classmethod
+    def setSigmaGaussian(cls, sigma):
+        cls._s().set_sigma(sigma)
+
+    @classmethod
+    def getPos(cls) -> DeviceArray:
+        return cls._s().pos()
+
+    @classmethod
+    def getNeg(cls) -> DeviceArray:
+        return cls._s().neg()

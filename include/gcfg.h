@@ -119,6 +119,62 @@ gcfg_status gcfg_tlinks(const uint8_t *d_rgb, const uint8_t *d_scrib, int n, int
 gcfg_status gcfg_nlinks(const uint8_t *d_rgb, int w, int h, double lambda, int32_t *d_up,
                         int32_t *d_down, int32_t *d_left, int32_t *d_right, void *stream);
 
+/* ---------------- DataTerm state (drop-in for DataTerm.h:9-19) ---------------- */
+
+/* The reference's data-term state (an image, a selection map, a colour model
+ * and the two t-link arrays; DataTerm.cpp:28-165) as a handle.  The colour
+ * model is the 16^3 histogram pair of gcfg_tlinks, rebuilt from the current
+ * image and selection map by gcfg_dt_compute: selection class 1 = foreground
+ * (the reference's only class), 2 = background (the spec scribbles).
+ * The t-links are dp = round(10 * -log p_bg) (source, "positive") and
+ * dn = round(10 * -log p_fg) (sink, "negative"), W*H int32 on the device,
+ * owned by the handle, ready for gcfg_init.  All host copies are blocking. */
+typedef struct gcfg_dataterm gcfg_dataterm;
+
+/* Side of the square that gcfg_dt_select_on_map marks (DataTerm.cpp:113). */
+#define GCFG_DT_SELECT_SIZE 5
+
+/* init_data_term (DataTerm.cpp:28): allocate for a w x h image; empty selection. */
+gcfg_status gcfg_dt_create(int w, int h, gcfg_dataterm **out);
+/* free_data_term (DataTerm.cpp:67); unlike the reference the t-link arrays
+ * are freed too (they belong to the handle). */
+gcfg_status gcfg_dt_destroy(gcfg_dataterm *dt);
+gcfg_status gcfg_dt_set_stream(gcfg_dataterm *dt, void *stream);
+/* setImage (DataTerm.cpp:80): host image, 3*w*h bytes interleaved (any
+ * channel order: the histogram bins and colour distances do not depend on it). */
+gcfg_status gcfg_dt_set_image(gcfg_dataterm *dt, const uint8_t *h_img);
+/* The same from device memory (no counterpart). */
+gcfg_status gcfg_dt_set_image_device(gcfg_dataterm *dt, const uint8_t *d_img);
+/* setSelection (DataTerm.cpp:139): host int32 map of w*h, each value stored
+ * as one byte (0 none, 1 foreground, 2 background). */
+gcfg_status gcfg_dt_set_selection(gcfg_dataterm *dt, const int32_t *h_select);
+/* The selection as a device byte map of w*h (no counterpart). */
+gcfg_status gcfg_dt_set_scribbles_device(gcfg_dataterm *dt, const uint8_t *d_scrib);
+/* reset (DataTerm.cpp:88): clear the selection. */
+gcfg_status gcfg_dt_reset(gcfg_dataterm *dt);
+/* selectOnMap (DataTerm.cpp:105): mark the GCFG_DT_SELECT_SIZE square with
+ * corner (x, y) as class cls (1 or 2), clipped to the image. */
+gcfg_status gcfg_dt_select_on_map(gcfg_dataterm *dt, int x, int y, int cls);
+/* setSigmaGaussian (DataTerm.cpp:97): stored; the histogram model has no
+ * kernel width, so it does not change the t-links. */
+gcfg_status gcfg_dt_set_sigma(gcfg_dataterm *dt, int sigma);
+/* getDataTermsMixture (DataTerm.cpp:129): compute the t-links into the
+ * handle's arrays (returns when they are written). */
+gcfg_status gcfg_dt_compute(gcfg_dataterm *dt);
+/* getPos / getNeg (DataTerm.cpp:12,20): the device t-link arrays. */
+int32_t *gcfg_dt_pos(gcfg_dataterm *dt);
+int32_t *gcfg_dt_neg(gcfg_dataterm *dt);
+/* The handle's device image (3*w*h) and selection map (w*h) (no counterpart). */
+uint8_t *gcfg_dt_image(gcfg_dataterm *dt);
+uint8_t *gcfg_dt_selection(gcfg_dataterm *dt);
+/* drawSelection (DataTerm.cpp:155): h_in becomes the current image; h_out
+ * receives it with class-1 pixels set to (0, 0, 255) as in the reference and
+ * class-2 pixels set to (255, 0, 0). */
+gcfg_status gcfg_dt_draw_selection(gcfg_dataterm *dt, const uint8_t *h_in, uint8_t *h_out);
+/* gcfg_nlinks of the handle's current image (no counterpart). */
+gcfg_status gcfg_dt_nlinks(gcfg_dataterm *dt, double lambda, int32_t *d_up, int32_t *d_down,
+                           int32_t *d_left, int32_t *d_right);
+
 /* ---------------- one-image segmentation pipeline ---------------- */
 
 typedef struct gcfg_segmenter gcfg_segmenter;

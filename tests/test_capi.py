@@ -13,7 +13,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def _declared(header):
     src = open(os.path.join(ROOT, "include", header)).read()
-    return sorted(set(re.findall(r"^\s*(?:gcfg_status|const char|int64_t|double)\s*\*?\s*(gcfg_\w+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:gcfg_status|const char|int64_t|int32_t|uint8_t|double)\s*\*?\s*(gcfg_\w+)\s*\(", src, re.M)))
 
 
 def test_header_matches_binding_list():
