@@ -387,6 +387,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-plain", action="store_true", help="skip the per-image comparison leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default solver settings)")
+    ap.add_argument("--no-graph", action="store_true", help="run the batch without CUDA graph replay")
     ap.add_argument("--serve-requests", type=int, default=1200)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -459,6 +461,13 @@ def main():
         return np.array(flows)
 
     step = step_batch if batched else step_plain
+
+    # solver settings for this batch (untimed), then CUDA graph replay
+    tuning = None
+    if batched and not args.no_tune:
+        tuning = bs.autotune(Ws, Hs, lams, d_rgb, d_scrib, reps=2)
+    if batched and not args.no_graph:
+        bs.set_graph(True)
 
     def timed(fn, steps):
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -561,7 +570,8 @@ def main():
             "config": {"workload": args.workload, "desc": spec["desc"], "images_per_step": n_img,
                        "pixels_per_step": px_per_step, "mode": "batched" if batched else "per-image",
                        "l2": "flushed (256 MB write) before every step",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}",
+                       "tuning": tuning, "cuda_graph": bs.graph_info() if batched else None},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 4 * px_per_step,
                     "d2h_bytes_per_step": 2 * px_per_step, "ms_per_step": e2e_total / args.steps},
             "roofline": roofline, "clocks": clk, "gpu_launches": launches,

@@ -56,6 +56,7 @@ extern std::atomic<long long> g_launches;
 
 constexpr int PK_COUNT_KINDS = GCFG_PK_NKINDS;
 bool prof_on();
+bool prof_on();
 void prof_begin(cudaStream_t st);
 void prof_end(int kind, cudaStream_t st);
 

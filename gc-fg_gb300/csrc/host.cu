@@ -79,7 +79,44 @@ struct Engine {
     Ctl *h_ctl = nullptr; size_t ch_ctl = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
+    int max_grid = 0;  // solver blocks (0: as many as fit, capped at half the tiles)
+
+    // CUDA graphs of the device part of batch runs (opt-in, see run_batch_graph)
+    struct GraphEntry {
+        std::vector<int> w, h;
+        std::vector<double> lam;
+        const void *ptr[4];
+        bool staging;
+        SolveParams prm;
+        int grid;
+        long long alloc_gen;
+        long long kernels;
+        long long last_use;
+        cudaGraphExec_t exec;
+    };
+    static constexpr int MAX_GRAPHS = 4;
+    bool graph_on = false, graph_broken = false;
+    std::vector<GraphEntry> graphs;
+    cudaStream_t cap_st = nullptr;
+    long long graph_kernels = 0, graph_replays = 0, graph_captures = 0, graph_clock = 0;
+    long long alloc_gen = 0;  // bumped whenever a buffer is reallocated
+    // sizes and lambdas of the layout currently on the device
+    std::vector<int> lay_w, lay_h;
+    std::vector<double> lay_lam;
+
     ~Engine() { release(); }
+
+    void drop_graphs() {
+        for (auto &g : graphs) cudaGraphExecDestroy(g.exec);
+        graphs.clear();
+    }
+
+    bool laid_out(int n, const int *W, const int *H, const double *lam) const {
+        if ((int)lay_w.size() != n) return false;
+        for (int i = 0; i < n; ++i)
+            if (lay_w[i] != W[i] || lay_h[i] != H[i] || lay_lam[i] != lam[i]) return false;
+        return true;
+    }
 
     void release() {
         cudaFree(d_img); cudaFree(d_ist); cudaFree(d_chunk); cudaFree(d_tile_img);
@@ -96,6 +133,9 @@ struct Engine {
         if (h_ctl) cudaFreeHost(h_ctl);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        drop_graphs();
+        if (cap_st) cudaStreamDestroy(cap_st);
+        cap_st = nullptr;
         d_img = nullptr; d_ist = nullptr; d_chunk = nullptr; d_tile_img = nullptr;
         d_cap = nullptr; d_exc = nullptr; d_h = nullptr; d_reach = nullptr;
         d_tmask = nullptr; d_tact = nullptr; d_tpos = nullptr;
@@ -125,7 +165,21 @@ struct Engine {
         }
     }
 
+    std::vector<const void *> buffers() const {
+        return {d_img, d_ist, d_chunk, d_tile_img, d_cap, d_exc, d_h, d_reach, d_tmask, d_tact, d_tpos,
+                d_lists, d_mpush, d_mgr, d_ctl, d_hist, d_dpl, d_dnl, d_rgb, d_scrib, d_smin, d_smax,
+                h_img, h_ist, h_chunk, h_tile_img, h_ctl};
+    }
+
+    // Grow the buffers; any reallocation invalidates the captured graphs.
     gcfg_status reserve(int imgs, int tiles, long long px, bool dataterm, bool staging, bool arena = true) {
+        const std::vector<const void *> before = buffers();
+        const gcfg_status rc = reserve_(imgs, tiles, px, dataterm, staging, arena);
+        if (buffers() != before) ++alloc_gen;
+        return rc;
+    }
+
+    gcfg_status reserve_(int imgs, int tiles, long long px, bool dataterm, bool staging, bool arena) {
         GCFG_TRY(grow(d_img, c_img, imgs));
         GCFG_TRY(grow(d_ist, c_ist, imgs));
         GCFG_TRY(grow(d_chunk, c_chunk, (size_t)imgs + 1));
@@ -207,6 +261,12 @@ struct Engine {
         if (arena)
             GCFG_CK(cudaMemcpyAsync(d_tile_img, h_tile_img, (size_t)t * sizeof(int), cudaMemcpyHostToDevice, st));
         GCFG_CK(cudaMemsetAsync(d_ist, 0, n * sizeof(ImgState), st));
+        lay_w.assign(W, W + n);
+        lay_h.assign(H, H + n);
+        if (lam)
+            lay_lam.assign(lam, lam + n);
+        else
+            lay_lam.assign(n, 0.0);
         return GCFG_OK;
     }
 
@@ -262,13 +322,19 @@ struct Engine {
 
     gcfg_status solve() {
         GCFG_CK(cudaMemsetAsync(d_ctl, 0, sizeof(Ctl), st));
-        return launch_solve(batch(), prm, n_tiles, st);
+        return launch_solve(batch(), prm, n_tiles, st, max_grid);
+    }
+
+    // Queue the read-back of the per-image states and the control block.
+    gcfg_status readback() {
+        GCFG_CK(cudaMemcpyAsync(h_ist, d_ist, n_img * sizeof(ImgState), cudaMemcpyDeviceToHost, st));
+        GCFG_CK(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+        return GCFG_OK;
     }
 
     // Read the per-image states and the control block (synchronises).
     gcfg_status fetch() {
-        GCFG_CK(cudaMemcpyAsync(h_ist, d_ist, n_img * sizeof(ImgState), cudaMemcpyDeviceToHost, st));
-        GCFG_CK(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+        GCFG_TRY(readback());
         GCFG_CK(cudaStreamSynchronize(st));
         return GCFG_OK;
     }
@@ -513,9 +579,9 @@ gcfg_status gcfg_nlinks(const uint8_t *d_rgb, int w, int h, double lambda, int32
 // Segmenter (one image) and batch
 // ---------------------------------------------------------------------------
 
-static gcfg_status run_batch(Engine &e, int n, const int *W, const int *H, const double *lam,
-                             const uint8_t *rgb, const uint8_t *scrib, uint8_t *smin, uint8_t *smax,
-                             int64_t *flows, gcfg_result *res, bool staging) {
+static gcfg_status run_batch_eager(Engine &e, int n, const int *W, const int *H, const double *lam,
+                                   const uint8_t *rgb, const uint8_t *scrib, uint8_t *smin, uint8_t *smax,
+                                   int64_t *flows, gcfg_result *res, bool staging) {
     GCFG_CK(cudaEventRecord(e.ev0, e.st));
     GCFG_TRY(e.layout(n, W, H, lam, true, staging));
     if (staging) {
@@ -545,6 +611,135 @@ static gcfg_status run_batch(Engine &e, int n, const int *W, const int *H, const
         if (res) res[i] = r;
     }
     return e.status();
+}
+
+// The device part of a run (per-image counters reset, data term, build,
+// persistent solve, extraction, read-back of the per-image states) captured
+// once into a CUDA graph and replayed while the batch is the same: same
+// sizes, lambdas, buffers and solver settings.  The persistent solver already
+// runs the whole push / local relabel / global relabel loop without host round
+// trips; the graph removes the remaining per-kernel launch work.  Host
+// copies of the host entry points stay outside the graph.
+static gcfg_status run_batch_graph(Engine &e, int n, const int *W, const int *H, const double *lam,
+                                   const uint8_t *rgb, const uint8_t *scrib, uint8_t *smin, uint8_t *smax,
+                                   int64_t *flows, gcfg_result *res, bool staging) {
+    // host inputs are copied in outside the graph; only device buffers are baked in
+    const void *ptr[4] = {staging ? nullptr : rgb, staging ? nullptr : scrib, smin, smax};
+    auto same = [&](const Engine::GraphEntry &g) {
+        if ((int)g.w.size() != n || g.staging != staging || g.grid != e.max_grid || g.alloc_gen != e.alloc_gen)
+            return false;
+        if (memcmp(&g.prm, &e.prm, sizeof(SolveParams)) != 0) return false;
+        for (int k = 0; k < 4; ++k)
+            if (g.ptr[k] != ptr[k]) return false;
+        for (int i = 0; i < n; ++i)
+            if (g.w[i] != W[i] || g.h[i] != H[i] || g.lam[i] != lam[i]) return false;
+        return true;
+    };
+    Engine::GraphEntry *hit = nullptr;
+    for (auto &g : e.graphs)
+        if (same(g)) hit = &g;
+    if (!e.laid_out(n, W, H, lam) || !hit) {
+        const long long gen = e.alloc_gen;
+        GCFG_TRY(e.layout(n, W, H, lam, true, staging));
+        if (e.alloc_gen != gen) {  // buffers moved: every captured graph is stale
+            e.drop_graphs();
+            hit = nullptr;
+        }
+    }
+    if (!hit) {
+        const uint8_t *drgb = staging ? e.d_rgb : rgb, *dscrib = staging ? e.d_scrib : scrib;
+        uint8_t *dmin = staging ? (smin ? e.d_smin : nullptr) : smin;
+        uint8_t *dmax = staging ? (smax ? e.d_smax : nullptr) : smax;
+        if (!e.cap_st) GCFG_CK(cudaStreamCreateWithFlags(&e.cap_st, cudaStreamNonBlocking));
+        // the layout uploads were queued on the caller's stream; the graph is
+        // launched there too, after them
+        cudaStream_t user = e.st;
+        e.st = e.cap_st;
+        const long long l0 = g_launches.load();
+        gcfg_status rc = GCFG_OK;
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(e.cap_st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            rc = GCFG_ERR_CUDA;
+        } else {
+            if (cudaMemsetAsync(e.d_ist, 0, (size_t)n * sizeof(ImgState), e.st) != cudaSuccess) rc = GCFG_ERR_CUDA;
+            if (rc == GCFG_OK) rc = e.build_images(drgb, dscrib);
+            if (rc == GCFG_OK) rc = e.solve();
+            if (rc == GCFG_OK && (dmin || dmax)) rc = launch_extract(e.batch(), dmin, dmax, nullptr, e.st);
+            if (rc == GCFG_OK) rc = e.readback();
+            if (cudaStreamEndCapture(e.cap_st, &g) != cudaSuccess && rc == GCFG_OK) rc = GCFG_ERR_CUDA;
+        }
+        e.st = user;
+        const long long kernels = g_launches.load() - l0;
+        g_launches.fetch_sub(kernels);  // counted when the graph runs
+        cudaGraphExec_t exec = nullptr;
+        if (rc == GCFG_OK && g && cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) {
+            exec = nullptr;
+            rc = GCFG_ERR_CUDA;
+        }
+        if (g) cudaGraphDestroy(g);
+        if (rc != GCFG_OK) {
+            // capture is not available here: run without graphs from now on
+            cudaGetLastError();
+            e.graph_broken = true;
+            e.drop_graphs();
+            return run_batch_eager(e, n, W, H, lam, rgb, scrib, smin, smax, flows, res, staging);
+        }
+        if ((int)e.graphs.size() >= Engine::MAX_GRAPHS) {  // drop the least recently used
+            size_t old = 0;
+            for (size_t k = 1; k < e.graphs.size(); ++k)
+                if (e.graphs[k].last_use < e.graphs[old].last_use) old = k;
+            cudaGraphExecDestroy(e.graphs[old].exec);
+            e.graphs.erase(e.graphs.begin() + old);
+        }
+        Engine::GraphEntry ge;
+        ge.w.assign(W, W + n);
+        ge.h.assign(H, H + n);
+        ge.lam.assign(lam, lam + n);
+        for (int k = 0; k < 4; ++k) ge.ptr[k] = ptr[k];
+        ge.staging = staging;
+        ge.prm = e.prm;
+        ge.grid = e.max_grid;
+        ge.alloc_gen = e.alloc_gen;
+        ge.kernels = kernels;
+        ge.last_use = 0;
+        ge.exec = exec;
+        e.graphs.push_back(ge);
+        hit = &e.graphs.back();
+        e.graph_captures++;
+    }
+    hit->last_use = ++e.graph_clock;
+    e.graph_kernels = hit->kernels;
+    if (staging) {
+        GCFG_CK(cudaMemcpyAsync(e.d_rgb, rgb, (size_t)e.n_px * 3, cudaMemcpyHostToDevice, e.st));
+        GCFG_CK(cudaMemcpyAsync(e.d_scrib, scrib, (size_t)e.n_px, cudaMemcpyHostToDevice, e.st));
+    }
+    GCFG_CK(cudaEventRecord(e.ev0, e.st));
+    GCFG_CK(cudaGraphLaunch(hit->exec, e.st));
+    GCFG_CK(cudaEventRecord(e.ev1, e.st));
+    g_launches.fetch_add(hit->kernels, std::memory_order_relaxed);
+    e.graph_replays++;
+    if (staging) {
+        if (smin) GCFG_CK(cudaMemcpyAsync(smin, e.d_smin, (size_t)e.n_px, cudaMemcpyDeviceToHost, e.st));
+        if (smax) GCFG_CK(cudaMemcpyAsync(smax, e.d_smax, (size_t)e.n_px, cudaMemcpyDeviceToHost, e.st));
+    }
+    GCFG_CK(cudaStreamSynchronize(e.st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e.ev0, e.ev1);
+    for (int i = 0; i < n; ++i) {
+        gcfg_result r;
+        e.result(i, &r, ms);
+        if (flows) flows[i] = r.flow;
+        if (res) res[i] = r;
+    }
+    return e.status();
+}
+
+static gcfg_status run_batch(Engine &e, int n, const int *W, const int *H, const double *lam,
+                             const uint8_t *rgb, const uint8_t *scrib, uint8_t *smin, uint8_t *smax,
+                             int64_t *flows, gcfg_result *res, bool staging) {
+    if (e.graph_on && !e.graph_broken && !prof_on())
+        return run_batch_graph(e, n, W, H, lam, rgb, scrib, smin, smax, flows, res, staging);
+    return run_batch_eager(e, n, W, H, lam, rgb, scrib, smin, smax, flows, res, staging);
 }
 
 gcfg_status gcfg_seg_create(int max_w, int max_h, gcfg_segmenter **out) {
@@ -617,6 +812,108 @@ gcfg_status gcfg_batch_set_params(gcfg_batch *b, int push_rounds_per_gr, int max
     b->e.prm.push_rounds = push_rounds_per_gr;
     b->e.prm.max_sweeps = max_tile_sweeps;
     b->e.prm.bfs_every = sweeps_per_local_relabel;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_batch_set_graph(gcfg_batch *b, int enable) {
+    if (!b) return GCFG_ERR_INVALID;
+    b->e.graph_on = enable != 0;
+    if (!enable) b->e.drop_graphs();
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_batch_graph_info(gcfg_batch *b, int *active, int64_t *captures, int64_t *replays,
+                                  int64_t *kernels_per_replay) {
+    if (!b) return GCFG_ERR_INVALID;
+    if (active) *active = b->e.graph_on && !b->e.graph_broken;
+    if (captures) *captures = b->e.graph_captures;
+    if (replays) *replays = b->e.graph_replays;
+    if (kernels_per_replay) *kernels_per_replay = b->e.graph_kernels;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const int *heights, const double *lambdas,
+                                const uint8_t *d_rgb, const uint8_t *d_scrib, int reps, gcfg_tuning *out) {
+    if (!b || n < 1 || !widths || !heights || !lambdas || !d_rgb || !d_scrib || reps < 1) return GCFG_ERR_INVALID;
+    Engine &e = b->e;
+    const bool graph = e.graph_on;
+    e.graph_on = false;  // time the eager runs; the graph is recaptured afterwards
+    e.drop_graphs();
+    int dev = 0, sms = 1, per_sm = 1;
+    GCFG_CK(cudaGetDevice(&dev));
+    GCFG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int full = solve_grid_blocks(1 << 30);
+    per_sm = full / (sms > 0 ? sms : 1);
+    if (per_sm < 1) per_sm = 1;
+
+    std::vector<int64_t> ref(n), got(n);
+    std::vector<gcfg_result> rr(n);
+    int tried = 0;
+    gcfg_status rc = GCFG_OK;
+    // time of one configuration: fastest of `reps` runs; every run must give
+    // the flows of the first
+    auto time_cfg = [&](const SolveParams &p, int bps, float *ms) -> gcfg_status {
+        e.prm = p;
+        e.max_grid = bps * sms;
+        float best = 1e30f;
+        for (int k = 0; k < reps; ++k) {
+            GCFG_TRY(run_batch_eager(e, n, widths, heights, lambdas, d_rgb, d_scrib, nullptr, nullptr, got.data(),
+                                     rr.data(), false));
+            if (tried == 0 && k == 0) ref = got;
+            if (got != ref) return GCFG_ERR_NOT_CONVERGED;
+            if (rr[0].ms < best) best = rr[0].ms;
+        }
+        ++tried;
+        *ms = best;
+        return GCFG_OK;
+    };
+    SolveParams cur = e.prm;
+    int cur_bps = e.max_grid > 0 ? (e.max_grid + sms - 1) / sms : per_sm;
+    if (cur_bps > per_sm) cur_bps = per_sm;
+    float ms_default = 0.f;
+    rc = time_cfg(cur, cur_bps, &ms_default);  // warms up, then the default
+    if (rc == GCFG_OK) rc = time_cfg(cur, cur_bps, &ms_default);
+    float best = ms_default;
+    static const int c_push[] = {2, 4, 8, 16};
+    static const int c_sweeps[] = {16, 32, 64, 128};
+    static const int c_bfs[] = {8, 16, 32, 64};
+    for (int pass = 0; pass < 2 && rc == GCFG_OK; ++pass) {
+        for (int which = 0; which < 4 && rc == GCFG_OK; ++which) {
+            const int nc = which == 3 ? per_sm : 4;
+            for (int c = 0; c < nc && rc == GCFG_OK; ++c) {
+                SolveParams p = cur;
+                int bps = cur_bps;
+                if (which == 0) p.push_rounds = c_push[c];
+                if (which == 1) p.max_sweeps = c_sweeps[c];
+                if (which == 2) p.bfs_every = c_bfs[c];
+                if (which == 3) bps = c + 1;
+                if (memcmp(&p, &cur, sizeof(p)) == 0 && bps == cur_bps) continue;
+                float ms = 0.f;
+                rc = time_cfg(p, bps, &ms);
+                if (rc == GCFG_OK && ms < best * 0.98f) {  // keep a change only for a clear gain
+                    best = ms;
+                    cur = p;
+                    cur_bps = bps;
+                }
+            }
+        }
+    }
+    e.prm = cur;
+    e.max_grid = cur_bps * sms;
+    e.graph_on = graph;
+    if (rc != GCFG_OK) return rc;
+    if (out) {
+        out->push_rounds_per_gr = cur.push_rounds;
+        out->max_tile_sweeps = cur.max_sweeps;
+        out->sweeps_per_local_relabel = cur.bfs_every;
+        out->blocks_per_sm = cur_bps;
+        out->ms_default = ms_default;
+        out->ms_best = best;
+        out->configs_tried = tried;
+        out->tile_w = TILE_W;
+        out->tile_h = TILE_H;
+        out->pad = 0;
+    }
     return GCFG_OK;
 }
 

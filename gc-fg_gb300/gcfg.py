@@ -37,7 +37,7 @@ EXPORTS = [
     "gcfg_seg_set_stream", "gcfg_seg_destroy", "gcfg_strerror", "gcfg_launch_count",
     "gcfg_profile_enable", "gcfg_profile_read", "gcfg_batch_create", "gcfg_batch_set_stream",
     "gcfg_batch_set_params", "gcfg_batch_run", "gcfg_batch_run_host", "gcfg_batch_destroy",
-    "gcfg_solve_noalloc",
+    "gcfg_solve_noalloc", "gcfg_batch_set_graph", "gcfg_batch_graph_info", "gcfg_batch_autotune",
 ]
 
 PROF_KINDS = ["hist", "tlut", "sigma", "wlut", "build", "solve", "extract", "other"]
@@ -62,6 +62,16 @@ class Result(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Tuning(C.Structure):
+    _fields_ = [("push_rounds_per_gr", C.c_int32), ("max_tile_sweeps", C.c_int32),
+                ("sweeps_per_local_relabel", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("ms_default", C.c_float), ("ms_best", C.c_float), ("configs_tried", C.c_int32),
+                ("tile_w", C.c_int32), ("tile_h", C.c_int32), ("pad", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
 
 
 class ProfEntry(C.Structure):
@@ -108,6 +118,10 @@ def load(path: str = LIB_PATH):
         "gcfg_batch_run": (S, [P, I, P, P, P, P, P, P, P, P, P]),
         "gcfg_batch_run_host": (S, [P, I, P, P, P, P, P, P, P, P, P]),
         "gcfg_batch_destroy": (S, [P]),
+        "gcfg_batch_set_graph": (S, [P, I]),
+        "gcfg_batch_graph_info": (S, [P, C.POINTER(I), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                      C.POINTER(C.c_int64)]),
+        "gcfg_batch_autotune": (S, [P, I, P, P, P, P, P, I, C.POINTER(Tuning)]),
         "gcfg_solve_noalloc": (S, [I, I, P, P, C.c_int32, P, P, P, P, P, C.POINTER(C.c_int64), P]),
         "gcfg_profile_enable": (S, [I]),
         "gcfg_profile_read": (S, [C.POINTER(ProfEntry), I, C.POINTER(I)]),
@@ -325,6 +339,25 @@ class BatchSolver:
     def set_params(self, push_rounds_per_gr, max_tile_sweeps, sweeps_per_local_relabel):
         _check(load().gcfg_batch_set_params(self.handle, int(push_rounds_per_gr), int(max_tile_sweeps),
                                             int(sweeps_per_local_relabel)), "gcfg_batch_set_params")
+
+    def set_graph(self, enable=True):
+        """CUDA graph replay of repeated identical batches (gcfg_batch_set_graph)."""
+        _check(load().gcfg_batch_set_graph(self.handle, int(bool(enable))), "gcfg_batch_set_graph")
+
+    def graph_info(self) -> dict:
+        a = C.c_int()
+        c, r, k = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(load().gcfg_batch_graph_info(self.handle, C.byref(a), C.byref(c), C.byref(r), C.byref(k)),
+               "gcfg_batch_graph_info")
+        return {"active": bool(a.value), "captures": c.value, "replays": r.value, "kernels_per_replay": k.value}
+
+    def autotune(self, widths, heights, lambdas, d_rgb, d_scrib, reps=3) -> dict:
+        """Pick the solver settings for this batch (gcfg_batch_autotune)."""
+        w, h, lam = self._arrays(widths, heights, lambdas)
+        t = Tuning()
+        _check(load().gcfg_batch_autotune(self.handle, len(w), _ptr(w), _ptr(h), _ptr(lam), _ptr(d_rgb),
+                                          _ptr(d_scrib), int(reps), C.byref(t)), "gcfg_batch_autotune")
+        return t.as_dict()
 
     @staticmethod
     def _arrays(widths, heights, lambdas):

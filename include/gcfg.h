@@ -223,6 +223,39 @@ gcfg_status gcfg_batch_run_host(gcfg_batch *b, int n, const int *widths, const i
                                 gcfg_result *h_res);
 gcfg_status gcfg_batch_destroy(gcfg_batch *b);
 
+/* CUDA graph replay (off by default).  When on, the device part of a run
+ * (data term, graph build, the persistent solver launch that runs the whole
+ * push / local relabel / global relabel loop, extraction, read-back of the
+ * results) is captured into a CUDA graph the first time a batch is run and
+ * replayed while the next runs have the same sizes, lambdas, device buffers
+ * and solver settings; anything else recaptures.  If the device cannot
+ * capture, runs continue without the graph (gcfg_batch_graph_info: active 0).
+ * Results are identical either way.  No counterpart in the reference. */
+gcfg_status gcfg_batch_set_graph(gcfg_batch *b, int enable);
+gcfg_status gcfg_batch_graph_info(gcfg_batch *b, int *active, int64_t *captures, int64_t *replays,
+                                  int64_t *kernels_per_replay);
+
+/* Autotuner result: the solver settings chosen for a batch. */
+typedef struct {
+    int32_t push_rounds_per_gr;       /* checkerboard push rounds between global relabels */
+    int32_t max_tile_sweeps;          /* push/relabel sweeps per tile visit */
+    int32_t sweeps_per_local_relabel; /* sweeps between exact local (tile BFS) relabels */
+    int32_t blocks_per_sm;            /* persistent solver blocks per SM */
+    float ms_default, ms_best;        /* device time of one run before / after tuning */
+    int32_t configs_tried;
+    int32_t tile_w, tile_h;           /* tile shape (fixed: the width of the bit-plane BFS) */
+    int32_t pad;
+} gcfg_tuning;
+
+/* Time the batch (device-resident, as gcfg_batch_run) under candidate solver
+ * settings by coordinate search, keep the fastest, and use it for the
+ * following runs of this handle.  Each setting is timed as the fastest of
+ * `reps` runs; every run must reproduce the flows of the first (else
+ * GCFG_ERR_NOT_CONVERGED).  No counterpart in the reference. */
+gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const int *heights,
+                                const double *lambdas, const uint8_t *d_rgb, const uint8_t *d_scrib,
+                                int reps, gcfg_tuning *out);
+
 /* ---------------- serving (continuous batching, resident images) ---------------- */
 
 /* A server keeps every admitted image resident on the device (pixels,

@@ -1,0 +1,95 @@
+"""Batch API: CUDA graph replay and the autotuner change no result."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import gcfg  # noqa: E402
+import synth  # noqa: E402
+
+
+def _batch(n, seed0):
+    shapes = [(W, H) for (W, H, _) in synth.batch_shapes(n, seed0, lo=48, hi=400)]
+    rgb, scrib, offs = synth.generate_packed([(3, W, H, seed0 + i) for i, (W, H) in enumerate(shapes)])
+    Ws = np.array([w for w, _ in shapes], np.int32)
+    Hs = np.array([h for _, h in shapes], np.int32)
+    lams = np.array([(10.0, 50.0, 200.0)[i % 3] for i in range(n)])
+    return Ws, Hs, lams, rgb, scrib
+
+
+def _run(bs, Ws, Hs, lams, d_rgb, d_scrib):
+    n_px = int(np.sum(Ws.astype(np.int64) * Hs))
+    smin = torch.empty(n_px, dtype=torch.uint8, device="cuda")
+    smax = torch.empty(n_px, dtype=torch.uint8, device="cuda")
+    flows, _ = bs.run(Ws, Hs, lams, d_rgb, d_scrib, smin, smax)
+    return flows, smin.cpu().numpy(), smax.cpu().numpy()
+
+
+def test_graph_replay_equals_eager():
+    Ws, Hs, lams, rgb, scrib = _batch(40, 3100)
+    d_rgb = torch.from_numpy(rgb).cuda()
+    d_scrib = torch.from_numpy(scrib).cuda()
+    bs = gcfg.BatchSolver(64, scrib.size)
+    ref = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
+    bs.set_graph(True)
+    n_px = scrib.size
+    smin = torch.empty(n_px, dtype=torch.uint8, device="cuda")
+    smax = torch.empty(n_px, dtype=torch.uint8, device="cuda")
+    l0 = gcfg.launch_count()
+    for _ in range(3):
+        smin.fill_(7)
+        smax.fill_(7)
+        flows, _ = bs.run(Ws, Hs, lams, d_rgb, d_scrib, smin, smax)
+        assert np.array_equal(flows, ref[0])
+        assert np.array_equal(smin.cpu().numpy(), ref[1]) and np.array_equal(smax.cpu().numpy(), ref[2])
+    info = bs.graph_info()
+    assert info["active"], "stream capture of the batch pipeline failed"
+    assert info["captures"] == 1 and info["replays"] == 3 and info["kernels_per_replay"] >= 5
+    assert gcfg.launch_count() - l0 == 3 * info["kernels_per_replay"]
+    # other lambdas: recaptured, and equal to an eager run
+    lams2 = lams[::-1].copy()
+    flows2, _ = bs.run(Ws, Hs, lams2, d_rgb, d_scrib, smin, smax)
+    assert bs.graph_info()["captures"] == 2
+    bs.set_graph(False)
+    assert np.array_equal(flows2, _run(bs, Ws, Hs, lams2, d_rgb, d_scrib)[0])
+    # host entry point through the graph
+    bs.set_graph(True)
+    h_min = np.zeros(n_px, np.uint8)
+    h_max = np.zeros(n_px, np.uint8)
+    for _ in range(2):
+        fh, _ = bs.run_host(Ws, Hs, lams, rgb, scrib, h_min, h_max)
+        assert np.array_equal(fh, ref[0]) and np.array_equal(h_min, ref[1]) and np.array_equal(h_max, ref[2])
+    # device and host runs alternating: both graphs stay cached, results unchanged
+    bs.run(Ws, Hs, lams, d_rgb, d_scrib, smin, smax)
+    c0 = bs.graph_info()["captures"]
+    for _ in range(3):
+        flows, _ = bs.run(Ws, Hs, lams, d_rgb, d_scrib, smin, smax)
+        fh, _ = bs.run_host(Ws, Hs, lams, rgb, scrib, h_min, h_max)
+        assert np.array_equal(flows, ref[0]) and np.array_equal(fh, ref[0])
+        assert np.array_equal(smin.cpu().numpy(), ref[1]) and np.array_equal(h_max, ref[2])
+    assert bs.graph_info()["captures"] == c0
+    # a different batch in between: its layout is uploaded again before a replay
+    Ws3, Hs3 = Ws[:10].copy(), Hs[:10].copy()
+    n3 = int(np.sum(Ws3.astype(np.int64) * Hs3))
+    f3, _ = bs.run(Ws3, Hs3, lams[:10], d_rgb, d_scrib, smin[:n3], smax[:n3])
+    flows, _ = bs.run(Ws, Hs, lams, d_rgb, d_scrib, smin, smax)
+    assert np.array_equal(flows, ref[0]) and np.array_equal(f3, ref[0][:10])
+    bs.close()
+
+
+def test_autotune_keeps_results():
+    Ws, Hs, lams, rgb, scrib = _batch(48, 3300)
+    d_rgb = torch.from_numpy(rgb).cuda()
+    d_scrib = torch.from_numpy(scrib).cuda()
+    bs = gcfg.BatchSolver(64, scrib.size)
+    ref = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
+    t = bs.autotune(Ws, Hs, lams, d_rgb, d_scrib, reps=2)
+    assert t["configs_tried"] >= 10
+    assert t["push_rounds_per_gr"] in (2, 4, 8, 16) and t["max_tile_sweeps"] in (16, 32, 64, 128)
+    assert t["sweeps_per_local_relabel"] in (8, 16, 32, 64) and 1 <= t["blocks_per_sm"] <= 8
+    assert t["ms_best"] <= t["ms_default"] and (t["tile_w"], t["tile_h"]) == (32, 32)
+    got = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
+    for a, b in zip(ref, got):
+        assert np.array_equal(a, b)
+    bs.close()
