@@ -31,6 +31,22 @@ __device__ __forceinline__ int diff2p(const uint8_t *__restrict__ a, const uint8
     return d0 * d0 + d1 * d1 + d2 * d2;
 }
 
+// Colour of a pixel as one word: r | g << 8 | b << 16.
+__device__ __forceinline__ uint32_t pack_rgb(const uint8_t *__restrict__ p) {
+    return (uint32_t)__ldg(p) | ((uint32_t)__ldg(p + 1) << 8) | ((uint32_t)__ldg(p + 2) << 16);
+}
+
+// ||a - b||^2 of two packed colours: per-byte absolute differences, then the
+// dot product of that word with itself (the top byte is 0 in both).
+__device__ __forceinline__ int diff2w(uint32_t a, uint32_t b) {
+    const uint32_t d = __vabsdiffu4(a, b);
+    return (int)__dp4a(d, d, 0u);
+}
+
+__device__ __forceinline__ int color_binw(uint32_t c) {
+    return (((c >> 4) & 0xFu) << 8) | (((c >> 12) & 0xFu) << 4) | ((c >> 20) & 0xFu);
+}
+
 // Image of a global chunk index (chunk_off: prefix sums of chunks per image).
 __device__ __forceinline__ int chunk_image(const long long *__restrict__ chunk_off, int n_img,
                                            long long chunk) {
@@ -76,8 +92,17 @@ __device__ __forceinline__ int tlink_quant(int h, long long N) {
 // <= ln(2 lambda): the error is then < lambda * 2e-7 * (ln(2 lambda) + 4),
 // below the margin 1e-5 * lambda + 1e-5 for every lambda up to 2^28.
 // (Large |a| only make v smaller: it underflows toward 0 and rounds to 0.)
+//
+// The fast path uses no conversion instructions (they share a slow pipe on
+// this GPU): d2 < 2^23 becomes a float by writing it into the mantissa of
+// 2^23, and for lambda < 2^22 the nearest integer of v comes from adding
+// 1.5 * 2^23 (round to nearest even; exact ties cannot pass the margin test).
+// v is at distance 0.5 - |v - rint(v)| from the nearest k + 0.5, so the
+// margin test reads |v - rint(v)| < 0.5 - margin.
 struct NlinkParams {
     float lf, inv;       // (float)lambda, (float)(1 / (2 sigma^2))
+    float half_margin;   // 0.5 - (1e-5 * lambda + 1e-5)
+    int small;           // lambda < 2^22: the magic-number rounding applies
     int constant;        // constant image: every weight is const_w = round(lambda)
     int const_w;
     double lambda, s2;   // only read on the exact (near-tie) path
@@ -113,11 +138,24 @@ __device__ __forceinline__ NlinkParams nlink_params(double lambda, const ImgStat
     q.inv = st.inv2s2;
     q.constant = st.inv2s2 == 0.f;
     q.const_w = st.const_w;
+    q.half_margin = 0.5f - (1e-5f * q.lf + 1e-5f);
+    q.small = q.lf < 4194304.0f;
     return q;
 }
 
+// Exact float of 0 <= d2 < 2^23 (squared colour distances are <= 3 * 255^2).
+__device__ __forceinline__ float small_int_to_float(int d2) {
+    return __fsub_rn(__int_as_float(0x4B000000 | d2), 8388608.0f);
+}
+
 __device__ __forceinline__ int nlink_quant(int d2, const NlinkParams &q) {
-    const float v = q.lf * expf(-(float)d2 * q.inv);
+    const float v = q.lf * expf(-small_int_to_float(d2) * q.inv);
+    if (q.small) {
+        const float t = __fadd_rn(v, 12582912.0f);  // 1.5 * 2^23 + rint(v)
+        const float rf = __fsub_rn(t, 12582912.0f);
+        if (fabsf(__fsub_rn(v, rf)) < q.half_margin) return __float_as_int(t) - 0x4B400000;
+        return nlink_exact(d2, q.lambda, q.s2);
+    }
     const float fr = v - floorf(v);
     if (fabsf(fr - 0.5f) > 1e-5f * q.lf + 1e-5f) return (int)floorf(v + 0.5f);
     return nlink_exact(d2, q.lambda, q.s2);
@@ -133,7 +171,7 @@ __global__ void __launch_bounds__(256) k_hist_sigma_b(const uint8_t *__restrict_
                                                       const long long *__restrict__ chunk_off, int n_img,
                                                       const int *__restrict__ ilist, int *__restrict__ hist,
                                                       ImgState *ist) {
-    __shared__ int sh[2 * NBINS];
+    __shared__ __align__(16) int sh[2 * NBINS];
     const int li = chunk_image(chunk_off, n_img, blockIdx.x);
     const int im = ilist ? ilist[li] : li;
     const int W = img[im].W, H = img[im].H;
@@ -143,28 +181,59 @@ __global__ void __launch_bounds__(256) k_hist_sigma_b(const uint8_t *__restrict_
     const long long pix0 = img[im].pix0;
     const uint8_t *base = rgb + 3 * pix0;
     const bool do_hist = scrib != nullptr;
-    if (do_hist)
-        for (int i = threadIdx.x; i < 2 * NBINS; i += blockDim.x) sh[i] = 0;
+    if (do_hist) {
+        int4 *s4 = reinterpret_cast<int4 *>(sh);
+        for (int i = threadIdx.x; i < 2 * NBINS / 4; i += blockDim.x) s4[i] = make_int4(0, 0, 0, 0);
+    }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned long long acc = 0;
-    // warps take rows, lanes take columns: no per-pixel division, and every
-    // lane of a warp runs the same iterations (full-warp collectives)
-    for (int y = y0 + warp; y < y1; y += blockDim.x >> 5) {
-        for (int xb = 0; xb < W; xb += 32) {
-            const int x = xb + lane;
+    // Items are (row, 32-column group) pairs of the chunk in row-major order;
+    // warp w takes items w, w + 8, ...  Two items' loads are issued before
+    // either is used.  Loop bounds are warp-uniform (full-warp collectives).
+    const int nw = blockDim.x >> 5;
+    const int ncg = (W + 31) >> 5;
+    const int items = (y1 - y0) * ncg;
+    int k = warp, y = y0 + warp / ncg, cg = warp % ncg;
+    constexpr int U = 2;
+    while (k < items) {
+        uint32_t c[U], dn[U], r31[U];
+        int sc[U], ys[U], xs[U];
+        bool ok[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            ok[u] = k < items;
+            const int x = cg * 32 + lane;
+            ys[u] = y;
+            xs[u] = x;
+            const bool in = ok[u] && x < W;
+            const long long i = (long long)y * W + x;
+            const uint8_t *p = base + 3 * i;
+            c[u] = in ? pack_rgb(p) : 0u;
+            dn[u] = (in && y + 1 < H) ? pack_rgb(p + 3 * (long long)W) : 0u;
+            r31[u] = (lane == 31 && in && x + 1 < W) ? pack_rgb(p + 3) : 0u;
+            sc[u] = (do_hist && in) ? (int)__ldg(scrib + pix0 + i) : 0;
+            k += nw;
+            cg += nw;
+            while (cg >= ncg) {
+                cg -= ncg;
+                ++y;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (!ok[u]) break;  // warp-uniform
+            const int x = xs[u];
+            uint32_t right = __shfl_down_sync(0xffffffffu, c[u], 1);
+            if (lane == 31) right = r31[u];
             int key = -1;
             if (x < W) {
-                const long long i = (long long)y * W + x;
-                const uint8_t *p = base + 3 * i;
-                if (x + 1 < W) acc += (unsigned)diff2p(p, p + 3);
-                if (y + 1 < H) acc += (unsigned)diff2p(p, p + 3 * (long long)W);
-                if (do_hist) {
-                    const int sc = scrib[pix0 + i];
-                    if (sc == 1 || sc == 2) key = (sc - 1) * NBINS + color_bin3(p);
-                }
+                if (x + 1 < W) acc += (unsigned)diff2w(c[u], right);
+                if (ys[u] + 1 < H) acc += (unsigned)diff2w(c[u], dn[u]);
+                if (sc[u] == 1 || sc[u] == 2) key = (sc[u] - 1) * NBINS + color_binw(c[u]);
             }
-            if (do_hist) {
+            // most warps hold no scribbled pixel: skip the bin matching there
+            if (do_hist && __ballot_sync(0xffffffffu, key >= 0)) {
                 const unsigned same = __match_any_sync(0xffffffffu, key);
                 if (key >= 0 && lane == __ffs(same) - 1) atomicAdd(&sh[key], __popc(same));
             }
@@ -174,8 +243,14 @@ __global__ void __launch_bounds__(256) k_hist_sigma_b(const uint8_t *__restrict_
     if (do_hist) {
         __syncthreads();
         int *dst = hist + (size_t)im * 2 * NBINS;
-        for (int i = threadIdx.x; i < 2 * NBINS; i += blockDim.x)
-            if (sh[i]) atomicAdd(dst + i, sh[i]);
+        const int4 *s4 = reinterpret_cast<const int4 *>(sh);
+        for (int i = threadIdx.x; i < 2 * NBINS / 4; i += blockDim.x) {
+            const int4 v = s4[i];
+            if (v.x) atomicAdd(dst + 4 * i + 0, v.x);
+            if (v.y) atomicAdd(dst + 4 * i + 1, v.y);
+            if (v.z) atomicAdd(dst + 4 * i + 2, v.z);
+            if (v.w) atomicAdd(dst + 4 * i + 3, v.w);
+        }
     }
 }
 
@@ -240,11 +315,22 @@ __device__ __forceinline__ int nlink_w(int d2, const NlinkParams &q) {
     return q.constant ? q.const_w : nlink_quant(d2, q);
 }
 
-// Fused image -> residual graph of one tile: t-link gather, n-link gather,
-// the reference's interior/border conventions, tile-major output.
+// Fused image -> residual graph of one tile: t-link gather, n-links, the
+// reference's interior/border conventions, tile-major output.
+//
+// The tile's colours and a 1-pixel halo are staged in shared memory as packed
+// words; every undirected edge between two interior pixels is weighed once
+// (the weight is symmetric in its two pixels) into a right-edge and a
+// down-edge table, and each pixel then reads its four capacities from them.
+// An edge that touches the 1-pixel image border has capacity 0, as in the
+// reference's graph (GraphCutKernels.cu:112-214).
 __global__ void __launch_bounds__(TILE_THREADS) k_build_img_b(Batch b, const uint8_t *__restrict__ rgb,
                                                                const int *__restrict__ dp_lut,
                                                                const int *__restrict__ dn_lut) {
+    constexpr int SW = TILE_W + 2, SH = TILE_H + 2;
+    __shared__ uint32_t col[SH][SW];              // pixel (x0 - 1 + j, y0 - 1 + i)
+    __shared__ int wr[TILE_H][TILE_W + 1];        // edge (x, y)-(x + 1, y), x = x0 - 1 + j, y = y0 + i
+    __shared__ int wd[TILE_H + 1][TILE_W];        // edge (x, y)-(x, y + 1), x = x0 + j, y = y0 - 1 + i
     const int t = batch_tile(b, blockIdx.x);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int im = __ldg(b.tile_img + t);
@@ -252,36 +338,98 @@ __global__ void __launch_bounds__(TILE_THREADS) k_build_img_b(Batch b, const uin
     const int lt = t - d.tile0;
     const int tx = lt % d.tiles_x, ty = lt / d.tiles_x;
     const int W = d.W, H = d.H;
+    const int x0 = tx * TILE_W, y0 = ty * TILE_H;
     const NlinkParams q = nlink_params(d.lambda, b.ist[im]);
     const int *dpl = dp_lut + (size_t)im * NBINS;
     const int *dnl = dn_lut + (size_t)im * NBINS;
     const uint8_t *base = rgb + 3 * d.pix0;
+
+    constexpr int STAGE = (SH * SW + TILE_THREADS - 1) / TILE_THREADS;
+    uint32_t cv[STAGE];
+#pragma unroll
+    for (int u = 0; u < STAGE; ++u) {  // every load first, then the stores
+        const int k = threadIdx.x + u * TILE_THREADS;
+        const int i = k / SW, j = k - i * SW;
+        const int x = x0 - 1 + j, y = y0 - 1 + i;
+        cv[u] = (k < SH * SW && x >= 0 && y >= 0 && x < W && y < H) ? pack_rgb(base + 3 * ((long long)y * W + x))
+                                                                    : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < STAGE; ++u) {
+        const int k = threadIdx.x + u * TILE_THREADS;
+        if (k < SH * SW) col[k / SW][k % SW] = cv[u];
+    }
+    __syncthreads();
+    // 2048 edges inside the tile's rows and columns, 8 per thread (right
+    // edges wr[i][1..32], then down edges wd[1..32][j]), and the 64 edges
+    // that reach into the tile from the left and from above (wr[i][0], wd[0][j])
+    {
+        constexpr int PER = 2 * TILE_W * TILE_H / TILE_THREADS;
+        int d2[PER];
+        bool use[PER];
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int k = threadIdx.x + u * TILE_THREADS;
+            if (k < TILE_W * TILE_H) {  // right edge of pixel (x0 + j, y0 + i)
+                const int i = k >> 5, j = k & 31;
+                const int x = x0 + j, y = y0 + i;
+                use[u] = x >= 1 && x <= W - 3 && y >= 1 && y <= H - 2;
+                d2[u] = diff2w(col[i + 1][j + 1], col[i + 1][j + 2]);
+            } else {  // down edge of pixel (x0 + j, y0 + i)
+                const int kk = k - TILE_W * TILE_H;
+                const int i = kk >> 5, j = kk & 31;
+                const int x = x0 + j, y = y0 + i;
+                use[u] = y >= 1 && y <= H - 3 && x >= 1 && x <= W - 2;
+                d2[u] = diff2w(col[i + 1][j + 1], col[i + 2][j + 1]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int k = threadIdx.x + u * TILE_THREADS;
+            const int w = use[u] ? nlink_w(d2[u], q) : 0;
+            if (k < TILE_W * TILE_H) wr[k >> 5][(k & 31) + 1] = w;
+            else wd[((k - TILE_W * TILE_H) >> 5) + 1][k & 31] = w;
+        }
+        if (threadIdx.x < 2 * 32) {
+            const int j = threadIdx.x & 31;
+            int w = 0;
+            if (threadIdx.x < 32) {  // edge (x0 - 1, y0 + j)-(x0, y0 + j)
+                const int x = x0 - 1, y = y0 + j;
+                if (x >= 1 && x <= W - 3 && y >= 1 && y <= H - 2) w = nlink_w(diff2w(col[j + 1][0], col[j + 1][1]), q);
+                wr[j][0] = w;
+            } else {  // edge (x0 + j, y0 - 1)-(x0 + j, y0)
+                const int x = x0 + j, y = y0 - 1;
+                if (y >= 1 && y <= H - 3 && x >= 1 && x <= W - 2) w = nlink_w(diff2w(col[0][j + 1], col[1][j + 1]), q);
+                wd[0][j] = w;
+            }
+        }
+    }
+    __syncthreads();
+
     const long long w32 = (long long)((W + 31) / 32) * 32;
     unsigned long long idp = 0, rinit = 0, pos = 0;
 #pragma unroll
     for (int k = 0; k < ROWS_PER_WARP; ++k) {
         const int r = warp + 8 * k;
-        const int x = tx * TILE_W + lane, y = ty * TILE_H + r;
+        const int x = x0 + lane, y = y0 + r;
         int4 c = make_int4(0, 0, 0, 0);
         int e = 0;
         if (x < W && y < H) {
-            const long long i = (long long)y * W + x;
-            const uint8_t *p = base + 3 * i;
-            const int bin = color_bin3(p);
+            const int bin = color_binw(col[r + 1][lane + 1]);
             const int vdp = __ldg(dpl + bin);
             if ((long long)x + (long long)y * w32 < (long long)W * H && vdp > 0) rinit += (unsigned)vdp;
             if (x > 0 && y > 0 && x < W - 1 && y < H - 1) {
-                c.x = x == 1 ? 0 : nlink_w(diff2p(p, p - 3), q);
-                c.y = x == W - 2 ? 0 : nlink_w(diff2p(p, p + 3), q);
-                c.z = y == 1 ? 0 : nlink_w(diff2p(p, p - 3 * (long long)W), q);
-                c.w = y == H - 2 ? 0 : nlink_w(diff2p(p, p + 3 * (long long)W), q);
+                c.x = wr[r][lane];      // left: edge (x - 1, y)-(x, y)
+                c.y = wr[r][lane + 1];  // right
+                c.z = wd[r][lane];      // up: edge (x, y - 1)-(x, y)
+                c.w = wd[r + 1][lane];  // down
                 e = vdp - __ldg(dnl + bin);
                 idp += (unsigned)vdp;
             }
         }
-        const size_t q = (size_t)t * TPX + r * 32 + lane;
-        b.cap[q] = c;
-        b.exc[q] = e;
+        const size_t qi = (size_t)t * TPX + r * 32 + lane;
+        b.cap[qi] = c;
+        b.exc[qi] = e;
         write_tile_masks(b, t, r, c, e);
         if (e > 0) pos += (unsigned)e;
     }

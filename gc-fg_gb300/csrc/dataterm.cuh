@@ -6,7 +6,10 @@
 namespace gcfg {
 
 constexpr int NBINS = 4096;                   // 16^3 colour bins per class
-constexpr int CHUNK_PX = 8192;                // pixels per block in per-image passes (about)
+constexpr int CHUNK_PX = 4096;                // pixels per block in per-image passes (about)
+
+// Rows of a W-wide image per block of the histogram / sigma pass.
+inline int rows_per_chunk(int W) { return W >= CHUNK_PX ? 1 : CHUNK_PX / W; }
 
 // Device buffers of the data term for a batch (per image: 2*4096 histogram
 // bins, 4096 dp and dn entries).

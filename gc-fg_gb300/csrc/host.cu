@@ -245,7 +245,7 @@ struct Engine {
             d.out0 = p;
             if (arena)
                 for (int k = 0; k < d.n_tiles; ++k) h_tile_img[t + k] = i;
-            d.rows_per_chunk = W[i] >= CHUNK_PX ? 1 : CHUNK_PX / W[i];
+            d.rows_per_chunk = rows_per_chunk(W[i]);
             h_chunk[i] = ch;
             t += d.n_tiles;
             p += (long long)W[i] * H[i];

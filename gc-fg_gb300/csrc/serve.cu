@@ -326,7 +326,7 @@ gcfg_status run_batch(Lane &L, std::vector<Req> &batch, const std::vector<Sessio
         const Session &x = snap[k];
         L.h_il[k] = x.slot;
         L.h_chunk[k] = ch;
-        const int rows = x.W >= CHUNK_PX ? 1 : CHUNK_PX / x.W;
+        const int rows = rows_per_chunk(x.W);
         ch += (x.H + rows - 1) / rows;
         for (long long i = 0; i < x.n_tiles; ++i) {
             const int t = (int)(x.tile0 + i);
