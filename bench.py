@@ -56,15 +56,20 @@ UNIT = "Mpixel/s"
 B_GR, B_PUSH, B_REACH, B_COUNT, B_BUILD, B_EXTRACT = 24, 48, 20, 8, 23, 6
 
 
-def workload(name):
+def workload(name, rank=0):
+    """Images of a workload.  Batches shard by image: under N ranks every
+    rank solves its own 256 images (seeds 1000 + 256 * rank + i), so the
+    per-GPU work is fixed and no image is shared (weak scaling)."""
+    import shard
     import synth
     if name == "batch256":
-        shapes = synth.batch_shapes(256, 1000)
+        seed0 = shard.weak_seed0(1000, 256, rank)
+        shapes = synth.batch_shapes(256, seed0)
         return dict(kind="batch", desc="256 uneven images (side log-U(64,1024), aspect U(0.5,2)), "
-                                      "scaled 256x256 ellipse generator, seeds 1000+i, lambda 50",
+                                      f"scaled 256x256 ellipse generator, seeds {seed0}+i, lambda 50",
                     images=[(3, W, H, seed, 50.0) for (W, H, seed) in shapes])
     if name == "batch64":
-        shapes = synth.batch_shapes(256, 1000)[:64]
+        shapes = synth.batch_shapes(256, shard.weak_seed0(1000, 256, rank))[:64]
         return dict(kind="batch", desc="the first 64 images of batch256 (small profiling case)",
                     images=[(3, W, H, seed, 50.0) for (W, H, seed) in shapes])
     if name == "plain1080":
@@ -393,11 +398,13 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default solver settings)")
     ap.add_argument("--no-graph", action="store_true", help="run the batch without CUDA graph replay")
+    ap.add_argument("--solver-params", default=None,
+                    help="push_rounds,max_sweeps,sweeps_per_local_relabel for the batch (skips the autotuner)")
     ap.add_argument("--serve-requests", type=int, default=1200)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_info()
-    spec = workload(args.workload)
+    spec = workload(args.workload, rank)
     if args.impl == "reference":
         return run_reference_arm(args, spec, rank, world)
 
@@ -469,7 +476,11 @@ def main():
 
     # solver settings for this batch (untimed), then CUDA graph replay
     tuning = None
-    if batched and not args.no_tune:
+    if batched and args.solver_params:
+        pr, ms, be = (int(v) for v in args.solver_params.split(","))
+        bs.set_params(pr, ms, be)
+        tuning = {"push_rounds_per_gr": pr, "max_tile_sweeps": ms, "sweeps_per_local_relabel": be, "fixed": True}
+    elif batched and not args.no_tune:
         tuning = bs.autotune(Ws, Hs, lams, d_rgb, d_scrib, reps=2)
     if batched and not args.no_graph:
         bs.set_graph(True)
@@ -522,15 +533,9 @@ def main():
                  "ms_per_step": plain_ms / psteps, "steps": psteps,
                  "flows_equal_batched": bool(np.array_equal(pflows, flows))}
 
-    def max_over_ranks(v):
-        if dist is None:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
-    total_ms = max_over_ranks(total_ms)
-    e2e_total = max_over_ranks(e2e_total)
+    import shard
+    total_ms = shard.max_over_ranks(total_ms, device="cuda")
+    e2e_total = shard.max_over_ranks(e2e_total, device="cuda")
     value = world * px_per_step * args.steps / (total_ms / 1e3) / 1e6
     e2e_value = world * px_per_step * args.steps / (e2e_total / 1e3) / 1e6
 
@@ -578,7 +583,7 @@ def main():
             "config": {"workload": args.workload, "desc": spec["desc"], "images_per_step": n_img,
                        "pixels_per_step": px_per_step, "mode": "batched" if batched else "per-image",
                        "l2": "flushed (256 MB write) before every step",
-                       "parallelism": f"replicas x{world}",
+                       "parallelism": (f"shard by image x{world}" if batched else f"replicas x{world}"),
                        "tuning": tuning, "cuda_graph": bs.graph_info() if batched else None},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 4 * px_per_step,
                     "d2h_bytes_per_step": 2 * px_per_step, "ms_per_step": e2e_total / args.steps},
