@@ -85,12 +85,15 @@ __device__ __forceinline__ int tlink_quant(int h, long long N) {
     return (int)round(tlink_raw(h, N));
 }
 
-// round(lambda * exp(-d2 / (2 s2))).  Float error: the exponent a carries
-// <= 3 ulp relative (1.8e-7 * |a|), expf <= 2 ulp, the product <= 1 ulp, so
-// the float value v is off by < v * 2e-7 * (|a| + 4).  A wrong rounding needs
-// v within that error of some k + 0.5, where |a| = ln(lambda / (k + 0.5))
-// <= ln(2 lambda): the error is then < lambda * 2e-7 * (ln(2 lambda) + 4),
-// below the margin 1e-5 * lambda + 1e-5 for every lambda up to 2^28.
+// round(lambda * exp(-d2 / (2 s2))).  Float error of v = lf * expf(a),
+// a = -d2 * inv: d2 is exact; inv = (float)(1 / (2 s2)) and the product each
+// round once, so a is off by <= 2^-23 |a| (1.2e-7 |a|); expf adds <= 2 ulp
+// (2.4e-7), lf = (float)lambda and the final product <= 0.5 ulp each
+// (1.2e-7): v is off by < v * 1.2e-7 * (|a| + 3).  A wrong rounding needs v
+// within that error of some k + 0.5, where v <= lambda and
+// |a| = ln(lambda / (k + 0.5)) <= ln(2 lambda): the error is then
+// < lambda * 1.2e-7 * (ln(2 lambda) + 3).  The margin used is about twice
+// that: lambda * 2.5e-7 * (ln(2 lambda + 1) + 4) + 1e-6, set per image.
 // (Large |a| only make v smaller: it underflows toward 0 and rounds to 0.)
 //
 // The fast path uses no conversion instructions (they share a slow pipe on
@@ -101,7 +104,8 @@ __device__ __forceinline__ int tlink_quant(int h, long long N) {
 // margin test reads |v - rint(v)| < 0.5 - margin.
 struct NlinkParams {
     float lf, inv;       // (float)lambda, (float)(1 / (2 sigma^2))
-    float half_margin;   // 0.5 - (1e-5 * lambda + 1e-5)
+    float margin;        // per image, from the error bound above
+    float half_margin;   // 0.5 - margin
     int small;           // lambda < 2^22: the magic-number rounding applies
     int constant;        // constant image: every weight is const_w = round(lambda)
     int const_w;
@@ -128,6 +132,8 @@ __global__ void k_img_params(const int *__restrict__ ilist, const ImgDesc *__res
     ist[im].inv2s2 = s2 > 0.0 ? (float)(1.0 / (2.0 * s2)) : 0.f;
     ist[im].lambda_f = (float)img[im].lambda;
     ist[im].const_w = (int)round(img[im].lambda);
+    const double lam = img[im].lambda;
+    ist[im].nl_margin = (float)(lam * 2.5e-7 * (log(2.0 * lam + 1.0) + 4.0) + 1e-6);
 }
 
 __device__ __forceinline__ NlinkParams nlink_params(double lambda, const ImgState &st) {
@@ -138,7 +144,8 @@ __device__ __forceinline__ NlinkParams nlink_params(double lambda, const ImgStat
     q.inv = st.inv2s2;
     q.constant = st.inv2s2 == 0.f;
     q.const_w = st.const_w;
-    q.half_margin = 0.5f - (1e-5f * q.lf + 1e-5f);
+    q.margin = st.nl_margin;
+    q.half_margin = 0.5f - q.margin;
     q.small = q.lf < 4194304.0f;
     return q;
 }
@@ -157,7 +164,7 @@ __device__ __forceinline__ int nlink_quant(int d2, const NlinkParams &q) {
         return nlink_exact(d2, q.lambda, q.s2);
     }
     const float fr = v - floorf(v);
-    if (fabsf(fr - 0.5f) > 1e-5f * q.lf + 1e-5f) return (int)floorf(v + 0.5f);
+    if (fabsf(fr - 0.5f) > q.margin) return (int)floorf(v + 0.5f);
     return nlink_exact(d2, q.lambda, q.s2);
 }
 

@@ -43,6 +43,8 @@ struct ImgState {
     float lambda_f;                  // (float)lambda
     int const_w;                     // round(lambda): every weight of a constant image
     int done;
+    float nl_margin;                 // n-link fast-path margin (see nlink_quant)
+    int pad_;
 };
 
 enum { L_PUSH0 = 0, L_PUSH1, L_PUSH2, L_GR0, L_GR1, L_NLISTS };

@@ -876,10 +876,10 @@ gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const i
     float best = ms_default;
     static const int c_push[] = {2, 4, 8, 16};
     static const int c_sweeps[] = {16, 32, 64, 128};
-    static const int c_bfs[] = {8, 16, 32, 64};
+    static const int c_bfs[] = {2, 4, 8, 16, 32};
     for (int pass = 0; pass < 2 && rc == GCFG_OK; ++pass) {
-        for (int which = 0; which < 4 && rc == GCFG_OK; ++which) {
-            const int nc = which == 3 ? per_sm : 4;
+        for (int which = 0; which < 5 && rc == GCFG_OK; ++which) {
+            const int nc = which == 3 ? per_sm : which == 2 ? 5 : which == 4 ? 2 : 4;
             for (int c = 0; c < nc && rc == GCFG_OK; ++c) {
                 SolveParams p = cur;
                 int bps = cur_bps;
@@ -887,6 +887,7 @@ gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const i
                 if (which == 1) p.max_sweeps = c_sweeps[c];
                 if (which == 2) p.bfs_every = c_bfs[c];
                 if (which == 3) bps = c + 1;
+                if (which == 4) p.bfs_first = c;
                 if (memcmp(&p, &cur, sizeof(p)) == 0 && bps == cur_bps) continue;
                 float ms = 0.f;
                 rc = time_cfg(p, bps, &ms);
@@ -906,13 +907,13 @@ gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const i
         out->push_rounds_per_gr = cur.push_rounds;
         out->max_tile_sweeps = cur.max_sweeps;
         out->sweeps_per_local_relabel = cur.bfs_every;
+        out->local_relabel_first = cur.bfs_first;
         out->blocks_per_sm = cur_bps;
         out->ms_default = ms_default;
         out->ms_best = best;
         out->configs_tried = tried;
         out->tile_w = TILE_W;
         out->tile_h = TILE_H;
-        out->pad = 0;
     }
     return GCFG_OK;
 }

@@ -68,10 +68,10 @@ class Tuning(C.Structure):
     _fields_ = [("push_rounds_per_gr", C.c_int32), ("max_tile_sweeps", C.c_int32),
                 ("sweeps_per_local_relabel", C.c_int32), ("blocks_per_sm", C.c_int32),
                 ("ms_default", C.c_float), ("ms_best", C.c_float), ("configs_tried", C.c_int32),
-                ("tile_w", C.c_int32), ("tile_h", C.c_int32), ("pad", C.c_int32)]
+                ("tile_w", C.c_int32), ("tile_h", C.c_int32), ("local_relabel_first", C.c_int32)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class ProfEntry(C.Structure):

@@ -102,7 +102,7 @@ gcfg_status gcfg_set_stream(gcfg_graph *g, void *stream);
  * per tile visit (solver schedule; does not change the result). */
 gcfg_status gcfg_set_schedule(gcfg_graph *g, int push_rounds_per_gr, int max_tile_sweeps);
 
-/* ---------------- data term + n-links (spec steps a, b) ---------------- */
+/* ---------------- data term + n-links ---------------- */
 
 /* Colour-histogram t-links for one image: 16^3 bins of (r>>4, g>>4, b>>4)
  * over fg (scrib == 1) and bg (scrib == 2) pixels, +1 Laplace smoothing;
@@ -125,7 +125,7 @@ gcfg_status gcfg_nlinks(const uint8_t *d_rgb, int w, int h, double lambda, int32
  * and the two t-link arrays; DataTerm.cpp:28-165) as a handle.  The colour
  * model is the 16^3 histogram pair of gcfg_tlinks, rebuilt from the current
  * image and selection map by gcfg_dt_compute: selection class 1 = foreground
- * (the reference's only class), 2 = background (the spec scribbles).
+ * (the reference's only class), 2 = background (scribbles of the second class).
  * The t-links are dp = round(10 * -log p_bg) (source, "positive") and
  * dn = round(10 * -log p_fg) (sink, "negative"), W*H int32 on the device,
  * owned by the handle, ready for gcfg_init.  All host copies are blocking. */
@@ -244,7 +244,7 @@ typedef struct {
     float ms_default, ms_best;        /* device time of one run before / after tuning */
     int32_t configs_tried;
     int32_t tile_w, tile_h;           /* tile shape (fixed: the width of the bit-plane BFS) */
-    int32_t pad;
+    int32_t local_relabel_first;      /* 1: exact local relabel at the start of every tile visit */
 } gcfg_tuning;
 
 /* Time the batch (device-resident, as gcfg_batch_run) under candidate solver

@@ -87,7 +87,8 @@ def test_autotune_keeps_results():
     t = bs.autotune(Ws, Hs, lams, d_rgb, d_scrib, reps=2)
     assert t["configs_tried"] >= 10
     assert t["push_rounds_per_gr"] in (2, 4, 8, 16) and t["max_tile_sweeps"] in (16, 32, 64, 128)
-    assert t["sweeps_per_local_relabel"] in (8, 16, 32, 64) and 1 <= t["blocks_per_sm"] <= 8
+    assert t["sweeps_per_local_relabel"] in (2, 4, 8, 16, 32, 64) and 1 <= t["blocks_per_sm"] <= 8
+    assert t["local_relabel_first"] in (0, 1)
     assert t["ms_best"] <= t["ms_default"] and (t["tile_w"], t["tile_h"]) == (32, 32)
     got = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
     for a, b in zip(ref, got):
