@@ -1,7 +1,9 @@
-"""Build libgcfg.so (the CUDA library) in-tree with nvcc for sm_103a.
+"""Build libgcfg.so (the CUDA library) in-tree with nvcc for sm_103a, and
+the command-line tools of cli/ into bin/.
 
 The translation units compile in parallel and link into one shared library
-next to this file; no cmake, one -gencode.
+next to this file; no cmake, one -gencode.  The tools (solve_mrf,
+segment_dat, multiply_mrf) are host C++ linked against the library.
 """
 from __future__ import annotations
 
@@ -66,5 +68,39 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+CLI = os.path.join(HERE, "cli")
+BIN = os.path.join(HERE, "bin")
+INCLUDE = os.path.join(HERE, "..", "include")
+TOOLS = {"solve_mrf": True, "segment_dat": True, "multiply_mrf": False}  # name -> links libgcfg
+
+
+def build_tools(force: bool = False, verbose: bool = False) -> list:
+    """Compile cli/<tool>.cpp into bin/<tool> (after the library)."""
+    build(force=False, verbose=verbose)
+    os.makedirs(BIN, exist_ok=True)
+    hdrs = [os.path.join(CLI, f) for f in os.listdir(CLI) if f.endswith(".hpp")]
+    hdrs += [os.path.join(INCLUDE, f) for f in ("gcfg.h", "GraphCut.h", "GraphCut.cu", "DataTerm.h")]
+
+    def one(name):
+        src = os.path.join(CLI, name + ".cpp")
+        exe = os.path.join(BIN, name)
+        deps = [src, *hdrs] + ([LIB] if TOOLS[name] else [])
+        if not force and os.path.exists(exe) and all(os.path.getmtime(d) <= os.path.getmtime(exe) for d in deps):
+            return exe
+        cmd = [NVCC, "-std=c++17", "-O2", "-I", INCLUDE, "-I", CLI, src, "-o", exe]
+        if TOOLS[name]:
+            cmd += ["-L", HERE, "-lgcfg", "-Xlinker", "-rpath=$ORIGIN/.."]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError(f"tool build failed for {name}:\n{r.stderr}")
+        return exe
+
+    with ThreadPoolExecutor(max_workers=len(TOOLS)) as ex:
+        return list(ex.map(one, sorted(TOOLS)))
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True))
+    print(build_tools(force="--force" in sys.argv, verbose=True))

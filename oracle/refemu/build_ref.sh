@@ -2,9 +2,15 @@
 # Builds the reference's own solver (GraphCut.cu + GraphCutKernels.cu, read
 # from the reference checkout, unmodified except that each `K<<<g,b>>>(`
 # launch is rewritten on the fly to `emu_launch(g,b, K, `) for the CPU
-# thread emulator) together with ref_harness.cpp into oracle/_ref/.
+# thread emulator) together with ref_harness.cpp into oracle/_ref/, and the
+# reference's applications that feed it: solveMRF.cu and Application.cu
+# (compiled from stdin in app_include/, whose GraphCut.cu declares the host
+# API that graphcut_ref.o defines) and multiplyMRF.cpp (plain C++; once as it
+# is, the 3600x3600 mode, and once with its DO_RIHANNA switch turned to 0 on
+# the fly, the general tiling mode).
 # Test infrastructure only: it produces the golden outputs that pin the
-# oracle.  Nothing from the reference is written anywhere but oracle/_ref/.
+# oracle and the tools.  Nothing from the reference is written anywhere but
+# oracle/_ref/.
 set -e
 REF=${GCFG_REFERENCE_DIR:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -20,4 +26,11 @@ sed -E 's/([A-Za-z_][A-Za-z0-9_]*)<<<([^>]*)>>>\(/emu_launch(\2, \1, /' "$REF/Gr
 g++ $FLAGS -I "$HERE" -c "$HERE/cuda_emu.cpp" -o "$OUT/cuda_emu.o"
 g++ $FLAGS -I "$HERE" -I "$REF" -include cuda_emu.h -c "$HERE/ref_harness.cpp" -o "$OUT/ref_harness.o"
 g++ -o "$OUT/ref_harness" "$OUT/graphcut_ref.o" "$OUT/cuda_emu.o" "$OUT/ref_harness.o"
+for app in solveMRF Application; do
+  (cd "$HERE/app_include" && g++ $FLAGS -x c++ -I "$HERE" -I "$REF" -include cuda_emu.h -c - \
+      -o "$OUT/${app}_ref.o" < "$REF/$app.cu")
+  g++ -o "$OUT/$app" "$OUT/${app}_ref.o" "$OUT/graphcut_ref.o" "$OUT/cuda_emu.o"
+done
+g++ -O2 -w -o "$OUT/multiplyMRF" "$REF/multiplyMRF.cpp"
+sed 's/^#define DO_RIHANNA 1/#define DO_RIHANNA 0/' "$REF/multiplyMRF.cpp" | g++ -O2 -w -x c++ - -o "$OUT/multiplyMRF_tile"
 echo "$OUT/ref_harness"
