@@ -399,7 +399,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default solver settings)")
     ap.add_argument("--no-graph", action="store_true", help="run the batch without CUDA graph replay")
     ap.add_argument("--solver-params", default=None,
-                    help="push_rounds,max_sweeps,sweeps_per_local_relabel for the batch (skips the autotuner)")
+                    help="push_rounds,max_sweeps,sweeps_per_local_relabel[,blocks_per_sm[,relabel_first"
+                         "[,push_only]]] for the batch (skips the autotuner)")
     ap.add_argument("--serve-requests", type=int, default=1200)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -477,9 +478,11 @@ def main():
     # solver settings for this batch (untimed), then CUDA graph replay
     tuning = None
     if batched and args.solver_params:
-        pr, ms, be = (int(v) for v in args.solver_params.split(","))
-        bs.set_params(pr, ms, be)
-        tuning = {"push_rounds_per_gr": pr, "max_tile_sweeps": ms, "sweeps_per_local_relabel": be, "fixed": True}
+        keys = ("push_rounds_per_gr", "max_tile_sweeps", "sweeps_per_local_relabel", "blocks_per_sm",
+                "local_relabel_first", "push_only")
+        tuning = dict(zip(keys, (int(v) for v in args.solver_params.split(","))))
+        bs.set_solver(**tuning)
+        tuning["fixed"] = True
     elif batched and not args.no_tune:
         tuning = bs.autotune(Ws, Hs, lams, d_rgb, d_scrib, reps=2)
     if batched and not args.no_graph:

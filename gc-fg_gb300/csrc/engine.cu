@@ -331,46 +331,48 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
     if (warp == 2) s.h[lane + 1][0] = g.nb[0] >= 0 ? __ldcg(b.h + (size_t)g.nb[0] * TPX + lane * 32 + 31) : INF_H;
     if (warp == 3) s.h[lane + 1][TILE_W + 1] = g.nb[1] >= 0 ? __ldcg(b.h + (size_t)g.nb[1] * TPX + lane * 32) : INF_H;
     if (warp < 4) s.halo_in[warp][lane] = 0;
-    if (threadIdx.x == 0) s.flag = 0;  // "pushed in sweep sw" marker: sw + 1
     __syncthreads();
     c1 = clock64();
     const long long c_load = c1 - c0;
 
     int any = 1;
     int sweeps = 0, bfs = 0;
+    int since_bfs = 0;
+    // Exact local relabel: tile BFS against the frozen halo (warp 0), the
+    // residual masks of the current capacities first.
+    auto local_relabel = [&]() {
+        ++bfs;
+        since_bfs = 0;
+#pragma unroll
+        for (int k = 0; k < ROWS_PER_WARP; ++k) {
+            const int r = warp + 8 * k;
+            const int4 c = s.c[r][lane];
+            const int e = s.e[r][lane];
+            const unsigned ml = __ballot_sync(FULL, c.x > 0);
+            const unsigned mr = __ballot_sync(FULL, c.y > 0);
+            const unsigned mu = __ballot_sync(FULL, c.z > 0);
+            const unsigned md = __ballot_sync(FULL, c.w > 0);
+            const unsigned mn = __ballot_sync(FULL, e < 0);
+            if (lane == 0) {
+                s.m[0][r] = ml; s.m[1][r] = mr; s.m[2][r] = mu; s.m[3][r] = md; s.m[4][r] = mn;
+            }
+        }
+        __syncthreads();
+        const long long cb0 = clock64();
+        if (warp == 0)
+            tile_bfs(s.m[0][lane], s.m[1][lane], s.m[2][lane], s.m[3][lane], s.m[4][lane],
+                     s.h[lane + 1][0], s.h[lane + 1][TILE_W + 1], s.h[0][lane + 1],
+                     s.h[TILE_H + 1][lane + 1], &s.h[1][1], TILE_W + 2);
+        __syncthreads();
+        cb += clock64() - cb0;
+    };
     // The exact local relabel (tile BFS) runs at the first sweep when
     // prm.bfs_first is set, after a sweep that pushed nothing while active
     // pixels remain, and at least every prm.bfs_every sweeps.
     bool need_bfs = prm.bfs_first != 0;
-    int since_bfs = 0;
     for (int sw = 0; sw < prm.max_sweeps; ++sw) {
         ++sweeps;
-        if (need_bfs || since_bfs >= prm.bfs_every) {
-            ++bfs;
-            since_bfs = 0;
-#pragma unroll
-            for (int k = 0; k < ROWS_PER_WARP; ++k) {
-                const int r = warp + 8 * k;
-                const int4 c = s.c[r][lane];
-                const int e = s.e[r][lane];
-                const unsigned ml = __ballot_sync(FULL, c.x > 0);
-                const unsigned mr = __ballot_sync(FULL, c.y > 0);
-                const unsigned mu = __ballot_sync(FULL, c.z > 0);
-                const unsigned md = __ballot_sync(FULL, c.w > 0);
-                const unsigned mn = __ballot_sync(FULL, e < 0);
-                if (lane == 0) {
-                    s.m[0][r] = ml; s.m[1][r] = mr; s.m[2][r] = mu; s.m[3][r] = md; s.m[4][r] = mn;
-                }
-            }
-            __syncthreads();
-            const long long cb0 = clock64();
-            if (warp == 0)
-                tile_bfs(s.m[0][lane], s.m[1][lane], s.m[2][lane], s.m[3][lane], s.m[4][lane],
-                         s.h[lane + 1][0], s.h[lane + 1][TILE_W + 1], s.h[0][lane + 1],
-                         s.h[TILE_H + 1][lane + 1], &s.h[1][1], TILE_W + 2);
-            __syncthreads();
-            cb += clock64() - cb0;
-        }
+        if (need_bfs || since_bfs >= prm.bfs_every) local_relabel();
         ++since_bfs;
         // ---- push phase: heights fixed.  All loads first, flows in
         // registers, then fire-and-forget shared atomics. ----
@@ -441,8 +443,28 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
                 }
             }
         }
-        if (pushed) s.flag = sw + 1;  // benign race: every writer stores the same value
-        __syncthreads();
+        // block-uniform "anything pushed in this sweep" (every warp takes the
+        // same branch below; a shared flag could be overwritten by a warp
+        // already in the next sweep)
+        const int pushed_any = __syncthreads_or(pushed);
+        if (prm.push_only) {
+            // heights change only here: a sweep that moved nothing gets an
+            // exact local relabel, after which the visit ends if no pixel
+            // with excess can reach the sink or the halo
+            if (!pushed_any) {
+                local_relabel();
+                int act = 0;
+#pragma unroll
+                for (int k = 0; k < ROWS_PER_WARP; ++k) {
+                    const int r = warp + 8 * k;
+                    act |= s.e[r][lane] > 0 && s.h[r + 1][lane + 1] < INF_H;
+                }
+                any = __syncthreads_or(act);
+                if (!any) break;
+            }
+            need_bfs = false;
+            continue;
+        }
         // ---- relabel phase: capacities and excess fixed ----
         int act = 0;
 #pragma unroll
@@ -473,7 +495,7 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
         }
         any = __syncthreads_or(act);
         if (!any) break;
-        need_bfs = s.flag != sw + 1;  // stalled: nothing was pushed in this sweep
+        need_bfs = !pushed_any;  // stalled: nothing was pushed in this sweep
     }
     const long long c2 = clock64();
     cs = c2 - c1 - cb;

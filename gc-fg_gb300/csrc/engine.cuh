@@ -105,6 +105,7 @@ struct SolveParams {
     int bfs_every;     // exact local relabel at least every this many sweeps
     int bfs_first;     // exact local relabel at the start of every tile visit
     int max_rounds;    // cap on BFS rounds of one global relabel / reach pass
+    int push_only;     // 1: sweeps only push; heights change only by exact local relabels
 };
 
 __host__ __device__ __forceinline__ int batch_ntiles(const Batch &b) { return b.tlist ? b.n_tlist : b.n_tiles; }

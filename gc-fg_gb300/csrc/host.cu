@@ -41,7 +41,7 @@ static gcfg_status grow_host(T *&p, size_t &cap, size_t need) {
 
 struct Engine {
     cudaStream_t st = nullptr;
-    SolveParams prm{64, 4, 64, 16, 0, 1 << 20};
+    SolveParams prm{64, 4, 64, 16, 0, 1 << 20, 0};
 
     int n_img = 0, n_tiles = 0;
     long long n_px = 0, total_chunks = 0;
@@ -815,6 +815,23 @@ gcfg_status gcfg_batch_set_params(gcfg_batch *b, int push_rounds_per_gr, int max
     return GCFG_OK;
 }
 
+gcfg_status gcfg_batch_set_solver(gcfg_batch *b, const gcfg_tuning *t) {
+    if (!b || !t || t->push_rounds_per_gr < 1 || t->max_tile_sweeps < 1 || t->sweeps_per_local_relabel < 1 ||
+        t->blocks_per_sm < 0 || (t->local_relabel_first != 0 && t->local_relabel_first != 1) ||
+        (t->push_only != 0 && t->push_only != 1))
+        return GCFG_ERR_INVALID;
+    int dev = 0, sms = 1;
+    GCFG_CK(cudaGetDevice(&dev));
+    GCFG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    b->e.prm.push_rounds = t->push_rounds_per_gr;
+    b->e.prm.max_sweeps = t->max_tile_sweeps;
+    b->e.prm.bfs_every = t->sweeps_per_local_relabel;
+    b->e.prm.bfs_first = t->local_relabel_first;
+    b->e.prm.push_only = t->push_only;
+    b->e.max_grid = t->blocks_per_sm * sms;  // 0: as many as fit
+    return GCFG_OK;
+}
+
 gcfg_status gcfg_batch_set_graph(gcfg_batch *b, int enable) {
     if (!b) return GCFG_ERR_INVALID;
     b->e.graph_on = enable != 0;
@@ -878,8 +895,8 @@ gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const i
     static const int c_sweeps[] = {16, 32, 64, 128};
     static const int c_bfs[] = {2, 4, 8, 16, 32};
     for (int pass = 0; pass < 2 && rc == GCFG_OK; ++pass) {
-        for (int which = 0; which < 5 && rc == GCFG_OK; ++which) {
-            const int nc = which == 3 ? per_sm : which == 2 ? 5 : which == 4 ? 2 : 4;
+        for (int which = 0; which < 6 && rc == GCFG_OK; ++which) {
+            const int nc = which == 3 ? per_sm : which == 2 ? 5 : which >= 4 ? 2 : 4;
             for (int c = 0; c < nc && rc == GCFG_OK; ++c) {
                 SolveParams p = cur;
                 int bps = cur_bps;
@@ -888,6 +905,7 @@ gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const i
                 if (which == 2) p.bfs_every = c_bfs[c];
                 if (which == 3) bps = c + 1;
                 if (which == 4) p.bfs_first = c;
+                if (which == 5) p.push_only = c;
                 if (memcmp(&p, &cur, sizeof(p)) == 0 && bps == cur_bps) continue;
                 float ms = 0.f;
                 rc = time_cfg(p, bps, &ms);
@@ -908,6 +926,7 @@ gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const i
         out->max_tile_sweeps = cur.max_sweeps;
         out->sweeps_per_local_relabel = cur.bfs_every;
         out->local_relabel_first = cur.bfs_first;
+        out->push_only = cur.push_only;
         out->blocks_per_sm = cur_bps;
         out->ms_default = ms_default;
         out->ms_best = best;

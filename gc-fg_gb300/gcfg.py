@@ -38,6 +38,7 @@ EXPORTS = [
     "gcfg_profile_enable", "gcfg_profile_read", "gcfg_batch_create", "gcfg_batch_set_stream",
     "gcfg_batch_set_params", "gcfg_batch_run", "gcfg_batch_run_host", "gcfg_batch_destroy",
     "gcfg_solve_noalloc", "gcfg_batch_set_graph", "gcfg_batch_graph_info", "gcfg_batch_autotune",
+    "gcfg_batch_set_solver",
 ]
 
 PROF_KINDS = ["hist", "tlut", "sigma", "wlut", "build", "solve", "extract", "other"]
@@ -68,10 +69,11 @@ class Tuning(C.Structure):
     _fields_ = [("push_rounds_per_gr", C.c_int32), ("max_tile_sweeps", C.c_int32),
                 ("sweeps_per_local_relabel", C.c_int32), ("blocks_per_sm", C.c_int32),
                 ("ms_default", C.c_float), ("ms_best", C.c_float), ("configs_tried", C.c_int32),
-                ("tile_w", C.c_int32), ("tile_h", C.c_int32), ("local_relabel_first", C.c_int32)]
+                ("tile_w", C.c_int32), ("tile_h", C.c_int32), ("local_relabel_first", C.c_int32),
+                ("push_only", C.c_int32), ("pad", C.c_int32)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
 
 
 class ProfEntry(C.Structure):
@@ -122,6 +124,7 @@ def load(path: str = LIB_PATH):
         "gcfg_batch_graph_info": (S, [P, C.POINTER(I), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                       C.POINTER(C.c_int64)]),
         "gcfg_batch_autotune": (S, [P, I, P, P, P, P, P, I, C.POINTER(Tuning)]),
+        "gcfg_batch_set_solver": (S, [P, C.POINTER(Tuning)]),
         "gcfg_solve_noalloc": (S, [I, I, P, P, C.c_int32, P, P, P, P, P, C.POINTER(C.c_int64), P]),
         "gcfg_profile_enable": (S, [I]),
         "gcfg_profile_read": (S, [C.POINTER(ProfEntry), I, C.POINTER(I)]),
@@ -351,6 +354,14 @@ class BatchSolver:
                "gcfg_batch_graph_info")
         return {"active": bool(a.value), "captures": c.value, "replays": r.value, "kernels_per_replay": k.value}
 
+    def set_solver(self, push_rounds_per_gr=4, max_tile_sweeps=64, sweeps_per_local_relabel=16,
+                   blocks_per_sm=0, local_relabel_first=0, push_only=0, **_ignored):
+        """Solver settings (keys as autotune() returns them)."""
+        t = Tuning(push_rounds_per_gr=int(push_rounds_per_gr), max_tile_sweeps=int(max_tile_sweeps),
+                   sweeps_per_local_relabel=int(sweeps_per_local_relabel), blocks_per_sm=int(blocks_per_sm),
+                   local_relabel_first=int(local_relabel_first), push_only=int(push_only))
+        _check(load().gcfg_batch_set_solver(self.handle, C.byref(t)), "gcfg_batch_set_solver")
+
     def autotune(self, widths, heights, lambdas, d_rgb, d_scrib, reps=3) -> dict:
         """Pick the solver settings for this batch (gcfg_batch_autotune)."""
         w, h, lam = self._arrays(widths, heights, lambdas)
@@ -543,7 +554,10 @@ EXPORTS += ["gcfg_dt_create", "gcfg_dt_destroy", "gcfg_dt_set_stream", "gcfg_dt_
             "gcfg_dt_set_image_device", "gcfg_dt_set_selection", "gcfg_dt_set_scribbles_device",
             "gcfg_dt_reset", "gcfg_dt_select_on_map", "gcfg_dt_set_sigma", "gcfg_dt_compute",
             "gcfg_dt_pos", "gcfg_dt_neg", "gcfg_dt_image", "gcfg_dt_selection",
-            "gcfg_dt_draw_selection", "gcfg_dt_nlinks"]
+            "gcfg_dt_draw_selection", "gcfg_dt_nlinks", "gcfg_dt_set_model", "gcfg_dt_kde_table"]
+
+GCFG_DT_HISTOGRAM = 0
+GCFG_DT_KDE = 1
 
 
 def _dt_lib():
@@ -568,6 +582,8 @@ def _dt_lib():
             "gcfg_dt_selection": (P, [P]),
             "gcfg_dt_draw_selection": (C.c_int, [P, P, P]),
             "gcfg_dt_nlinks": (C.c_int, [P, C.c_double, P, P, P, P]),
+            "gcfg_dt_set_model": (C.c_int, [P, C.c_int]),
+            "gcfg_dt_kde_table": (C.c_int, [P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -635,6 +651,16 @@ class DataTermState:
 
     def set_sigma(self, sigma):
         _check(self._lib().gcfg_dt_set_sigma(self.handle, int(sigma)), "gcfg_dt_set_sigma")
+
+    def set_model(self, model):
+        """'histogram' (default) or 'kde' (the reference's kernel density)."""
+        m = {"histogram": GCFG_DT_HISTOGRAM, "kde": GCFG_DT_KDE}.get(model, model)
+        _check(self._lib().gcfg_dt_set_model(self.handle, int(m)), "gcfg_dt_set_model")
+
+    def kde_table(self):
+        g = np.empty(101, np.float32)
+        _check(self._lib().gcfg_dt_kde_table(self.handle, _ptr(g)), "gcfg_dt_kde_table")
+        return g
 
     def compute(self):
         _check(self._lib().gcfg_dt_compute(self.handle), "gcfg_dt_compute")
@@ -730,6 +756,11 @@ class DataTerm:
     @classmethod
     def setSigmaGaussian(cls, sigma):
         cls._s().set_sigma(sigma)
+
+    @classmethod
+    def useKernelDensity(cls, on=True):
+        """The reference's own colour model instead of the histogram pair."""
+        cls._s().set_model("kde" if on else "histogram")
 
     @classmethod
     def getPos(cls) -> DeviceArray:

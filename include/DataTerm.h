@@ -8,9 +8,10 @@
  * (host int map: 0 none, 1 foreground, 2 background); getDataTermsMixture()
  * computes the device t-link arrays that getPos()/getNeg() return and that
  * go straight into GC_Init.  The colour model is the 16^3 histogram pair of
- * the selected pixels of the current image (the reference splats a Gaussian
- * kernel density instead); setSigmaGaussian() is accepted and has no effect
- * on it.  selectBackgroundOnMap() (no counterpart) marks a background square.
+ * the selected pixels of the current image; useKernelDensity() switches to
+ * the reference's own model (a Gaussian kernel density, whose width
+ * setSigmaGaussian() sets; it has no effect on the histogram model).
+ * selectBackgroundOnMap() (no counterpart) marks a background square.
  * Errors: a message on stderr and exit(), like the reference's cutil checks.
  * Requires C++17 (inline variables). */
 #ifndef GCFG_DATATERM_H_
@@ -100,6 +101,14 @@ inline void getDataTermsMixture() {
 
 inline void setSigmaGaussian(int sigma) {
     detail::check(gcfg_dt_set_sigma(detail::live("setSigmaGaussian"), sigma), "setSigmaGaussian");
+}
+
+/* The reference's own colour model (a kernel density that selectOnMap
+ * splats into, DataTerm.cpp:97-137) instead of the histogram pair; call after
+ * init_data_term (no counterpart: the reference has only this model). */
+inline void useKernelDensity(bool on = true) {
+    detail::check(gcfg_dt_set_model(detail::live("useKernelDensity"), on ? GCFG_DT_KDE : GCFG_DT_HISTOGRAM),
+                  "useKernelDensity");
 }
 
 }  // namespace DataTerm

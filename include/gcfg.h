@@ -134,6 +134,12 @@ typedef struct gcfg_dataterm gcfg_dataterm;
 /* Side of the square that gcfg_dt_select_on_map marks (DataTerm.cpp:113). */
 #define GCFG_DT_SELECT_SIZE 5
 
+/* Colour models of a DataTerm handle. */
+enum {
+    GCFG_DT_HISTOGRAM = 0, /* default: 16^3 histogram pair of the selected pixels (see above) */
+    GCFG_DT_KDE = 1        /* the reference's kernel density (DataTerm.cpp:97-137) */
+};
+
 /* init_data_term (DataTerm.cpp:28): allocate for a w x h image; empty selection. */
 gcfg_status gcfg_dt_create(int w, int h, gcfg_dataterm **out);
 /* free_data_term (DataTerm.cpp:67); unlike the reference the t-link arrays
@@ -171,6 +177,22 @@ uint8_t *gcfg_dt_selection(gcfg_dataterm *dt);
  * receives it with class-1 pixels set to (0, 0, 255) as in the reference and
  * class-2 pixels set to (255, 0, 0). */
 gcfg_status gcfg_dt_draw_selection(gcfg_dataterm *dt, const uint8_t *h_in, uint8_t *h_out);
+/* Choose the colour model.  GCFG_DT_KDE is the reference's own data term: a
+ * kernel density over the 256^3 colour cube (64 MB, allocated on first use)
+ * to which every class-1 gcfg_dt_select_on_map adds, for each pixel of its
+ * 5x5 square, gauss[floor(|c - colour|)] at every cube point c within
+ * distance 101 (DataTermKernels.cu:116-150), where gauss is the 101-entry
+ * table of gcfg_dt_set_sigma (default sigma 5, DataTerm.cpp:6,63); then
+ * gcfg_dt_compute gives pos = (int)(300000 p), neg = (int)(300000 (1 - p))
+ * with p the density at the pixel's colour (DataTermKernels.cu:61-83).  In
+ * this model gcfg_dt_set_selection only sets the map and gcfg_dt_reset also
+ * clears the density, as in the reference.  Unlike the reference, the square
+ * is clipped to the image and every pixel gets t-links (the reference skips
+ * the pixels outside whole 16x16 blocks). */
+gcfg_status gcfg_dt_set_model(gcfg_dataterm *dt, int model);
+/* The kernel density's 101-entry table (host float[101]); GCFG_ERR_STATE
+ * before the model was first chosen. */
+gcfg_status gcfg_dt_kde_table(gcfg_dataterm *dt, float *h_gauss);
 /* gcfg_nlinks of the handle's current image (no counterpart). */
 gcfg_status gcfg_dt_nlinks(gcfg_dataterm *dt, double lambda, int32_t *d_up, int32_t *d_down,
                            int32_t *d_left, int32_t *d_right);
@@ -245,10 +267,18 @@ typedef struct {
     int32_t configs_tried;
     int32_t tile_w, tile_h;           /* tile shape (fixed: the width of the bit-plane BFS) */
     int32_t local_relabel_first;      /* 1: exact local relabel at the start of every tile visit */
+    int32_t push_only;                /* 1: sweeps only push; heights change by exact local relabels */
+    int32_t pad;
 } gcfg_tuning;
 
+/* Use these solver settings for the following runs (for example the record
+ * an earlier gcfg_batch_autotune returned; blocks_per_sm 0 = as many as fit;
+ * ms_*, configs_tried and the tile shape are ignored).  Results do not depend
+ * on them.  No counterpart in the reference. */
+gcfg_status gcfg_batch_set_solver(gcfg_batch *b, const gcfg_tuning *t);
+
 /* Time the batch (device-resident, as gcfg_batch_run) under candidate solver
- * settings by coordinate search, keep the fastest, and use it for the
+ * settings (the fields above) by coordinate search, keep the fastest, and use it for the
  * following runs of this handle.  Each setting is timed as the fastest of
  * `reps` runs; every run must reproduce the flows of the first (else
  * GCFG_ERR_NOT_CONVERGED).  No counterpart in the reference. */

@@ -684,3 +684,54 @@ int or_segment_batch(int n_img, const int *Ws, const int *Hs, const int64_t *off
     return c.err;
 }
 
+
+/* ---------------------------------------------------------------------------
+ * Kernel-density data term of the reference (DataTerm.cpp:97-137,
+ * DataTermKernels.cu:19-31, 61-83, 116-161).
+ * ------------------------------------------------------------------------- */
+
+void or_kde_gauss(int sigma, float *gauss) {
+    /* K_InitGaussian (DataTermKernels.cu:19-31): 1 / (sigma * 2.507) *
+     * expf(-0.5 * (x / sigma)^2) with its types: x / sigma in float, the
+     * exponent in double rounded to float for expf, the product in double. */
+    for (int x = 0; x < 101; ++x) {
+        const float xs = (float)x / (float)sigma;
+        const double a = -0.5 * (double)xs * (double)xs;
+        gauss[x] = (float)(1.0 / ((double)(float)sigma * 2.507) * (double)expf((float)a));
+    }
+}
+
+int or_kde_select(const uint8_t *img, int W, int H, int x, int y, uint8_t *sel) {
+    int k = 0;
+    for (int i = 0; i < 5; ++i)
+        for (int j = 0; j < 5; ++j) {
+            const int px = x + i, py = y + j;
+            if (px < 0 || py < 0 || px >= W || py >= H) continue;
+            const uint8_t *p = img + 3 * ((size_t)py * W + px);
+            sel[3 * k] = p[0];
+            sel[3 * k + 1] = p[1];
+            sel[3 * k + 2] = p[2];
+            ++k;
+        }
+    return k;
+}
+
+void or_kde_terms(const float *gauss, const uint8_t *sel, int n_sel, const uint8_t *img, int n,
+                  int32_t *pos, int32_t *neg) {
+    for (int i = 0; i < n; ++i) {
+        const uint8_t *c = img + 3 * (size_t)i;
+        float p = 0.0f;
+        for (int k = 0; k < n_sel; ++k) {
+            const int d0 = (int)c[0] - sel[3 * k], d1 = (int)c[1] - sel[3 * k + 1], d2 = (int)c[2] - sel[3 * k + 2];
+            const int d = d0 * d0 + d1 * d1 + d2 * d2;
+            if (d < 101 * 101) {
+                int r = (int)sqrt((double)d); /* floor(sqrt(d)), exact for d < 2^26 */
+                while (r * r > d) --r;
+                while ((r + 1) * (r + 1) <= d) ++r;
+                p = p + gauss[r];
+            }
+        }
+        pos[i] = (int32_t)(300000.0 * (double)p);
+        neg[i] = (int32_t)(300000.0 * (double)(1.0f - p));
+    }
+}

@@ -95,6 +95,25 @@ int or_segment(const uint8_t *rgb, const uint8_t *scrib, int W, int H,
                int32_t *up, int32_t *down, int32_t *left, int32_t *right,
                uint8_t *smin, uint8_t *smax, int64_t *flow);
 
+/* The reference's kernel-density data term (DataTerm.cpp:97-137,
+ * DataTermKernels.cu:19-31, 61-83, 116-161).  The class density at colour c
+ * is, summed in float in selection order (one selectOnMap launch after the
+ * other, each adding one term per colour-cube point),
+ *   p(c) = sum_k gauss[floor(sqrt(|c - s_k|^2))]  over |c - s_k|^2 < 101^2,
+ * where s_k are the colours of the selected pixels; t-links are
+ *   pos = (int)(300000.0 * p),  neg = (int)(300000.0 * (1.0f - p)).
+ * gauss: the 101-entry table (input); sel: n_sel colours (3 bytes each, in
+ * order); img: n pixels (3 bytes each); pos/neg: n int32 outputs. */
+void or_kde_terms(const float *gauss, const uint8_t *sel, int n_sel, const uint8_t *img, int n,
+                  int32_t *pos, int32_t *neg);
+/* The reference's Gaussian table for a sigma (K_InitGaussian), in double
+ * precision rounded to float (the reference's expf may differ by an ulp). */
+void or_kde_gauss(int sigma, float *gauss);
+/* The colours selectOnMap(x, y) adds, in the reference's order (x offset
+ * outer, y offset inner, DataTerm.cpp:111-123), clipped to the image.
+ * Returns the number written (<= 25) to sel (3 bytes each). */
+int or_kde_select(const uint8_t *img, int W, int H, int x, int y, uint8_t *sel);
+
 /* Batch of independent solves over `nthreads` host threads (one image per
  * task), for the CPU baseline. Arrays are concatenated; offs[i] is the pixel
  * offset of image i.  Returns 0 on success. */

@@ -74,6 +74,9 @@ def lib():
         _lib.or_segment.argtypes = [P, P, C.c_int, C.c_int, C.c_double, C.c_int, P, P, P, P, P, P,
                                     P, P, C.POINTER(C.c_int64)]
         _lib.or_segment_batch.argtypes = [C.c_int, P, P, P, P, P, P, C.c_int, C.c_int, P, P, P]
+        _lib.or_kde_gauss.argtypes = [C.c_int, P]
+        _lib.or_kde_select.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, P]
+        _lib.or_kde_terms.argtypes = [P, P, C.c_int, P, C.c_int, P, P]
     return _lib
 
 
@@ -219,3 +222,30 @@ def segment_batch(images, lambdas, nthreads: int, solver="bk"):
 
 def fnv1a(a) -> int:
     return synth.fnv1a(a)
+
+
+def kde_gauss(sigma: int):
+    """The reference's 101-entry Gaussian table (double evaluation)."""
+    g = np.empty(101, np.float32)
+    lib().or_kde_gauss(int(sigma), _p(g))
+    return g
+
+
+def kde_select(rgb, x: int, y: int):
+    """Colours a selectOnMap(x, y) adds, in the reference's order."""
+    H, W = rgb.shape[:2]
+    sel = np.empty((25, 3), np.uint8)
+    k = lib().or_kde_select(_p(np.ascontiguousarray(rgb)), W, H, int(x), int(y), _p(sel))
+    return sel[:k]
+
+
+def kde_terms(gauss, sel, rgb):
+    """(pos, neg) int32 of the reference's kernel-density data term."""
+    gauss = np.ascontiguousarray(gauss, np.float32)
+    sel = np.ascontiguousarray(sel, np.uint8).reshape(-1, 3)
+    rgb = np.ascontiguousarray(rgb, np.uint8)
+    n = rgb.size // 3
+    pos = np.empty(rgb.shape[:-1], np.int32)
+    neg = np.empty(rgb.shape[:-1], np.int32)
+    lib().or_kde_terms(_p(gauss), _p(sel), len(sel), _p(rgb), n, _p(pos), _p(neg))
+    return pos, neg

@@ -7,7 +7,8 @@
 # (compiled from stdin in app_include/, whose GraphCut.cu declares the host
 # API that graphcut_ref.o defines) and multiplyMRF.cpp (plain C++; once as it
 # is, the 3600x3600 mode, and once with its DO_RIHANNA switch turned to 0 on
-# the fly, the general tiling mode).
+# the fly, the general tiling mode), and the reference's DataTerm.cpp with
+# dt_harness.cpp (its kernel-density data term).
 # Test infrastructure only: it produces the golden outputs that pin the
 # oracle and the tools.  Nothing from the reference is written anywhere but
 # oracle/_ref/.
@@ -31,6 +32,12 @@ for app in solveMRF Application; do
       -o "$OUT/${app}_ref.o" < "$REF/$app.cu")
   g++ -o "$OUT/$app" "$OUT/${app}_ref.o" "$OUT/graphcut_ref.o" "$OUT/cuda_emu.o"
 done
+# the reference's DataTerm namespace (DataTerm.cpp + DataTermKernels.cu) and its driver
+(cd "$HERE/app_include" && sed -E 's/([A-Za-z_][A-Za-z0-9_]*)<<<([^>]*)>>>\(/emu_launch(\2, \1, /' "$REF/DataTerm.cpp" |
+  g++ $FLAGS -x c++ -I "$HERE" -I "$REF" -include cuda_emu.h -include cutil.h "-Duchar=unsigned char" -c - \
+      -o "$OUT/dataterm_ref.o")
+g++ $FLAGS -I "$HERE" -c "$HERE/dt_harness.cpp" -o "$OUT/dt_harness.o"
+g++ -o "$OUT/dt_harness" "$OUT/dataterm_ref.o" "$OUT/cuda_emu.o" "$OUT/dt_harness.o"
 g++ -O2 -w -o "$OUT/multiplyMRF" "$REF/multiplyMRF.cpp"
 sed 's/^#define DO_RIHANNA 1/#define DO_RIHANNA 0/' "$REF/multiplyMRF.cpp" | g++ -O2 -w -x c++ - -o "$OUT/multiplyMRF_tile"
 echo "$OUT/ref_harness"

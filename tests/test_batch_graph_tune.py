@@ -88,8 +88,28 @@ def test_autotune_keeps_results():
     assert t["configs_tried"] >= 10
     assert t["push_rounds_per_gr"] in (2, 4, 8, 16) and t["max_tile_sweeps"] in (16, 32, 64, 128)
     assert t["sweeps_per_local_relabel"] in (2, 4, 8, 16, 32, 64) and 1 <= t["blocks_per_sm"] <= 8
-    assert t["local_relabel_first"] in (0, 1)
+    assert t["local_relabel_first"] in (0, 1) and t["push_only"] in (0, 1)
     assert t["ms_best"] <= t["ms_default"] and (t["tile_w"], t["tile_h"]) == (32, 32)
+    got = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
+    for a, b in zip(ref, got):
+        assert np.array_equal(a, b)
+    bs.close()
+
+
+@pytest.mark.parametrize("settings", [
+    dict(push_only=1, sweeps_per_local_relabel=4),
+    dict(push_only=1, sweeps_per_local_relabel=32, max_tile_sweeps=16),
+    dict(push_only=1, local_relabel_first=1, push_rounds_per_gr=2),
+    dict(push_only=0, local_relabel_first=1, sweeps_per_local_relabel=2, blocks_per_sm=2),
+    dict(push_only=0, push_rounds_per_gr=16, max_tile_sweeps=128, blocks_per_sm=1),
+])
+def test_solver_settings_do_not_change_results(settings):
+    Ws, Hs, lams, rgb, scrib = _batch(32, 3500)
+    d_rgb = torch.from_numpy(rgb).cuda()
+    d_scrib = torch.from_numpy(scrib).cuda()
+    bs = gcfg.BatchSolver(64, scrib.size)
+    ref = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
+    bs.set_solver(**settings)
     got = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
     for a, b in zip(ref, got):
         assert np.array_equal(a, b)
