@@ -224,37 +224,56 @@ __device__ __forceinline__ unsigned mask_word(const Batch &b, int t, int k, int 
     return __ldcg(b.tmask + ((size_t)t * 6 + k) * 32 + row);
 }
 
-// Exact distances of tile t given its halo; queues neighbours whose halo
-// (our border) decreased.  round0: the heights of every tile are stale, so
-// the halo and "old" border values come from the sink-connected bits.
-__device__ void gr_tile(const Batch &b, int t, bool round0, int tag_next, int slot_next, int *hs) {
-    const int lane = threadIdx.x & 31;
+// Where a global-relabel tile visit starts: the tile's neighbours and whether
+// its image is finished.  Loaded one visit ahead, so that the dependent loads
+// tile -> image -> descriptor overlap the previous visit's BFS; the masks and
+// halo words then load in one level at the start of the visit.
+struct GrGeo {
+    int nb[4];
+    bool skip;
+};
+
+__device__ __forceinline__ void gr_prefetch(const Batch &b, int t, GrGeo &gg) {
     const TileGeo g = tile_geo(b, t);
+    gg.skip = vload(&b.ist[g.img].done) != 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) gg.nb[k] = g.nb[k];
+}
+
+// Exact distances of tile t given its halo; queues neighbours whose halo
+// (our border) changed.  round0: the heights of every tile are stale, so the
+// halo and "old" border values come from the sink-connected bits.
+__device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int tag_next, int slot_next, int *hs) {
+    const int lane = threadIdx.x & 31;
     const size_t base = (size_t)t * TPX;
     unsigned m[6];
     load_tile_masks(b, t, m);
-    int o_top, o_bot, o_lft, o_rgt, ht, hb, hl, hr;
+    int ht, hb, hl, hr;
     if (round0) {
-        const unsigned n0 = __shfl_sync(FULL, m[4], 0), n31 = __shfl_sync(FULL, m[4], 31);
-        o_top = (n0 >> lane) & 1u ? 1 : INF_H;
-        o_bot = (n31 >> lane) & 1u ? 1 : INF_H;
-        o_lft = (m[4] & 1u) ? 1 : INF_H;
-        o_rgt = (m[4] >> 31) ? 1 : INF_H;
         ht = g.nb[2] >= 0 && ((mask_word(b, g.nb[2], 4, 31) >> lane) & 1u) ? 1 : INF_H;
         hb = g.nb[3] >= 0 && ((mask_word(b, g.nb[3], 4, 0) >> lane) & 1u) ? 1 : INF_H;
         hl = g.nb[0] >= 0 && (mask_word(b, g.nb[0], 4, lane) >> 31) ? 1 : INF_H;
         hr = g.nb[1] >= 0 && (mask_word(b, g.nb[1], 4, lane) & 1u) ? 1 : INF_H;
     } else {
-        o_top = __ldcg(b.h + base + lane);
-        o_bot = __ldcg(b.h + base + 31 * 32 + lane);
-        o_lft = __ldcg(b.h + base + lane * 32);
-        o_rgt = __ldcg(b.h + base + lane * 32 + 31);
         ht = g.nb[2] >= 0 ? __ldcg(b.h + (size_t)g.nb[2] * TPX + 31 * 32 + lane) : INF_H;
         hb = g.nb[3] >= 0 ? __ldcg(b.h + (size_t)g.nb[3] * TPX + lane) : INF_H;
         hl = g.nb[0] >= 0 ? __ldcg(b.h + (size_t)g.nb[0] * TPX + lane * 32 + 31) : INF_H;
         hr = g.nb[1] >= 0 ? __ldcg(b.h + (size_t)g.nb[1] * TPX + lane * 32) : INF_H;
     }
     const unsigned reached = tile_bfs(m[0], m[1], m[2], m[3], m[4], hl, hr, ht, hb, hs, 33);
+    int o_top, o_bot, o_lft, o_rgt;  // this tile's border before the visit (no other warp writes it meanwhile)
+    if (round0) {
+        const unsigned n0 = __shfl_sync(FULL, m[4], 0), n31 = __shfl_sync(FULL, m[4], 31);
+        o_top = (n0 >> lane) & 1u ? 1 : INF_H;
+        o_bot = (n31 >> lane) & 1u ? 1 : INF_H;
+        o_lft = (m[4] & 1u) ? 1 : INF_H;
+        o_rgt = (m[4] >> 31) ? 1 : INF_H;
+    } else {
+        o_top = __ldcg(b.h + base + lane);
+        o_bot = __ldcg(b.h + base + 31 * 32 + lane);
+        o_lft = __ldcg(b.h + base + lane * 32);
+        o_rgt = __ldcg(b.h + base + lane * 32 + 31);
+    }
     int act = __popc(m[5] & reached);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) act += __shfl_down_sync(FULL, act, o);
@@ -605,8 +624,10 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
         if (gtid == 0) ctl->total_active = 0;
         for (int k = gwarp; k < nt; k += nwarps) {
             const int t = batch_tile(b, k);
-            if (vload(&b.ist[__ldg(b.tile_img + t)].done)) continue;
-            gr_tile(b, t, true, G + 1, L_GR0 + ((G + 1) & 1), sm.w.hs[warp]);
+            GrGeo g;
+            gr_prefetch(b, t, g);
+            if (g.skip) continue;
+            gr_run(b, t, g, true, G + 1, L_GR0 + ((G + 1) & 1), sm.w.hs[warp]);
             if (lane == 0) atomicAdd(&ctl->gr_tiles, 1ull);
         }
         if (!grid_sync(b, (1u << L_PUSH0) | (1u << L_PUSH1) | (1u << L_PUSH2))) return;
@@ -625,7 +646,9 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
                 idx = __shfl_sync(FULL, idx, 0);
                 if (idx >= n) break;
                 const int t = b.lists[(size_t)slot * b.list_cap + idx];
-                gr_tile(b, t, false, G + 1, L_GR0 + ((G + 1) & 1), sm.w.hs[warp]);
+                GrGeo g;
+                gr_prefetch(b, t, g);
+                gr_run(b, t, g, false, G + 1, L_GR0 + ((G + 1) & 1), sm.w.hs[warp]);
                 if (lane == 0) atomicAdd(&ctl->gr_tiles, 1ull);
             }
             if (!grid_sync(b, 1u << slot)) return;

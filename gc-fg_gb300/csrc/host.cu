@@ -100,6 +100,20 @@ struct Engine {
     cudaStream_t cap_st = nullptr;
     long long graph_kernels = 0, graph_replays = 0, graph_captures = 0, graph_clock = 0;
     long long alloc_gen = 0;  // bumped whenever a buffer is reallocated
+
+    // Host entry points of many images: groups of consecutive images are
+    // uploaded on cp_st while earlier groups already compute on st.
+    static constexpr int MAX_GROUPS = 4;
+    struct Group {
+        int i0, i1, t0, t1;
+        long long p0, p1, c0, c1;
+    };
+    std::vector<Group> groups;
+    cudaStream_t cp_st = nullptr;
+    cudaEvent_t ev_in[MAX_GROUPS] = {}, ev_out[MAX_GROUPS] = {}, ev_mark = nullptr;
+    int *d_iota = nullptr; size_t c_iota = 0; int iota_n = 0;   // 0, 1, 2, ... (image and tile lists)
+    long long *d_gchunk = nullptr; size_t c_gchunk = 0;         // group-relative chunk offsets
+    long long *h_gchunk = nullptr; size_t ch_gchunk = 0;
     // sizes and lambdas of the layout currently on the device
     std::vector<int> lay_w, lay_h;
     std::vector<double> lay_lam;
@@ -136,6 +150,21 @@ struct Engine {
         drop_graphs();
         if (cap_st) cudaStreamDestroy(cap_st);
         cap_st = nullptr;
+        if (cp_st) cudaStreamDestroy(cp_st);
+        cp_st = nullptr;
+        for (int g = 0; g < MAX_GROUPS; ++g) {
+            if (ev_in[g]) cudaEventDestroy(ev_in[g]);
+            if (ev_out[g]) cudaEventDestroy(ev_out[g]);
+            ev_in[g] = ev_out[g] = nullptr;
+        }
+        if (ev_mark) cudaEventDestroy(ev_mark);
+        ev_mark = nullptr;
+        cudaFree(d_iota);
+        cudaFree(d_gchunk);
+        if (h_gchunk) cudaFreeHost(h_gchunk);
+        d_iota = nullptr;
+        d_gchunk = nullptr;
+        h_gchunk = nullptr;
         d_img = nullptr; d_ist = nullptr; d_chunk = nullptr; d_tile_img = nullptr;
         d_cap = nullptr; d_exc = nullptr; d_h = nullptr; d_reach = nullptr;
         d_tmask = nullptr; d_tact = nullptr; d_tpos = nullptr;
@@ -267,6 +296,63 @@ struct Engine {
             lay_lam.assign(lam, lam + n);
         else
             lay_lam.assign(n, 0.0);
+        return GCFG_OK;
+    }
+
+    // Split the laid-out batch into up to MAX_GROUPS groups of consecutive
+    // images of about equal pixel counts, and upload their lists.
+    gcfg_status make_groups(int n, const int *W, const int *H) {
+        const int G = n < MAX_GROUPS ? n : MAX_GROUPS;
+        groups.clear();
+        long long p = 0, c = 0;
+        int t = 0, i = 0;
+        for (int g = 0; g < G; ++g) {
+            Group gr;
+            gr.i0 = i;
+            gr.p0 = p;
+            gr.t0 = t;
+            gr.c0 = c;
+            const long long target = n_px * (g + 1) / G;
+            while (i < n && (i == gr.i0 || p < target) && n - i > G - 1 - g) {
+                p += (long long)W[i] * H[i];
+                t += div_up(W[i], TILE_W) * div_up(H[i], TILE_H);
+                ++i;
+            }
+            if (g == G - 1) {
+                while (i < n) {
+                    p += (long long)W[i] * H[i];
+                    t += div_up(W[i], TILE_W) * div_up(H[i], TILE_H);
+                    ++i;
+                }
+            }
+            gr.i1 = i;
+            gr.p1 = p;
+            gr.t1 = t;
+            gr.c1 = h_chunk[i];
+            c = gr.c1;
+            groups.push_back(gr);
+        }
+        const int need_iota = n > n_tiles ? n : n_tiles;
+        if (need_iota > iota_n || !d_iota) {
+            GCFG_TRY(grow(d_iota, c_iota, (size_t)need_iota));
+            std::vector<int> iota((size_t)need_iota);
+            for (int k = 0; k < need_iota; ++k) iota[k] = k;
+            GCFG_CK(cudaMemcpy(d_iota, iota.data(), iota.size() * sizeof(int), cudaMemcpyHostToDevice));
+            iota_n = need_iota;
+        }
+        GCFG_TRY(grow(d_gchunk, c_gchunk, (size_t)n + G));
+        GCFG_TRY(grow_host(h_gchunk, ch_gchunk, (size_t)n + G));
+        for (int g = 0; g < G; ++g) {
+            const Group &gr = groups[g];
+            for (int k = gr.i0; k <= gr.i1; ++k) h_gchunk[k + g] = h_chunk[k] - h_chunk[gr.i0];
+        }
+        GCFG_CK(cudaMemcpyAsync(d_gchunk, h_gchunk, ((size_t)n + G) * sizeof(long long), cudaMemcpyHostToDevice, st));
+        if (!cp_st) GCFG_CK(cudaStreamCreateWithFlags(&cp_st, cudaStreamNonBlocking));
+        for (int g = 0; g < MAX_GROUPS; ++g) {
+            if (!ev_in[g]) GCFG_CK(cudaEventCreateWithFlags(&ev_in[g], cudaEventDisableTiming));
+            if (!ev_out[g]) GCFG_CK(cudaEventCreateWithFlags(&ev_out[g], cudaEventDisableTiming));
+        }
+        if (!ev_mark) GCFG_CK(cudaEventCreateWithFlags(&ev_mark, cudaEventDisableTiming));
         return GCFG_OK;
     }
 
@@ -734,9 +820,77 @@ static gcfg_status run_batch_graph(Engine &e, int n, const int *W, const int *H,
     return e.status();
 }
 
+// Host-buffer entry point for several images: the groups' uploads (copy
+// stream) overlap the data term and graph build of the groups already on the
+// device, and after the solve each group's extraction is followed by its
+// download while the next group is extracted.
+static gcfg_status run_batch_staged(Engine &e, int n, const int *W, const int *H, const double *lam,
+                                    const uint8_t *h_rgb, const uint8_t *h_scrib, uint8_t *h_smin,
+                                    uint8_t *h_smax, int64_t *flows, gcfg_result *res) {
+    GCFG_CK(cudaEventRecord(e.ev0, e.st));
+    GCFG_TRY(e.layout(n, W, H, lam, true, true));
+    GCFG_TRY(e.make_groups(n, W, H));
+    // the uploads overwrite buffers that earlier work on st may read
+    GCFG_CK(cudaEventRecord(e.ev_mark, e.st));
+    GCFG_CK(cudaStreamWaitEvent(e.cp_st, e.ev_mark, 0));
+    const int G = (int)e.groups.size();
+    for (int g = 0; g < G; ++g) {
+        const Engine::Group &gr = e.groups[g];
+        const size_t np = (size_t)(gr.p1 - gr.p0);
+        GCFG_CK(cudaMemcpyAsync(e.d_rgb + 3 * gr.p0, h_rgb + 3 * gr.p0, 3 * np, cudaMemcpyHostToDevice, e.cp_st));
+        GCFG_CK(cudaMemcpyAsync(e.d_scrib + gr.p0, h_scrib + gr.p0, np, cudaMemcpyHostToDevice, e.cp_st));
+        GCFG_CK(cudaEventRecord(e.ev_in[g], e.cp_st));
+    }
+    for (int g = 0; g < G; ++g) {
+        const Engine::Group &gr = e.groups[g];
+        GCFG_CK(cudaStreamWaitEvent(e.st, e.ev_in[g], 0));
+        DtArgs a = e.dt(e.d_rgb, e.d_scrib);
+        a.n_img = gr.i1 - gr.i0;
+        a.ilist = e.d_iota + gr.i0;
+        a.total_chunks = gr.c1 - gr.c0;
+        a.chunk_off = e.d_gchunk + gr.i0 + g;
+        GCFG_CK(cudaMemsetAsync(e.d_hist + (size_t)gr.i0 * 2 * NBINS, 0,
+                                (size_t)(gr.i1 - gr.i0) * 2 * NBINS * sizeof(int), e.st));
+        GCFG_TRY(dt_tables(a, e.st));
+        Batch b = e.batch();
+        b.tlist = e.d_iota + gr.t0;
+        b.n_tlist = gr.t1 - gr.t0;
+        GCFG_TRY(dt_build(b, a, e.st));
+    }
+    GCFG_TRY(e.solve());
+    for (int g = 0; g < G; ++g) {
+        const Engine::Group &gr = e.groups[g];
+        Batch b = e.batch();
+        b.tlist = e.d_iota + gr.t0;
+        b.n_tlist = gr.t1 - gr.t0;
+        if (h_smin || h_smax)
+            GCFG_TRY(launch_extract(b, h_smin ? e.d_smin : nullptr, h_smax ? e.d_smax : nullptr, nullptr, e.st));
+        GCFG_CK(cudaEventRecord(e.ev_out[g], e.st));
+        GCFG_CK(cudaStreamWaitEvent(e.cp_st, e.ev_out[g], 0));
+        const size_t np = (size_t)(gr.p1 - gr.p0);
+        if (h_smin) GCFG_CK(cudaMemcpyAsync(h_smin + gr.p0, e.d_smin + gr.p0, np, cudaMemcpyDeviceToHost, e.cp_st));
+        if (h_smax) GCFG_CK(cudaMemcpyAsync(h_smax + gr.p0, e.d_smax + gr.p0, np, cudaMemcpyDeviceToHost, e.cp_st));
+    }
+    GCFG_TRY(e.readback());
+    GCFG_CK(cudaEventRecord(e.ev_mark, e.cp_st));
+    GCFG_CK(cudaStreamWaitEvent(e.st, e.ev_mark, 0));
+    GCFG_CK(cudaEventRecord(e.ev1, e.st));
+    GCFG_CK(cudaStreamSynchronize(e.st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e.ev0, e.ev1);
+    for (int i = 0; i < n; ++i) {
+        gcfg_result r;
+        e.result(i, &r, ms);
+        if (flows) flows[i] = r.flow;
+        if (res) res[i] = r;
+    }
+    return e.status();
+}
+
 static gcfg_status run_batch(Engine &e, int n, const int *W, const int *H, const double *lam,
                              const uint8_t *rgb, const uint8_t *scrib, uint8_t *smin, uint8_t *smax,
                              int64_t *flows, gcfg_result *res, bool staging) {
+    if (staging && n > 1) return run_batch_staged(e, n, W, H, lam, rgb, scrib, smin, smax, flows, res);
     if (e.graph_on && !e.graph_broken && !prof_on())
         return run_batch_graph(e, n, W, H, lam, rgb, scrib, smin, smax, flows, res, staging);
     return run_batch_eager(e, n, W, H, lam, rgb, scrib, smin, smax, flows, res, staging);
