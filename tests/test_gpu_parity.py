@@ -256,3 +256,63 @@ def test_tlinks_bit_exact_many(cfg, W, H, seed):
     gcfg.tlinks(dev(rgb), dev(scrib), dp, dn)
     odp, odn = O.tlinks(rgb, scrib)
     assert np.array_equal(dp.cpu().numpy(), odp) and np.array_equal(dn.cpu().numpy(), odn)
+
+
+def test_batch_degenerate_shapes():
+    """Images with no interior pixel (1xN, Nx1, 2x2), a single tile, tiles
+    just past a multiple of 32, mixed with a normal image in one batch."""
+    shapes = [(1, 1), (1, 7), (7, 1), (2, 2), (2, 50), (50, 2), (3, 3), (33, 1), (32, 32), (33, 33), (65, 31),
+              (200, 150)]
+    imgs = [O.generate(3, W, H, 1700 + i) for i, (W, H) in enumerate(shapes)]
+    lams = [(10.0, 50.0, 200.0)[i % 3] for i in range(len(imgs))]
+    Ws = [s.shape[1] for _, s in imgs]
+    Hs = [s.shape[0] for _, s in imgs]
+    rgb = np.concatenate([r.reshape(-1) for r, _ in imgs])
+    scrib = np.concatenate([s.reshape(-1) for _, s in imgs])
+    total = scrib.size
+    bs = gcfg.BatchSolver(len(imgs), total)
+    smin = torch.zeros(total, dtype=torch.uint8, device="cuda")
+    smax = torch.zeros(total, dtype=torch.uint8, device="cuda")
+    flows, _ = bs.run(Ws, Hs, lams, dev(rgb), dev(scrib), smin, smax)
+    smin = smin.cpu().numpy()
+    smax = smax.cpu().numpy()
+    off = 0
+    for i, ((r, s), lam) in enumerate(zip(imgs, lams)):
+        o = O.segment(r, s, lam)
+        k = s.size
+        assert flows[i] == o["flow"], shapes[i]
+        assert np.array_equal(smin[off:off + k].reshape(s.shape), o["smin"]), shapes[i]
+        assert np.array_equal(smax[off:off + k].reshape(s.shape), o["smax"]), shapes[i]
+        off += k
+    hmin = np.zeros(total, np.uint8)
+    hmax = np.zeros(total, np.uint8)
+    flows_h, _ = bs.run_host(Ws, Hs, lams, rgb, scrib, hmin, hmax)
+    assert np.array_equal(flows_h, flows) and np.array_equal(hmin, smin) and np.array_equal(hmax, smax)
+
+
+def test_batch256_full_size_cuts_match_per_image():
+    """The full 256-image workload: every image's cuts from the batched solve
+    equal the one-image path's, and a sample of flows equals the oracle's."""
+    import synth
+    shapes = synth.batch_shapes(256, 1000)
+    rgb, scrib, offs = synth.generate_packed([(3, W, H, s) for (W, H, s) in shapes])
+    Ws = [W for (W, _, _) in shapes]
+    Hs = [H for (_, H, _) in shapes]
+    total = scrib.size
+    d_rgb, d_scrib = dev(rgb), dev(scrib)
+    bs = gcfg.BatchSolver(256, total)
+    smin = torch.zeros(total, dtype=torch.uint8, device="cuda")
+    smax = torch.zeros(total, dtype=torch.uint8, device="cuda")
+    flows, _ = bs.run(Ws, Hs, [50.0] * 256, d_rgb, d_scrib, smin, smax)
+    seg = gcfg.Segmenter(max(Ws), max(Hs))
+    for i, (W, H, _) in enumerate(shapes):
+        o, n = int(offs[i]), W * H
+        a = torch.zeros(n, dtype=torch.uint8, device="cuda")
+        b = torch.zeros(n, dtype=torch.uint8, device="cuda")
+        r = seg.run(d_rgb[3 * o:3 * (o + n)], d_scrib[o:o + n], W, H, 50.0, a, b)
+        assert r["flow"] == flows[i], i
+        assert torch.equal(a, smin[o:o + n]) and torch.equal(b, smax[o:o + n]), i
+    for i in range(0, 256, 37):
+        W, H, _ = shapes[i]
+        o, n = int(offs[i]), W * H
+        assert flows[i] == O.segment(rgb[3 * o:3 * (o + n)].reshape(H, W, 3), scrib[o:o + n].reshape(H, W), 50.0)["flow"]
