@@ -1,0 +1,464 @@
+// engine8.cu -- graphs with the 8-neighbourhood (the reference built with
+// NEIGHBORHOOD == 8: GraphCut.h:22, the #if NEIGHBORHOOD == 8 blocks of
+// GraphCut.cu and GraphCutKernels.cu).
+//
+// A separate engine from the tiled 4-neighbour solver, so that the latter
+// keeps its layout and tuning.  Pixels are row-major; the residual
+// capacities are eight planes, cap[d * n + i] from pixel i toward direction
+// d (0 left, 1 right, 2 up, 3 down, 4 up-left, 5 up-right, 6 down-left,
+// 7 down-right).  One cooperative launch runs the whole solve:
+//   * exact global relabel: a frontier BFS from the sink-connected pixels
+//     (excess < 0) over the reverse residual edges, level by level;
+//   * count: pixels with excess that can still reach the sink; none left
+//     after an exact global relabel means the preflow is maximum (an exact
+//     termination test);
+//   * pulses: a push half (heights fixed; an edge pair (u, v) is used by at
+//     most one side in a half, since h(u) = h(v) + 1 and h(v) = h(u) + 1
+//     cannot both hold) and a relabel half (heights only increase);
+//   * cuts: S_max = pixels at height INF after the last exact global
+//     relabel, S_min = the forward closure of the pixels with excess.
+// Every spin is bounded; a timeout or an iteration cap sets an error that
+// the host reports as GCFG_ERR_NOT_CONVERGED.
+#include <cstring>
+
+#include "engine.cuh"
+
+namespace gcfg {
+namespace {
+
+constexpr int ND = 8;
+__device__ __forceinline__ int dxd(int d) { return d == 0 || d == 4 || d == 6 ? -1 : (d == 1 || d == 5 || d == 7 ? 1 : 0); }
+__device__ __forceinline__ int dyd(int d) { return d == 2 || d == 4 || d == 5 ? -1 : (d == 3 || d == 6 || d == 7 ? 1 : 0); }
+__device__ __forceinline__ int opp(int d) { return d < 4 ? (d ^ 1) : 11 - d; }
+
+struct Ctl8 {
+    unsigned bar_count, bar_gen;
+    int err, err_code;
+    int fsize[2];
+    int pad0[2];
+    unsigned long long active, pos_excess, interior_dp, ref_init;
+    int global_relabels, pulses, gr_levels, reach_levels;
+};
+
+struct G8 {
+    int W, H;
+    long long n;
+    int *cap;  // 8 * n
+    int *e, *h, *mark;
+    int *fr0, *fr1;
+    Ctl8 *ctl;
+};
+
+struct P8 {
+    int max_outer;   // global relabels at most
+    int pulses;      // push/relabel pulses between global relabels
+};
+
+enum { E8_BARRIER = 1, E8_OUTER = 2, E8_QUEUE = 3 };
+
+__device__ __forceinline__ void set_err8(Ctl8 *c, int code) {
+    atomicExch(&c->err, 1);
+    atomicCAS(&c->err_code, 0, code);
+}
+
+// Grid barrier (bounded spin); the last block to arrive clears frontier
+// size `reset` (>= 0) before releasing the others.
+__device__ bool sync8(Ctl8 *c, int reset) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = &c->bar_gen;
+        const unsigned gen = *vgen;
+        __threadfence();
+        if (atomicAdd(&c->bar_count, 1u) == gridDim.x - 1) {
+            if (reset >= 0) c->fsize[reset] = 0;
+            c->bar_count = 0;
+            __threadfence();
+            atomicAdd(&c->bar_gen, 1u);
+        } else {
+            unsigned long long it = 0;
+            while (*vgen == gen) {
+                if (++it > (1ull << 25)) {
+                    set_err8(c, E8_BARRIER);
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int *)&c->err == 0;
+}
+
+__device__ __forceinline__ void append(const G8 &g, int *fr, int slot, int v) {
+    const int pos = atomicAdd(&g.ctl->fsize[slot], 1);
+    if (pos < g.n) fr[pos] = v;
+    else set_err8(g.ctl, E8_QUEUE);
+}
+
+__device__ __forceinline__ bool nbr(const G8 &g, int i, int d, int &j) {
+    const int x = i % g.W + dxd(d), y = i / g.W + dyd(d);
+    if (x < 0 || y < 0 || x >= g.W || y >= g.H) return false;
+    j = y * g.W + x;
+    return true;
+}
+
+// Graph of the reference's InitGraph / InitGraphVarEdges with NEIGHBORHOOD
+// == 8 (GraphCutKernels.cu:112-214): interior pixels only, excess dp - dn,
+// caps from the arrays (or the penalty), edges toward the 1-pixel border
+// zeroed, diagonals included.
+struct Arr8 {
+    const int *a[8];  // left, right, up, down, up-left, up-right, down-left, down-right (NULL: penalty)
+};
+
+__global__ void k8_build(G8 g, const int *__restrict__ dp, const int *__restrict__ dn, int penalty, Arr8 arr) {
+    const long long w32 = (long long)((g.W + 31) / 32) * 32;
+    unsigned long long idp = 0, rinit = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < g.n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % g.W), y = (int)(i / g.W);
+        const bool inside = x > 0 && y > 0 && x < g.W - 1 && y < g.H - 1;
+        const int vdp = dp[i];
+        if ((long long)x + (long long)y * w32 < g.n && vdp > 0) rinit += (unsigned)vdp;
+        int e = 0;
+        if (inside) {
+            e = vdp - dn[i];
+            idp += (unsigned)vdp;
+            if (vdp < 0 || dn[i] < 0 || vdp > GCFG_MAX_CAP8 || dn[i] > GCFG_MAX_CAP8) set_err8(g.ctl, 9);
+        }
+        for (int d = 0; d < ND; ++d) {
+            int c = 0;
+            if (inside) {
+                c = arr.a[0] ? arr.a[d][i] : penalty;
+                if (c < 0 || c > GCFG_MAX_CAP8) set_err8(g.ctl, 9);
+                const int xx = x + dxd(d), yy = y + dyd(d);
+                if (xx < 1 || yy < 1 || xx > g.W - 2 || yy > g.H - 2) c = 0;  // toward the border ring
+            }
+            g.cap[(long long)d * g.n + i] = c;
+        }
+        g.e[i] = e;
+    }
+    if (idp) atomicAdd(&g.ctl->interior_dp, idp);
+    if (rinit) atomicAdd(&g.ctl->ref_init, rinit);
+}
+
+__global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
+    Ctl8 *c = g.ctl;
+    const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nth = (long long)gridDim.x * blockDim.x;
+    bool finished = false;
+    for (int outer = 0; outer < prm.max_outer; ++outer) {
+        // ---- exact global relabel ----
+        for (long long i = gtid; i < g.n; i += nth) {
+            const bool s = g.e[i] < 0;
+            g.h[i] = s ? 1 : INF_H;
+            if (s) append(g, g.fr0, 0, (int)i);
+        }
+        if (gtid == 0) c->active = 0;
+        if (!sync8(c, 1)) return;
+        for (int L = 1;; ++L) {
+            const int cur = (L - 1) & 1, nxt = L & 1;
+            const int ncur = *(volatile int *)&c->fsize[cur];
+            if (ncur == 0) break;
+            const int *fc = cur ? g.fr1 : g.fr0;
+            int *fn = nxt ? g.fr1 : g.fr0;
+            for (long long k = gtid; k < ncur; k += nth) {
+                const int v = fc[k];
+                for (int d = 0; d < ND; ++d) {
+                    int u;
+                    if (!nbr(g, v, d, u)) continue;
+                    // u -> v is u's edge in the opposite direction
+                    if (g.cap[(long long)opp(d) * g.n + u] > 0 && *(volatile int *)&g.h[u] == INF_H &&
+                        atomicCAS(&g.h[u], INF_H, L + 1) == INF_H)
+                        append(g, fn, nxt, u);
+                }
+            }
+            if (gtid == 0) c->gr_levels++;
+            if (!sync8(c, cur)) return;
+        }
+        if (gtid == 0) c->global_relabels++;
+        // ---- count: excess that can still reach the sink ----
+        unsigned long long act = 0;
+        for (long long i = gtid; i < g.n; i += nth) act += g.e[i] > 0 && g.h[i] < INF_H;
+        if (act) atomicAdd(&c->active, act);
+        if (!sync8(c, 0)) return;
+        if (*(volatile unsigned long long *)&c->active == 0) {
+            finished = true;
+            break;
+        }
+        // ---- push / relabel pulses ----
+        for (int p = 0; p < prm.pulses; ++p) {
+            for (long long i = gtid; i < g.n; i += nth) {
+                int e = g.e[i];
+                const int hi = g.h[i];
+                if (e <= 0 || hi >= INF_H) continue;
+                const int e0 = e;
+                for (int d = 0; d < ND && e > 0; ++d) {
+                    const int cd = g.cap[(long long)d * g.n + i];
+                    int j;
+                    if (cd <= 0 || !nbr(g, (int)i, d, j) || g.h[j] != hi - 1) continue;
+                    const int f = min(e, cd);
+                    g.cap[(long long)d * g.n + i] = cd - f;
+                    atomicAdd(&g.cap[(long long)opp(d) * g.n + j], f);
+                    atomicAdd(&g.e[j], f);
+                    e -= f;
+                }
+                if (e != e0) atomicSub(&g.e[i], e0 - e);
+            }
+            if (!sync8(c, -1)) return;
+            for (long long i = gtid; i < g.n; i += nth) {
+                const int e = g.e[i];
+                const int hi = g.h[i];
+                if (e <= 0 || hi >= INF_H) continue;
+                int m = INF_H;
+                for (int d = 0; d < ND; ++d) {
+                    int j;
+                    if (g.cap[(long long)d * g.n + i] > 0 && nbr(g, (int)i, d, j)) m = min(m, g.h[j]);
+                }
+                if (m >= hi) g.h[i] = m >= INF_H - 1 ? INF_H : m + 1;
+            }
+            if (gtid == 0) c->pulses++;
+            if (!sync8(c, -1)) return;
+        }
+    }
+    if (!finished) {
+        if (gtid == 0) set_err8(c, E8_OUTER);
+        return;
+    }
+    // ---- final positive excess and the source-side closure (S_min) ----
+    unsigned long long pos = 0;
+    for (long long i = gtid; i < g.n; i += nth) {
+        const int e = g.e[i];
+        const bool s = e > 0;
+        if (s) pos += (unsigned)e;
+        g.mark[i] = s;
+        if (s) append(g, g.fr0, 0, (int)i);
+    }
+    if (pos) atomicAdd(&c->pos_excess, pos);
+    if (!sync8(c, 1)) return;
+    for (int L = 1;; ++L) {
+        const int cur = (L - 1) & 1, nxt = L & 1;
+        const int ncur = *(volatile int *)&c->fsize[cur];
+        if (ncur == 0) break;
+        const int *fc = cur ? g.fr1 : g.fr0;
+        int *fn = nxt ? g.fr1 : g.fr0;
+        for (long long k = gtid; k < ncur; k += nth) {
+            const int u = fc[k];
+            for (int d = 0; d < ND; ++d) {
+                int v;
+                if (!nbr(g, u, d, v) || g.cap[(long long)d * g.n + u] <= 0) continue;
+                if (*(volatile int *)&g.mark[v] == 0 && atomicCAS(&g.mark[v], 0, 1) == 0) append(g, fn, nxt, v);
+            }
+        }
+        if (gtid == 0) c->reach_levels++;
+        if (!sync8(c, cur)) return;
+    }
+}
+
+__global__ void k8_extract(G8 g, int *label, uint8_t *smin, uint8_t *smax) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < g.n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % g.W), y = (int)(i / g.W);
+        const bool inside = x > 0 && y > 0 && x < g.W - 1 && y < g.H - 1;
+        const int s = inside && g.h[i] >= INF_H;
+        if (label) label[i] = s;
+        if (smax) smax[i] = (uint8_t)s;
+        if (smin) smin[i] = (uint8_t)g.mark[i];
+    }
+}
+
+int grid8(long long n) {
+    long long b = (n + 255) / 256;
+    return (int)(b < 4096 ? (b > 0 ? b : 1) : 4096);
+}
+
+}  // namespace
+}  // namespace gcfg
+
+using namespace gcfg;
+
+struct gcfg_graph8 {
+    int W = 0, H = 0;
+    long long n = 0;
+    const int32_t *dp = nullptr, *dn = nullptr;
+    const int32_t *arr[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    int32_t penalty = 0;
+    bool varying = false, built = false, solved = false;
+    int *cap = nullptr, *e = nullptr, *h = nullptr, *mark = nullptr, *fr0 = nullptr, *fr1 = nullptr;
+    int32_t *d_label = nullptr;
+    Ctl8 *ctl = nullptr, *h_ctl = nullptr;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int pulses = 16, max_outer = 100000;
+
+    G8 g() const {
+        G8 x;
+        x.W = W;
+        x.H = H;
+        x.n = n;
+        x.cap = cap;
+        x.e = e;
+        x.h = h;
+        x.mark = mark;
+        x.fr0 = fr0;
+        x.fr1 = fr1;
+        x.ctl = ctl;
+        return x;
+    }
+    void release() {
+        cudaFree(cap); cudaFree(e); cudaFree(h); cudaFree(mark); cudaFree(fr0); cudaFree(fr1);
+        cudaFree(d_label); cudaFree(ctl);
+        if (h_ctl) cudaFreeHost(h_ctl);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+    }
+};
+
+extern "C" {
+
+gcfg_status gcfg_set_dataterms8(gcfg_graph8 *g, const int32_t *dp, const int32_t *dn) {
+    if (!g) return GCFG_ERR_INVALID;
+    g->dp = dp;
+    g->dn = dn;
+    g->built = false;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_set_edges8(gcfg_graph8 *g, const int32_t *up, const int32_t *down, const int32_t *left,
+                            const int32_t *right, const int32_t *upleft, const int32_t *upright,
+                            const int32_t *downleft, const int32_t *downright) {
+    if (!g || !up || !down || !left || !right || !upleft || !upright || !downleft || !downright)
+        return GCFG_ERR_INVALID;
+    const int32_t *a[8] = {left, right, up, down, upleft, upright, downleft, downright};
+    memcpy(g->arr, a, sizeof(a));
+    g->varying = true;
+    g->built = false;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_set_penalty8(gcfg_graph8 *g, int32_t penalty) {
+    if (!g || penalty < 0 || penalty > GCFG_MAX_CAP8) return GCFG_ERR_INVALID;
+    g->penalty = penalty;
+    g->varying = false;
+    g->built = false;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_set_stream8(gcfg_graph8 *g, void *stream) {
+    if (!g) return GCFG_ERR_INVALID;
+    g->st = (cudaStream_t)stream;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_set_graph8(gcfg_graph8 *g) {
+    if (!g || !g->dp || !g->dn) return GCFG_ERR_STATE;
+    GCFG_CK(cudaMemsetAsync(g->ctl, 0, sizeof(Ctl8), g->st));
+    Arr8 arr;
+    for (int d = 0; d < 8; ++d) arr.a[d] = g->varying ? g->arr[d] : nullptr;
+    k8_build<<<grid8(g->n), 256, 0, g->st>>>(g->g(), g->dp, g->dn, g->penalty, arr);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    GCFG_CK(cudaGetLastError());
+    GCFG_CK(cudaMemcpyAsync(g->h_ctl, g->ctl, sizeof(Ctl8), cudaMemcpyDeviceToHost, g->st));
+    GCFG_CK(cudaStreamSynchronize(g->st));
+    if (g->h_ctl->err) return GCFG_ERR_INVALID;  // capacities outside [0, GCFG_MAX_CAP8]
+    g->built = true;
+    g->solved = false;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_init8(int w, int h, const int32_t *dp, const int32_t *dn, int32_t penalty, const int32_t *up,
+                       const int32_t *down, const int32_t *left, const int32_t *right, const int32_t *upleft,
+                       const int32_t *upright, const int32_t *downleft, const int32_t *downright,
+                       gcfg_graph8 **out) {
+    if (!out || w <= 0 || h <= 0 || (long long)w * h > (1LL << 31) - 1) return GCFG_ERR_INVALID;
+    if (penalty < 0 || penalty > GCFG_MAX_CAP8) return GCFG_ERR_INVALID;
+    gcfg_graph8 *g = new gcfg_graph8();
+    g->W = w;
+    g->H = h;
+    g->n = (long long)w * h;
+    g->penalty = penalty;
+    const size_t n = (size_t)g->n;
+    gcfg_status rc = GCFG_OK;
+    if (cudaMalloc(&g->cap, 8 * n * sizeof(int)) != cudaSuccess || cudaMalloc(&g->e, n * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&g->h, n * sizeof(int)) != cudaSuccess || cudaMalloc(&g->mark, n * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&g->fr0, n * sizeof(int)) != cudaSuccess || cudaMalloc(&g->fr1, n * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&g->d_label, n * sizeof(int)) != cudaSuccess || cudaMalloc(&g->ctl, sizeof(Ctl8)) != cudaSuccess ||
+        cudaMallocHost(&g->h_ctl, sizeof(Ctl8)) != cudaSuccess)
+        rc = GCFG_ERR_OOM;
+    if (rc == GCFG_OK && (cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess))
+        rc = GCFG_ERR_CUDA;
+    if (rc == GCFG_OK && dp) {
+        gcfg_set_dataterms8(g, dp, dn);
+        if (up) rc = gcfg_set_edges8(g, up, down, left, right, upleft, upright, downleft, downright);
+        if (rc == GCFG_OK) rc = gcfg_set_graph8(g);
+    }
+    if (rc) {
+        g->release();
+        delete g;
+        return rc;
+    }
+    *out = g;
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_optimize8(gcfg_graph8 *g, int32_t *host_label, gcfg_result *res) {
+    if (!g) return GCFG_ERR_INVALID;
+    if (!g->built) return GCFG_ERR_STATE;
+    int per_sm = 0, sms = 0, dev = 0;
+    GCFG_CK(cudaGetDevice(&dev));
+    GCFG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    GCFG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k8_solve, 256, 0));
+    long long want = (g->n + 255) / 256;
+    long long grid = (long long)(per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+    if (want < grid) grid = want > 0 ? want : 1;
+    G8 gg = g->g();
+    P8 prm{g->max_outer, g->pulses};
+    void *args[] = {&gg, &prm};
+    GCFG_CK(cudaEventRecord(g->ev0, g->st));
+    GCFG_CK(cudaLaunchCooperativeKernel((const void *)k8_solve, dim3((unsigned)grid), dim3(256), args, 0, g->st));
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    k8_extract<<<grid8(g->n), 256, 0, g->st>>>(gg, g->d_label, nullptr, nullptr);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    GCFG_CK(cudaGetLastError());
+    GCFG_CK(cudaEventRecord(g->ev1, g->st));
+    if (host_label)
+        GCFG_CK(cudaMemcpyAsync(host_label, g->d_label, (size_t)g->n * sizeof(int32_t), cudaMemcpyDeviceToHost, g->st));
+    GCFG_CK(cudaMemcpyAsync(g->h_ctl, g->ctl, sizeof(Ctl8), cudaMemcpyDeviceToHost, g->st));
+    GCFG_CK(cudaStreamSynchronize(g->st));
+    g->built = false;  // the graph is consumed, as in the reference
+    const Ctl8 &c = *g->h_ctl;
+    const gcfg_status st = c.err ? GCFG_ERR_NOT_CONVERGED : GCFG_OK;
+    g->solved = st == GCFG_OK;
+    if (res) {
+        memset(res, 0, sizeof(*res));
+        res->flow = (long long)c.interior_dp - (long long)c.pos_excess;
+        res->ref_energy = (int32_t)((uint32_t)c.ref_init - (uint32_t)c.pos_excess);
+        res->status = st;
+        res->global_relabels = c.global_relabels;
+        res->gr_sweeps = c.gr_levels;
+        res->push_rounds = c.pulses;
+        res->cut_sweeps = c.reach_levels;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, g->ev0, g->ev1);
+        res->ms = ms;
+    }
+    return st;
+}
+
+gcfg_status gcfg_get_cuts8(gcfg_graph8 *g, uint8_t *d_smin, uint8_t *d_smax) {
+    if (!g) return GCFG_ERR_INVALID;
+    if (!g->solved) return GCFG_ERR_STATE;
+    k8_extract<<<grid8(g->n), 256, 0, g->st>>>(g->g(), nullptr, d_smin, d_smax);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    GCFG_CK(cudaGetLastError());
+    GCFG_CK(cudaStreamSynchronize(g->st));
+    return GCFG_OK;
+}
+
+gcfg_status gcfg_end8(gcfg_graph8 *g) {
+    if (!g) return GCFG_ERR_INVALID;
+    cudaStreamSynchronize(g->st);
+    g->release();
+    delete g;
+    return GCFG_OK;
+}
+
+}  // extern "C"

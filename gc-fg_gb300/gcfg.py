@@ -27,6 +27,7 @@ GCFG_ERR_STATE = 5
 GCFG_ERR_CAPACITY = 6
 GCFG_ERR_TOO_LARGE = 7
 GCFG_MAX_CAP = (1 << 28) - 1
+GCFG_MAX_CAP8 = (1 << 27) - 1
 GCFG_NOALLOC_MAX_TILES = 640
 
 # Every function declared in include/gcfg.h (checked by the CPU test suite).
@@ -39,6 +40,8 @@ EXPORTS = [
     "gcfg_batch_set_params", "gcfg_batch_run", "gcfg_batch_run_host", "gcfg_batch_destroy",
     "gcfg_solve_noalloc", "gcfg_batch_set_graph", "gcfg_batch_graph_info", "gcfg_batch_autotune",
     "gcfg_batch_set_solver",
+    "gcfg_init8", "gcfg_set_dataterms8", "gcfg_set_edges8", "gcfg_set_penalty8", "gcfg_set_graph8",
+    "gcfg_optimize8", "gcfg_get_cuts8", "gcfg_end8", "gcfg_set_stream8",
 ]
 
 PROF_KINDS = ["hist", "tlut", "sigma", "wlut", "build", "solve", "extract", "other"]
@@ -125,6 +128,15 @@ def load(path: str = LIB_PATH):
                                       C.POINTER(C.c_int64)]),
         "gcfg_batch_autotune": (S, [P, I, P, P, P, P, P, I, C.POINTER(Tuning)]),
         "gcfg_batch_set_solver": (S, [P, C.POINTER(Tuning)]),
+        "gcfg_init8": (S, [I, I, P, P, C.c_int32, P, P, P, P, P, P, P, P, C.POINTER(P)]),
+        "gcfg_set_dataterms8": (S, [P, P, P]),
+        "gcfg_set_edges8": (S, [P, P, P, P, P, P, P, P, P]),
+        "gcfg_set_penalty8": (S, [P, C.c_int32]),
+        "gcfg_set_graph8": (S, [P]),
+        "gcfg_optimize8": (S, [P, P, C.POINTER(Result)]),
+        "gcfg_get_cuts8": (S, [P, P, P]),
+        "gcfg_end8": (S, [P]),
+        "gcfg_set_stream8": (S, [P, P]),
         "gcfg_solve_noalloc": (S, [I, I, P, P, C.c_int32, P, P, P, P, P, C.POINTER(C.c_int64), P]),
         "gcfg_profile_enable": (S, [I]),
         "gcfg_profile_read": (S, [C.POINTER(ProfEntry), I, C.POINTER(I)]),
@@ -769,3 +781,46 @@ class DataTerm:
     @classmethod
     def getNeg(cls) -> DeviceArray:
         return cls._s().neg()
+
+
+# ---------------------------------------------------------------------------
+# 8-neighbourhood graphs (the reference built with NEIGHBORHOOD == 8)
+# ---------------------------------------------------------------------------
+
+class GlobalWrapper8:
+    """Handle of one 8-connected residual graph."""
+
+    def __init__(self, handle, width, height, keep):
+        self.handle, self.width, self.height, self._keep = handle, width, height, keep
+
+
+def GC_Init8(width, height, data_positive=None, data_negative=None, penalty=0, up=None, down=None, left=None,
+             right=None, upleft=None, upright=None, downleft=None, downright=None):
+    """GC_Init of the reference built with NEIGHBORHOOD == 8
+    (GraphCut.cu:187-194): four straight and four diagonal capacity arrays
+    (device int32 W*H, torch tensors) or a constant penalty."""
+    arrs = (up, down, left, right, upleft, upright, downleft, downright)
+    h = C.c_void_p()
+    _check(load().gcfg_init8(int(width), int(height), _ptr(data_positive), _ptr(data_negative), int(penalty),
+                             *[_ptr(a) for a in arrs], C.byref(h)), "gcfg_init8")
+    return GlobalWrapper8(h, width, height, [data_positive, data_negative, *arrs])
+
+
+def GC_Optimize8(gw, label=None) -> dict:
+    res = Result()
+    _check(load().gcfg_optimize8(gw.handle, _ptr(label), C.byref(res)), "gcfg_optimize8")
+    return res.as_dict()
+
+
+def GC_SetGraph8(gw):
+    _check(load().gcfg_set_graph8(gw.handle), "gcfg_set_graph8")
+
+
+def GC_GetCuts8(gw, smin=None, smax=None):
+    _check(load().gcfg_get_cuts8(gw.handle, _ptr(smin), _ptr(smax)), "gcfg_get_cuts8")
+
+
+def GC_End8(gw):
+    if gw.handle:
+        load().gcfg_end8(gw.handle)
+        gw.handle = None

@@ -102,6 +102,36 @@ gcfg_status gcfg_set_stream(gcfg_graph *g, void *stream);
  * per tile visit (solver schedule; does not change the result). */
 gcfg_status gcfg_set_schedule(gcfg_graph *g, int push_rounds_per_gr, int max_tile_sweeps);
 
+/* ---------------- graph API with the 8-neighbourhood ---------------- */
+
+/* The reference built with NEIGHBORHOOD == 8 (GraphCut.h:22; GC_Init's extra
+ * upleft/upright/downleft/downright arrays, GraphCut.cu:187-194): the same
+ * calls and meanings as above with four more per-direction capacity arrays
+ * (device int32 W*H each; upleft[p] is the capacity from p to the pixel above
+ * and to its left, and so on).  The diagonals of the interior pixels next to
+ * the border are zeroed like the straight edges (GraphCutKernels.cu:147-151,
+ * 204-208).  Capacities are limited to GCFG_MAX_CAP8 so that an excess over
+ * nine edges stays inside int32.  A separate, pixel-parallel engine solves
+ * these graphs (exact global relabels and termination, as for 4). */
+typedef struct gcfg_graph8 gcfg_graph8;
+#define GCFG_MAX_CAP8 ((1 << 27) - 1)
+
+gcfg_status gcfg_init8(int w, int h, const int32_t *dp, const int32_t *dn, int32_t penalty,
+                       const int32_t *up, const int32_t *down, const int32_t *left,
+                       const int32_t *right, const int32_t *upleft, const int32_t *upright,
+                       const int32_t *downleft, const int32_t *downright, gcfg_graph8 **out);
+gcfg_status gcfg_set_dataterms8(gcfg_graph8 *g, const int32_t *dp, const int32_t *dn);
+gcfg_status gcfg_set_edges8(gcfg_graph8 *g, const int32_t *up, const int32_t *down,
+                            const int32_t *left, const int32_t *right, const int32_t *upleft,
+                            const int32_t *upright, const int32_t *downleft,
+                            const int32_t *downright);
+gcfg_status gcfg_set_penalty8(gcfg_graph8 *g, int32_t penalty);
+gcfg_status gcfg_set_graph8(gcfg_graph8 *g);
+gcfg_status gcfg_optimize8(gcfg_graph8 *g, int32_t *host_label, gcfg_result *res);
+gcfg_status gcfg_get_cuts8(gcfg_graph8 *g, uint8_t *d_smin, uint8_t *d_smax);
+gcfg_status gcfg_end8(gcfg_graph8 *g);
+gcfg_status gcfg_set_stream8(gcfg_graph8 *g, void *stream);
+
 /* ---------------- data term + n-links ---------------- */
 
 /* Colour-histogram t-links for one image: 16^3 bins of (r>>4, g>>4, b>>4)

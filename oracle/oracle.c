@@ -735,3 +735,188 @@ void or_kde_terms(const float *gauss, const uint8_t *sel, int n_sel, const uint8
         neg[i] = (int32_t)(300000.0 * (double)(1.0f - p));
     }
 }
+
+/* ---------------------------------------------------------------------------
+ * 8-connected graphs (the reference built with NEIGHBORHOOD == 8).
+ * Directions: 0 left, 1 right, 2 up, 3 down, 4 up-left, 5 up-right,
+ * 6 down-left, 7 down-right; caps8[8 * i + d] is the capacity from pixel i to
+ * its neighbour in direction d.
+ * ------------------------------------------------------------------------- */
+
+static const int D8X[8] = {-1, 1, 0, 0, -1, 1, -1, 1};
+static const int D8Y[8] = {0, 0, -1, 1, -1, -1, 1, 1};
+static const int D8OPP[8] = {1, 0, 3, 2, 7, 6, 5, 4};
+
+/* InitGraph / InitGraphVarEdges with NEIGHBORHOOD == 8
+ * (GraphCutKernels.cu:112-214): interior nodes only; arrays[d] (or the
+ * penalty) per direction; the edges of x == 1 toward the left column, of
+ * x == W-2 toward the right, of y == 1 upward and of y == H-2 downward
+ * (diagonals included) are zeroed. */
+void or8_build(int W, int H, const int32_t *dp, const int32_t *dn, int penalty, const int32_t *const *arrays,
+               int32_t *caps8, int32_t *excess) {
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const int64_t i = (int64_t)y * W + x;
+            int32_t *c = caps8 + 8 * i;
+            const int inside = x > 0 && y > 0 && x < W - 1 && y < H - 1;
+            for (int d = 0; d < 8; ++d) c[d] = inside ? (arrays ? arrays[d][i] : penalty) : 0;
+            excess[i] = inside ? dp[i] - dn[i] : 0;
+            if (!inside) continue;
+            if (x == 1) c[0] = c[4] = c[6] = 0;
+            if (x == W - 2) c[1] = c[5] = c[7] = 0;
+            if (y == 1) c[2] = c[4] = c[5] = 0;
+            if (y == H - 2) c[3] = c[6] = c[7] = 0;
+        }
+}
+
+static inline int or8_nbr(int W, int H, int64_t i, int d, int64_t *j) {
+    const int x = (int)(i % W) + D8X[d], y = (int)(i / W) + D8Y[d];
+    if (x < 0 || y < 0 || x >= W || y >= H) return 0;
+    *j = (int64_t)y * W + x;
+    return 1;
+}
+
+/* exact residual BFS distance to the sink-connected nodes (excess < 0) */
+static void or8_global_relabel(int W, int H, const int32_t *caps8, const int32_t *excess, int32_t *h, int32_t INF,
+                               int64_t *queue) {
+    const int64_t n = (int64_t)W * H;
+    int64_t qh = 0, qt = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        h[i] = INF;
+        if (excess[i] < 0) { h[i] = 1; queue[qt++] = i; }
+    }
+    while (qh < qt) {
+        const int64_t v = queue[qh++];
+        for (int d = 0; d < 8; ++d) {
+            int64_t u;
+            if (!or8_nbr(W, H, v, d, &u)) continue;
+            /* u -> v is u's edge in the direction opposite to d */
+            if (h[u] == INF && caps8[8 * u + D8OPP[d]] > 0) {
+                h[u] = h[v] + 1;
+                queue[qt++] = u;
+            }
+        }
+    }
+}
+
+/* FIFO push-relabel with exact global relabels (8 directions). */
+int or8_maxflow(int W, int H, int32_t *caps8, int32_t *excess) {
+    const int64_t n = (int64_t)W * H;
+    const int32_t INF = (int32_t)(n + 1);
+    int32_t *h = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+    int64_t *queue = (int64_t *)malloc((size_t)(n + 1) * sizeof(int64_t));
+    int64_t *fifo = (int64_t *)malloc((size_t)(n + 1) * sizeof(int64_t));
+    uint8_t *inq = (uint8_t *)calloc((size_t)n, 1);
+    if (!h || !queue || !fifo || !inq) {
+        free(h); free(queue); free(fifo); free(inq);
+        return -2;
+    }
+    int64_t fh = 0, fcount = 0, cap_q = n + 1, work = 0;
+#define FIFO8_PUSH(v) do { fifo[(fh + fcount) % cap_q] = (v); fcount++; inq[v] = 1; } while (0)
+    or8_global_relabel(W, H, caps8, excess, h, INF, queue);
+    for (int64_t i = 0; i < n; ++i)
+        if (excess[i] > 0 && h[i] < INF) FIFO8_PUSH(i);
+    while (fcount > 0) {
+        const int64_t u = fifo[fh];
+        fh = (fh + 1) % cap_q;
+        fcount--;
+        inq[u] = 0;
+        while (excess[u] > 0 && h[u] < INF) {
+            for (int d = 0; d < 8 && excess[u] > 0; ++d) {
+                const int32_t r = caps8[8 * u + d];
+                int64_t v;
+                if (r <= 0 || !or8_nbr(W, H, u, d, &v) || h[u] != h[v] + 1) continue;
+                const int32_t f = excess[u] < r ? excess[u] : r;
+                caps8[8 * u + d] -= f;
+                caps8[8 * v + D8OPP[d]] += f;
+                excess[u] -= f;
+                const int32_t ev = excess[v];
+                excess[v] += f;
+                if (ev <= 0 && excess[v] > 0 && !inq[v] && h[v] < INF) FIFO8_PUSH(v);
+            }
+            if (excess[u] <= 0) break;
+            int32_t m = INF;
+            for (int d = 0; d < 8; ++d) {
+                int64_t v;
+                if (caps8[8 * u + d] <= 0 || !or8_nbr(W, H, u, d, &v)) continue;
+                if (h[v] < m) m = h[v];
+            }
+            h[u] = m >= INF - 1 ? INF : m + 1;
+            work += 20;
+        }
+        if (work > 6 * n + 64 && fcount > 0) {
+            or8_global_relabel(W, H, caps8, excess, h, INF, queue);
+            work = 0;
+            fh = 0;
+            fcount = 0;
+            memset(inq, 0, (size_t)n);
+            for (int64_t i = 0; i < n; ++i)
+                if (excess[i] > 0 && h[i] < INF) FIFO8_PUSH(i);
+        }
+    }
+#undef FIFO8_PUSH
+    or8_global_relabel(W, H, caps8, excess, h, INF, queue);
+    int ok = 1;
+    for (int64_t i = 0; i < n; ++i)
+        if (excess[i] > 0 && h[i] < INF) { ok = 0; break; }
+    free(h); free(queue); free(fifo); free(inq);
+    return ok ? 0 : -3;
+}
+
+/* smax: interior nodes that cannot reach the sink; smin: nodes reachable
+ * from positive excess (8-connected residual graph). */
+void or8_cuts(int W, int H, const int32_t *caps8, const int32_t *excess, uint8_t *smin, uint8_t *smax) {
+    const int64_t n = (int64_t)W * H;
+    int64_t *queue = (int64_t *)malloc((size_t)(n + 1) * sizeof(int64_t));
+    uint8_t *mark = (uint8_t *)calloc((size_t)n, 1);
+    int64_t qh = 0, qt = 0;
+    for (int64_t i = 0; i < n; ++i)
+        if (excess[i] < 0) { mark[i] = 1; queue[qt++] = i; }
+    while (qh < qt) {
+        const int64_t v = queue[qh++];
+        for (int d = 0; d < 8; ++d) {
+            int64_t u;
+            if (!or8_nbr(W, H, v, d, &u)) continue;
+            if (!mark[u] && caps8[8 * u + D8OPP[d]] > 0) { mark[u] = 1; queue[qt++] = u; }
+        }
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        const int x = (int)(i % W), y = (int)(i / W);
+        smax[i] = (uint8_t)(x > 0 && y > 0 && x < W - 1 && y < H - 1 && !mark[i]);
+    }
+    memset(mark, 0, (size_t)n);
+    qh = qt = 0;
+    for (int64_t i = 0; i < n; ++i)
+        if (excess[i] > 0) { mark[i] = 1; queue[qt++] = i; }
+    while (qh < qt) {
+        const int64_t u = queue[qh++];
+        for (int d = 0; d < 8; ++d) {
+            int64_t v;
+            if (!or8_nbr(W, H, u, d, &v)) continue;
+            if (!mark[v] && caps8[8 * u + d] > 0) { mark[v] = 1; queue[qt++] = v; }
+        }
+    }
+    memcpy(smin, mark, (size_t)n);
+    free(queue);
+    free(mark);
+}
+
+int or8_solve(int W, int H, const int32_t *dp, const int32_t *dn, int penalty, const int32_t *const *arrays,
+              uint8_t *smin, uint8_t *smax, int64_t *flow, int32_t *excess_out) {
+    const int64_t n = (int64_t)W * H;
+    int32_t *caps8 = (int32_t *)malloc((size_t)(8 * n) * sizeof(int32_t));
+    int32_t *ex = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+    if (!caps8 || !ex) { free(caps8); free(ex); return -2; }
+    or8_build(W, H, dp, dn, penalty, arrays, caps8, ex);
+    const int rc = or8_maxflow(W, H, caps8, ex);
+    if (rc == 0) {
+        int64_t pos = 0;
+        for (int64_t i = 0; i < n; ++i) if (ex[i] > 0) pos += ex[i];
+        if (flow) *flow = or_interior_dp(W, H, dp) - pos;
+        if (smin && smax) or8_cuts(W, H, caps8, ex, smin, smax);
+        if (excess_out) memcpy(excess_out, ex, (size_t)n * sizeof(int32_t));
+    }
+    free(caps8);
+    free(ex);
+    return rc;
+}

@@ -95,6 +95,15 @@ int or_segment(const uint8_t *rgb, const uint8_t *scrib, int W, int H,
                int32_t *up, int32_t *down, int32_t *left, int32_t *right,
                uint8_t *smin, uint8_t *smax, int64_t *flow);
 
+/* 8-connected graphs (the reference built with NEIGHBORHOOD == 8,
+ * GraphCutKernels.cu:112-214 and the #if NEIGHBORHOOD == 8 blocks).
+ * Directions 0 left, 1 right, 2 up, 3 down, 4 up-left, 5 up-right,
+ * 6 down-left, 7 down-right.  arrays: NULL (constant penalty) or 8 W*H
+ * arrays in that order (the reference's up/down/left/right/upleft/upright/
+ * downleft/downright arguments). */
+int or8_solve(int W, int H, const int32_t *dp, const int32_t *dn, int penalty, const int32_t *const *arrays,
+              uint8_t *smin, uint8_t *smax, int64_t *flow, int32_t *excess_out);
+
 /* The reference's kernel-density data term (DataTerm.cpp:97-137,
  * DataTermKernels.cu:19-31, 61-83, 116-161).  The class density at colour c
  * is, summed in float in selection order (one selectOnMap launch after the

@@ -74,6 +74,7 @@ def lib():
         _lib.or_segment.argtypes = [P, P, C.c_int, C.c_int, C.c_double, C.c_int, P, P, P, P, P, P,
                                     P, P, C.POINTER(C.c_int64)]
         _lib.or_segment_batch.argtypes = [C.c_int, P, P, P, P, P, P, C.c_int, C.c_int, P, P, P]
+        _lib.or8_solve.argtypes = [C.c_int, C.c_int, P, P, C.c_int, P, P, P, C.POINTER(C.c_int64), P]
         _lib.or_kde_gauss.argtypes = [C.c_int, P]
         _lib.or_kde_select.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, P]
         _lib.or_kde_terms.argtypes = [P, P, C.c_int, P, C.c_int, P, P]
@@ -249,3 +250,27 @@ def kde_terms(gauss, sel, rgb):
     neg = np.empty(rgb.shape[:-1], np.int32)
     lib().or_kde_terms(_p(gauss), _p(sel), len(sel), _p(rgb), n, _p(pos), _p(neg))
     return pos, neg
+
+
+def solve8(dp, dn, penalty=0, arrays=None):
+    """8-connected solve in the reference's conventions.  arrays: None
+    (constant penalty) or 8 (H, W) arrays: left, right, up, down, up-left,
+    up-right, down-left, down-right.  Returns dict(flow, smin, smax, excess)."""
+    dp = np.ascontiguousarray(dp, np.int32)
+    dn = np.ascontiguousarray(dn, np.int32)
+    H, W = dp.shape
+    keep = None
+    ptrs = None
+    if arrays is not None:
+        keep = [np.ascontiguousarray(a, np.int32) for a in arrays]
+        assert len(keep) == 8
+        ptrs = (C.c_void_p * 8)(*[a.ctypes.data for a in keep])
+    smin = np.empty((H, W), np.uint8)
+    smax = np.empty((H, W), np.uint8)
+    ex = np.empty((H, W), np.int32)
+    flow = C.c_int64()
+    rc = lib().or8_solve(W, H, _p(dp), _p(dn), int(penalty), C.cast(ptrs, C.c_void_p) if ptrs is not None else None,
+                         _p(smin), _p(smax), C.byref(flow), _p(ex))
+    if rc != 0:
+        raise RuntimeError(f"or8_solve failed: {rc}")
+    return dict(flow=flow.value, smin=smin, smax=smax, excess=ex)

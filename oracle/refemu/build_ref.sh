@@ -7,8 +7,9 @@
 # (compiled from stdin in app_include/, whose GraphCut.cu declares the host
 # API that graphcut_ref.o defines) and multiplyMRF.cpp (plain C++; once as it
 # is, the 3600x3600 mode, and once with its DO_RIHANNA switch turned to 0 on
-# the fly, the general tiling mode), and the reference's DataTerm.cpp with
-# dt_harness.cpp (its kernel-density data term).
+# the fly, the general tiling mode), the reference's DataTerm.cpp with
+# dt_harness.cpp (its kernel-density data term), and the solver built with
+# NEIGHBORHOOD 8 with ref_harness8.cpp.
 # Test infrastructure only: it produces the golden outputs that pin the
 # oracle and the tools.  Nothing from the reference is written anywhere but
 # oracle/_ref/.
@@ -32,6 +33,14 @@ for app in solveMRF Application; do
       -o "$OUT/${app}_ref.o" < "$REF/$app.cu")
   g++ -o "$OUT/$app" "$OUT/${app}_ref.o" "$OUT/graphcut_ref.o" "$OUT/cuda_emu.o"
 done
+# the solver again with NEIGHBORHOOD 8 (its header, switched on the fly, is
+# streamed ahead of the source; no modified copy is written anywhere)
+N8='s/^#define NEIGHBORHOOD 4/#define NEIGHBORHOOD 8/'
+{ sed "$N8" "$REF/GraphCut.h"; sed -E 's/([A-Za-z_][A-Za-z0-9_]*)<<<([^>]*)>>>\(/emu_launch(\2, \1, /' "$REF/GraphCut.cu"; } |
+  g++ $FLAGS -x c++ -I "$HERE" -I "$REF" -include cuda_emu.h -c - -o "$OUT/graphcut8_ref.o"
+{ sed "$N8" "$REF/GraphCut.h"; cat "$HERE/ref_harness8.cpp"; } |
+  g++ $FLAGS -x c++ -I "$HERE" -I "$REF" -include cuda_emu.h -c - -o "$OUT/ref_harness8.o"
+g++ -o "$OUT/ref_harness8" "$OUT/graphcut8_ref.o" "$OUT/cuda_emu.o" "$OUT/ref_harness8.o"
 # the reference's DataTerm namespace (DataTerm.cpp + DataTermKernels.cu) and its driver
 (cd "$HERE/app_include" && sed -E 's/([A-Za-z_][A-Za-z0-9_]*)<<<([^>]*)>>>\(/emu_launch(\2, \1, /' "$REF/DataTerm.cpp" |
   g++ $FLAGS -x c++ -I "$HERE" -I "$REF" -include cuda_emu.h -include cutil.h "-Duchar=unsigned char" -c - \
