@@ -41,7 +41,7 @@ EXPORTS = [
     "gcfg_solve_noalloc", "gcfg_batch_set_graph", "gcfg_batch_graph_info", "gcfg_batch_autotune",
     "gcfg_batch_set_solver",
     "gcfg_init8", "gcfg_set_dataterms8", "gcfg_set_edges8", "gcfg_set_penalty8", "gcfg_set_graph8",
-    "gcfg_optimize8", "gcfg_get_cuts8", "gcfg_end8", "gcfg_set_stream8",
+    "gcfg_optimize8", "gcfg_get_cuts8", "gcfg_end8", "gcfg_set_stream8", "gcfg_set_schedule8",
 ]
 
 PROF_KINDS = ["hist", "tlut", "sigma", "wlut", "build", "solve", "extract", "other"]
@@ -137,6 +137,7 @@ def load(path: str = LIB_PATH):
         "gcfg_get_cuts8": (S, [P, P, P]),
         "gcfg_end8": (S, [P]),
         "gcfg_set_stream8": (S, [P, P]),
+        "gcfg_set_schedule8": (S, [P, I, I]),
         "gcfg_solve_noalloc": (S, [I, I, P, P, C.c_int32, P, P, P, P, P, C.POINTER(C.c_int64), P]),
         "gcfg_profile_enable": (S, [I]),
         "gcfg_profile_read": (S, [C.POINTER(ProfEntry), I, C.POINTER(I)]),
@@ -810,6 +811,10 @@ def GC_Optimize8(gw, label=None) -> dict:
     res = Result()
     _check(load().gcfg_optimize8(gw.handle, _ptr(label), C.byref(res)), "gcfg_optimize8")
     return res.as_dict()
+
+
+def GC_SetSchedule8(gw, pulses_per_gr, blocks_per_sm=0):
+    _check(load().gcfg_set_schedule8(gw.handle, int(pulses_per_gr), int(blocks_per_sm)), "gcfg_set_schedule8")
 
 
 def GC_SetGraph8(gw):
