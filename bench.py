@@ -658,7 +658,7 @@ def main():
                                  "gr_tiles", "reach_tiles", "push_sweeps", "push_local_relabels",
                                  "t_global_relabel_ms", "t_count_ms", "t_push_ms", "t_reach_ms",
                                  "cyc_load", "cyc_local_relabel", "cyc_sweeps", "cyc_writeback",
-                                 "cyc_take")}}
+                                 "cyc_take", "bfs_iters_push", "bfs_iters_gr", "cyc_global_relabel")}}
     if plain is not None:
         line["plain_per_image"] = plain
     if batched and not args.no_serve and rank == 0:

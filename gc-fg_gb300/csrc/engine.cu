@@ -113,8 +113,9 @@ __device__ bool grid_sync(const Batch &b, unsigned reset_mask) {
         }
         __threadfence();
     }
-    __syncthreads();
-    return *(volatile int *)&c->err == 0;
+    // thread 0's reading of the error word decides for the whole block, so
+    // that every thread of a block leaves (or continues) together
+    return !__syncthreads_or(threadIdx.x == 0 && *(volatile int *)&c->err != 0);
 }
 
 __device__ __forceinline__ int vload(const int *p) { return *(volatile const int *)p; }
@@ -151,7 +152,7 @@ struct PhaseClock {
 // hs[row * stride + col]; unreachable nodes get INF.  Returns this row's
 // reached set.
 __device__ unsigned tile_bfs(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd, unsigned sink, int hl,
-                         int hr, int ht, int hb, int *hs, int stride) {
+                         int hr, int ht, int hb, int *hs, int stride, int *iters) {
     const int lane = threadIdx.x & 31;
     int *row = hs + lane * stride;
 #pragma unroll 8
@@ -159,7 +160,8 @@ __device__ unsigned tile_bfs(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd,
     unsigned S = sink;
     for (unsigned m = sink; m; m &= m - 1) row[__ffs(m) - 1] = 1;
     int lvl = 1;
-    for (int it = 0; it < BFS_MAX_ITERS; ++it) {
+    int it = 0;
+    for (; it < BFS_MAX_ITERS; ++it) {
         const unsigned T = __ballot_sync(FULL, ht <= lvl);
         const unsigned B = __ballot_sync(FULL, hb <= lvl);
         unsigned up = __shfl_up_sync(FULL, S, 1);
@@ -184,12 +186,44 @@ __device__ unsigned tile_bfs(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd,
             lvl = nxt;
         }
     }
+    *iters = it;
     return S;
 }
 
 // ---------------------------------------------------------------------------
 // Shared memory of the persistent kernel (phases reuse the same bytes)
 // ---------------------------------------------------------------------------
+
+// Per-block solver statistics, accumulated in shared memory with shared
+// atomics and added to the Ctl counters once when the kernel ends, so that
+// no tile visit issues a global atomic on a shared counter address.
+enum {
+    ST_PUSH_TILES, ST_GR_TILES, ST_REACH_TILES, ST_PUSH_SWEEPS, ST_PUSH_BFS,
+    ST_CYC_LOAD, ST_CYC_BFS, ST_CYC_SWEEP, ST_CYC_WB, ST_CYC_TAKE,
+    ST_BFS_IT_PUSH, ST_BFS_IT_GR, ST_CYC_GR, ST_N
+};
+
+__device__ __forceinline__ void stat_add(unsigned long long *st, int k, unsigned long long v) {
+    atomicAdd(st + k, v);
+}
+
+__device__ __forceinline__ unsigned long long *ctl_stat(Ctl *c, int k) {
+    switch (k) {
+        case ST_PUSH_TILES: return &c->push_tiles;
+        case ST_GR_TILES: return &c->gr_tiles;
+        case ST_REACH_TILES: return &c->reach_tiles;
+        case ST_PUSH_SWEEPS: return &c->push_sweeps;
+        case ST_PUSH_BFS: return &c->push_bfs;
+        case ST_CYC_LOAD: return &c->cyc_load;
+        case ST_CYC_BFS: return &c->cyc_bfs;
+        case ST_CYC_SWEEP: return &c->cyc_sweep;
+        case ST_CYC_WB: return &c->cyc_wb;
+        case ST_CYC_TAKE: return &c->cyc_take;
+        case ST_BFS_IT_PUSH: return &c->bfs_it_push;
+        case ST_BFS_IT_GR: return &c->bfs_it_gr;
+        default: return &c->cyc_gr;
+    }
+}
 
 struct SmemPush {
     int4 c[TILE_H][TILE_W];
@@ -243,7 +277,8 @@ __device__ __forceinline__ void gr_prefetch(const Batch &b, int t, GrGeo &gg) {
 // Exact distances of tile t given its halo; queues neighbours whose halo
 // (our border) changed.  round0: the heights of every tile are stale, so the
 // halo and "old" border values come from the sink-connected bits.
-__device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int tag_next, int slot_next, int *hs) {
+__device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int tag_next, int slot_next, int *hs,
+                       unsigned long long *st) {
     const int lane = threadIdx.x & 31;
     const size_t base = (size_t)t * TPX;
     unsigned m[6];
@@ -260,7 +295,6 @@ __device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int t
         hl = g.nb[0] >= 0 ? __ldcg(b.h + (size_t)g.nb[0] * TPX + lane * 32 + 31) : INF_H;
         hr = g.nb[1] >= 0 ? __ldcg(b.h + (size_t)g.nb[1] * TPX + lane * 32) : INF_H;
     }
-    const unsigned reached = tile_bfs(m[0], m[1], m[2], m[3], m[4], hl, hr, ht, hb, hs, 33);
     int o_top, o_bot, o_lft, o_rgt;  // this tile's border before the visit (no other warp writes it meanwhile)
     if (round0) {
         const unsigned n0 = __shfl_sync(FULL, m[4], 0), n31 = __shfl_sync(FULL, m[4], 31);
@@ -274,6 +308,9 @@ __device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int t
         o_lft = __ldcg(b.h + base + lane * 32);
         o_rgt = __ldcg(b.h + base + lane * 32 + 31);
     }
+    int its = 0;
+    const unsigned reached = tile_bfs(m[0], m[1], m[2], m[3], m[4], hl, hr, ht, hb, hs, 33, &its);
+    if (lane == 0) stat_add(st, ST_BFS_IT_GR, (unsigned long long)its);
     int act = __popc(m[5] & reached);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) act += __shfl_down_sync(FULL, act, o);
@@ -333,7 +370,8 @@ __device__ void reach_tile(const Batch &b, int t, bool round0, int tag_next, int
 // Push/relabel on one tile (whole block)
 // ---------------------------------------------------------------------------
 
-__device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int phase, SmemPush &s) {
+__device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int phase, SmemPush &s,
+                          unsigned long long *st) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     long long c0 = clock64(), c1, cb = 0, cs = 0;
     const TileGeo g = tile_geo(b, t);
@@ -378,10 +416,13 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
         }
         __syncthreads();
         const long long cb0 = clock64();
-        if (warp == 0)
+        if (warp == 0) {
+            int its = 0;
             tile_bfs(s.m[0][lane], s.m[1][lane], s.m[2][lane], s.m[3][lane], s.m[4][lane],
                      s.h[lane + 1][0], s.h[lane + 1][TILE_W + 1], s.h[0][lane + 1],
-                     s.h[TILE_H + 1][lane + 1], &s.h[1][1], TILE_W + 2);
+                     s.h[TILE_H + 1][lane + 1], &s.h[1][1], TILE_W + 2, &its);
+            if (lane == 0) stat_add(st, ST_BFS_IT_PUSH, (unsigned long long)its);
+        }
         __syncthreads();
         cb += clock64() - cb0;
     };
@@ -572,12 +613,13 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
     if (any && threadIdx.x == 0) enqueue(b, b.mark_push, (phase + 2) % 3, phase + 2, t);
     __syncthreads();
     if (threadIdx.x == 0) {
-        atomicAdd(&b.ctl->push_sweeps, (unsigned long long)sweeps);
-        atomicAdd(&b.ctl->push_bfs, (unsigned long long)bfs);
-        atomicAdd(&b.ctl->cyc_load, (unsigned long long)c_load);
-        atomicAdd(&b.ctl->cyc_bfs, (unsigned long long)cb);
-        atomicAdd(&b.ctl->cyc_sweep, (unsigned long long)cs);
-        atomicAdd(&b.ctl->cyc_wb, (unsigned long long)(clock64() - c2));
+        stat_add(st, ST_PUSH_TILES, 1ull);
+        stat_add(st, ST_PUSH_SWEEPS, (unsigned long long)sweeps);
+        stat_add(st, ST_PUSH_BFS, (unsigned long long)bfs);
+        stat_add(st, ST_CYC_LOAD, (unsigned long long)c_load);
+        stat_add(st, ST_CYC_BFS, (unsigned long long)cb);
+        stat_add(st, ST_CYC_SWEEP, (unsigned long long)cs);
+        stat_add(st, ST_CYC_WB, (unsigned long long)(clock64() - c2));
     }
 }
 
@@ -591,11 +633,14 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
 
 __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(Batch b, SolveParams prm) {
     __shared__ Smem sm;
+    __shared__ unsigned long long st[ST_N];
     Ctl *ctl = b.ctl;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int gwarp = blockIdx.x * 8 + warp, nwarps = gridDim.x * 8;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
 
+    if (threadIdx.x < ST_N) st[threadIdx.x] = 0;
+    __syncthreads();
     PhaseClock clk;
     clk.start();
     // fresh de-duplication marks and reach bits for this solve
@@ -627,8 +672,12 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
             GrGeo g;
             gr_prefetch(b, t, g);
             if (g.skip) continue;
-            gr_run(b, t, g, true, G + 1, L_GR0 + ((G + 1) & 1), sm.w.hs[warp]);
-            if (lane == 0) atomicAdd(&ctl->gr_tiles, 1ull);
+            const long long c0 = clock64();
+            gr_run(b, t, g, true, G + 1, L_GR0 + ((G + 1) & 1), sm.w.hs[warp], st);
+            if (lane == 0) {
+                stat_add(st, ST_CYC_GR, (unsigned long long)(clock64() - c0));
+                stat_add(st, ST_GR_TILES, 1ull);
+            }
         }
         if (!grid_sync(b, (1u << L_PUSH0) | (1u << L_PUSH1) | (1u << L_PUSH2))) return;
         ++G;
@@ -646,10 +695,14 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
                 idx = __shfl_sync(FULL, idx, 0);
                 if (idx >= n) break;
                 const int t = b.lists[(size_t)slot * b.list_cap + idx];
+                const long long c0 = clock64();
                 GrGeo g;
                 gr_prefetch(b, t, g);
-                gr_run(b, t, g, false, G + 1, L_GR0 + ((G + 1) & 1), sm.w.hs[warp]);
-                if (lane == 0) atomicAdd(&ctl->gr_tiles, 1ull);
+                gr_run(b, t, g, false, G + 1, L_GR0 + ((G + 1) & 1), sm.w.hs[warp], st);
+                if (lane == 0) {
+                    stat_add(st, ST_CYC_GR, (unsigned long long)(clock64() - c0));
+                    stat_add(st, ST_GR_TILES, 1ull);
+                }
             }
             if (!grid_sync(b, 1u << slot)) return;
             ++G;
@@ -701,10 +754,9 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
                     __syncthreads();
                     const int idx = sm.p.idx;
                     __syncthreads();
-                    if (threadIdx.x == 0) atomicAdd(&ctl->cyc_take, (unsigned long long)(clock64() - ct));
+                    if (threadIdx.x == 0) stat_add(st, ST_CYC_TAKE, (unsigned long long)(clock64() - ct));
                     if (idx >= n) break;
-                    push_tile(b, b.lists[(size_t)slot * b.list_cap + idx], prm, p, sm.p);
-                    if (threadIdx.x == 0) atomicAdd(&ctl->push_tiles, 1ull);
+                    push_tile(b, b.lists[(size_t)slot * b.list_cap + idx], prm, p, sm.p, st);
                     __syncthreads();
                 }
                 if (!grid_sync(b, 1u << slot)) return;
@@ -741,13 +793,15 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
             idx = __shfl_sync(FULL, idx, 0);
             if (idx >= n) break;
             reach_tile(b, b.lists[(size_t)slot * b.list_cap + idx], false, G + 1, L_GR0 + ((G + 1) & 1));
-            if (lane == 0) atomicAdd(&ctl->reach_tiles, 1ull);
+            if (lane == 0) stat_add(st, ST_REACH_TILES, 1ull);
         }
         if (!grid_sync(b, 1u << slot)) return;
         ++G;
         if (gtid == 0) ctl->reach_rounds++;
     }
     clk.charge(&ctl->t_reach);
+    __syncthreads();
+    if (threadIdx.x < ST_N && st[threadIdx.x]) atomicAdd(ctl_stat(ctl, threadIdx.x), st[threadIdx.x]);
 }
 
 // ---------------------------------------------------------------------------

@@ -67,6 +67,9 @@ struct Ctl {
     unsigned long long push_sweeps, push_bfs;
     // SM cycles per section of the push visits, summed over visits
     unsigned long long cyc_load, cyc_bfs, cyc_sweep, cyc_wb, cyc_take;
+    // tile-BFS loop iterations (levels and halo jumps) of push and global-
+    // relabel visits, and SM cycles summed over global-relabel visits
+    unsigned long long bfs_it_push, bfs_it_gr, cyc_gr;
 };
 
 struct Batch {

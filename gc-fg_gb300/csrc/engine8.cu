@@ -86,8 +86,8 @@ __device__ bool sync8(Ctl8 *c, int reset) {
         }
         __threadfence();
     }
-    __syncthreads();
-    return *(volatile int *)&c->err == 0;
+    // thread 0's reading of the error word decides for the whole block
+    return !__syncthreads_or(threadIdx.x == 0 && *(volatile int *)&c->err != 0);
 }
 
 __device__ __forceinline__ void append(const G8 &g, int *fr, int slot, int v) {

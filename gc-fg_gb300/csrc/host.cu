@@ -454,6 +454,9 @@ struct Engine {
         r->cyc_sweeps = (long long)h_ctl->cyc_sweep;
         r->cyc_writeback = (long long)h_ctl->cyc_wb;
         r->cyc_take = (long long)h_ctl->cyc_take;
+        r->bfs_iters_push = (long long)h_ctl->bfs_it_push;
+        r->bfs_iters_gr = (long long)h_ctl->bfs_it_gr;
+        r->cyc_global_relabel = (long long)h_ctl->cyc_gr;
         r->ms = ms;
     }
 };
