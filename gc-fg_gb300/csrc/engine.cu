@@ -80,6 +80,25 @@ __device__ __forceinline__ void enqueue(const Batch &b, int *mark, int slot, int
     }
 }
 
+// Warp-collective enqueue (all 32 lanes call it): each lane with `want`
+// queues its tile t as enqueue() does, and the lanes that queue something
+// share one atomic on the list size.
+__device__ __forceinline__ void enqueue_warp(const Batch &b, int *mark, int slot, int tag, int t, bool want) {
+    const int lane = threadIdx.x & 31;
+    const bool won = want && atomicMax(mark + t, tag) < tag;
+    const unsigned m = __ballot_sync(0xffffffffu, won);
+    if (!m) return;
+    const int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&b.ctl->size[slot], __popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (won) {
+        const int pos = base + __popc(m & ((1u << lane) - 1u));
+        if (pos < b.list_cap) b.lists[(size_t)slot * b.list_cap + pos] = t;
+        else set_error(b, ERRC_QUEUE);
+    }
+}
+
 // Grid-wide barrier over the co-resident blocks of the cooperative launch.
 // The last block to arrive clears the queues named in reset_mask before it
 // releases the others.  The spin is bounded: on timeout the error flag is
@@ -322,10 +341,10 @@ __device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int t
     const bool ch_bot = __any_sync(FULL, hs[31 * 33 + lane] != o_bot);
     const bool ch_lft = __any_sync(FULL, hs[lane * 33] != o_lft);
     const bool ch_rgt = __any_sync(FULL, hs[lane * 33 + 31] != o_rgt);
-    if (lane == 0 && ch_lft && g.nb[0] >= 0) enqueue(b, b.mark_gr, slot_next, tag_next, g.nb[0]);
-    if (lane == 1 && ch_rgt && g.nb[1] >= 0) enqueue(b, b.mark_gr, slot_next, tag_next, g.nb[1]);
-    if (lane == 2 && ch_top && g.nb[2] >= 0) enqueue(b, b.mark_gr, slot_next, tag_next, g.nb[2]);
-    if (lane == 3 && ch_bot && g.nb[3] >= 0) enqueue(b, b.mark_gr, slot_next, tag_next, g.nb[3]);
+    // lanes 0..3 queue the left, right, upper and lower neighbour
+    const int nbt = lane == 0 ? g.nb[0] : lane == 1 ? g.nb[1] : lane == 2 ? g.nb[2] : g.nb[3];
+    const bool ch = lane == 0 ? ch_lft : lane == 1 ? ch_rgt : lane == 2 ? ch_top : ch_bot;
+    enqueue_warp(b, b.mark_gr, slot_next, tag_next, nbt, lane < 4 && ch && nbt >= 0);
     __syncwarp();
 }
 
@@ -360,10 +379,9 @@ __device__ void reach_tile(const Batch &b, int t, bool round0, int tag_next, int
     const bool out_r = __any_sync(FULL, (fresh & Rr & 0x80000000u) != 0);
     const bool out_u = __any_sync(FULL, lane == 0 && (fresh & Ru) != 0);
     const bool out_d = __any_sync(FULL, lane == 31 && (fresh & Rd) != 0);
-    if (lane == 0 && out_l && g.nb[0] >= 0) enqueue(b, b.mark_gr, slot_next, tag_next, g.nb[0]);
-    if (lane == 1 && out_r && g.nb[1] >= 0) enqueue(b, b.mark_gr, slot_next, tag_next, g.nb[1]);
-    if (lane == 2 && out_u && g.nb[2] >= 0) enqueue(b, b.mark_gr, slot_next, tag_next, g.nb[2]);
-    if (lane == 3 && out_d && g.nb[3] >= 0) enqueue(b, b.mark_gr, slot_next, tag_next, g.nb[3]);
+    const int nbt = lane == 0 ? g.nb[0] : lane == 1 ? g.nb[1] : lane == 2 ? g.nb[2] : g.nb[3];
+    const bool out = lane == 0 ? out_l : lane == 1 ? out_r : lane == 2 ? out_u : out_d;
+    enqueue_warp(b, b.mark_gr, slot_next, tag_next, nbt, lane < 4 && out && nbt >= 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -637,6 +655,7 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
     Ctl *ctl = b.ctl;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int gwarp = blockIdx.x * 8 + warp, nwarps = gridDim.x * 8;
+    const int swarp = warp * gridDim.x + blockIdx.x;  // block-interleaved warp rank
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
 
     if (threadIdx.x < ST_N) st[threadIdx.x] = 0;
@@ -689,11 +708,9 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
                 if (gtid == 0) set_error(b, ERRC_GR_ROUNDS);
                 return;
             }
-            for (;;) {
-                int idx = 0;
-                if (lane == 0) idx = atomicAdd(&ctl->take[slot], 1);
-                idx = __shfl_sync(FULL, idx, 0);
-                if (idx >= n) break;
+            // static assignment, interleaved over the blocks so that a small
+            // frontier spreads over every SM (no queue-take atomics)
+            for (int idx = swarp; idx < n; idx += nwarps) {
                 const int t = b.lists[(size_t)slot * b.list_cap + idx];
                 const long long c0 = clock64();
                 GrGeo g;
@@ -710,19 +727,46 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
         }
         clk.charge(&ctl->t_gr);
         // ------------------------ count active nodes ------------------------
-        for (int k = gtid; k < nt; k += nthreads) {
-            const int t = batch_tile(b, k);
-            const int img = __ldg(b.tile_img + t);
-            if (vload(&b.ist[img].done)) continue;
-            const int nact = vload(b.tile_act + t);
-            const unsigned long long pos = __ldcg(b.tile_pos + t);
-            if (pos) atomicAdd(&b.ist[img].pos_excess, pos);
-            if (nact) {
-                atomicAdd(&b.ist[img].active, (unsigned long long)nact);
-                atomicAdd(&ctl->total_active, (unsigned long long)nact);
-                const TileGeo g = tile_geo(b, t);
-                enqueue(b, b.mark_push, (P + g.color) % 3, P + g.color, t);
+        // warp-uniform loop: the sums of a warp's tiles go out with one
+        // atomic per image (a warp's tiles belong to one or two images) and
+        // one for the batch total; the queue appends share one per colour
+        for (int kb = gtid - lane; kb < nt; kb += nthreads) {
+            const int k = kb + lane;
+            int t = 0, img = -1, nact = 0, color = 0;
+            unsigned long long pos = 0;
+            if (k < nt) {
+                t = batch_tile(b, k);
+                img = __ldg(b.tile_img + t);
+                if (vload(&b.ist[img].done)) {
+                    img = -1;
+                } else {
+                    nact = vload(b.tile_act + t);
+                    pos = __ldcg(b.tile_pos + t);
+                    if (nact) color = tile_geo(b, t).color;
+                }
             }
+            unsigned todo = __ballot_sync(FULL, img >= 0 && (nact || pos));
+            while (todo) {
+                const int leader = __ffs(todo) - 1;
+                const int limg = __shfl_sync(FULL, img, leader);
+                const bool mine = ((todo >> lane) & 1u) && img == limg;
+                unsigned long long vp = mine ? pos : 0ull;
+                unsigned va = mine ? (unsigned)nact : 0u;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    vp += __shfl_xor_sync(FULL, vp, o);
+                    va += __shfl_xor_sync(FULL, va, o);
+                }
+                if (lane == leader) {
+                    if (vp) atomicAdd(&b.ist[limg].pos_excess, vp);
+                    if (va) atomicAdd(&b.ist[limg].active, (unsigned long long)va);
+                }
+                todo &= ~__ballot_sync(FULL, mine);
+            }
+            const unsigned wact = __reduce_add_sync(FULL, (unsigned)nact);
+            if (lane == 0 && wact) atomicAdd(&ctl->total_active, (unsigned long long)wact);
+            enqueue_warp(b, b.mark_push, P % 3, P, t, nact && color == 0);
+            enqueue_warp(b, b.mark_push, (P + 1) % 3, P + 1, t, nact && color == 1);
         }
         if (!grid_sync(b, 0)) return;
         clk.charge(&ctl->t_count);
@@ -787,11 +831,7 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
             if (gtid == 0) set_error(b, ERRC_REACH_ROUNDS);
             return;
         }
-        for (;;) {
-            int idx = 0;
-            if (lane == 0) idx = atomicAdd(&ctl->take[slot], 1);
-            idx = __shfl_sync(FULL, idx, 0);
-            if (idx >= n) break;
+        for (int idx = swarp; idx < n; idx += nwarps) {
             reach_tile(b, b.lists[(size_t)slot * b.list_cap + idx], false, G + 1, L_GR0 + ((G + 1) & 1));
             if (lane == 0) stat_add(st, ST_REACH_TILES, 1ull);
         }
