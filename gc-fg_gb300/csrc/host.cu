@@ -8,6 +8,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <utility>
 #include <vector>
 
 #include "dataterm.cuh"
@@ -118,6 +119,69 @@ struct Engine {
     std::vector<int> lay_w, lay_h;
     std::vector<double> lay_lam;
 
+    // Asynchronous host entry point: two batches in flight, each with its
+    // own pinned host tables, device staging buffers and timing events.  The
+    // set of the batch being queued or collected is swapped into the members
+    // above for the duration of that call (slot 0 is the members' own set,
+    // slot 1 is `alt`), so the rest of the engine is unchanged.  Compute of
+    // the two batches stays ordered on st; their uploads (cp_st) and
+    // downloads (dn_st) overlap the other batch's compute.
+    struct RunSet {
+        ImgDesc *h_img = nullptr; size_t ch_img = 0;
+        ImgState *h_ist = nullptr; size_t ch_ist = 0;
+        long long *h_chunk = nullptr; size_t ch_chunk = 0;
+        int *h_tile_img = nullptr; size_t ch_timg = 0;
+        long long *h_gchunk = nullptr; size_t ch_gchunk = 0;
+        Ctl *h_ctl = nullptr; size_t ch_ctl = 0;
+        uint8_t *d_rgb = nullptr; size_t c_rgb = 0;
+        uint8_t *d_scrib = nullptr; size_t c_scrib = 0;
+        uint8_t *d_smin = nullptr; size_t c_smin = 0;
+        uint8_t *d_smax = nullptr; size_t c_smax = 0;
+        cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    };
+    RunSet alt;
+    struct Flight {
+        bool busy = false;
+        long long ticket = 0;
+        int n = 0;
+        cudaEvent_t ev_up = nullptr;   // inputs of the batch uploaded (cp_st)
+        cudaEvent_t ev_ext = nullptr;  // labels of the batch extracted (st)
+        cudaEvent_t ev_dn = nullptr;   // downloads of the batch done (dn_st)
+    };
+    Flight flight[2];
+    cudaStream_t dn_st = nullptr;
+    long long next_ticket = 1;
+    int next_slot = 0;
+
+    bool in_flight() const { return flight[0].busy || flight[1].busy; }
+
+    void swap_set(RunSet &o) {
+        std::swap(h_img, o.h_img); std::swap(ch_img, o.ch_img);
+        std::swap(h_ist, o.h_ist); std::swap(ch_ist, o.ch_ist);
+        std::swap(h_chunk, o.h_chunk); std::swap(ch_chunk, o.ch_chunk);
+        std::swap(h_tile_img, o.h_tile_img); std::swap(ch_timg, o.ch_timg);
+        std::swap(h_gchunk, o.h_gchunk); std::swap(ch_gchunk, o.ch_gchunk);
+        std::swap(h_ctl, o.h_ctl); std::swap(ch_ctl, o.ch_ctl);
+        std::swap(d_rgb, o.d_rgb); std::swap(c_rgb, o.c_rgb);
+        std::swap(d_scrib, o.d_scrib); std::swap(c_scrib, o.c_scrib);
+        std::swap(d_smin, o.d_smin); std::swap(c_smin, o.c_smin);
+        std::swap(d_smax, o.d_smax); std::swap(c_smax, o.c_smax);
+        std::swap(ev0, o.ev0); std::swap(ev1, o.ev1);
+    }
+
+    static void free_set(RunSet &o) {
+        if (o.h_img) cudaFreeHost(o.h_img);
+        if (o.h_ist) cudaFreeHost(o.h_ist);
+        if (o.h_chunk) cudaFreeHost(o.h_chunk);
+        if (o.h_tile_img) cudaFreeHost(o.h_tile_img);
+        if (o.h_gchunk) cudaFreeHost(o.h_gchunk);
+        if (o.h_ctl) cudaFreeHost(o.h_ctl);
+        cudaFree(o.d_rgb); cudaFree(o.d_scrib); cudaFree(o.d_smin); cudaFree(o.d_smax);
+        if (o.ev0) cudaEventDestroy(o.ev0);
+        if (o.ev1) cudaEventDestroy(o.ev1);
+        o = RunSet();
+    }
+
     ~Engine() { release(); }
 
     void drop_graphs() {
@@ -133,6 +197,15 @@ struct Engine {
     }
 
     void release() {
+        free_set(alt);
+        for (Flight &f : flight) {
+            if (f.ev_up) cudaEventDestroy(f.ev_up);
+            if (f.ev_ext) cudaEventDestroy(f.ev_ext);
+            if (f.ev_dn) cudaEventDestroy(f.ev_dn);
+            f = Flight();
+        }
+        if (dn_st) cudaStreamDestroy(dn_st);
+        dn_st = nullptr;
         cudaFree(d_img); cudaFree(d_ist); cudaFree(d_chunk); cudaFree(d_tile_img);
         cudaFree(d_cap); cudaFree(d_exc); cudaFree(d_h); cudaFree(d_reach);
         cudaFree(d_tmask); cudaFree(d_tact); cudaFree(d_tpos);
@@ -827,24 +900,23 @@ static gcfg_status run_batch_graph(Engine &e, int n, const int *W, const int *H,
 // stream) overlap the data term and graph build of the groups already on the
 // device, and after the solve each group's extraction is followed by its
 // download while the next group is extracted.
-static gcfg_status run_batch_staged(Engine &e, int n, const int *W, const int *H, const double *lam,
-                                    const uint8_t *h_rgb, const uint8_t *h_scrib, uint8_t *h_smin,
-                                    uint8_t *h_smax, int64_t *flows, gcfg_result *res) {
-    GCFG_CK(cudaEventRecord(e.ev0, e.st));
-    GCFG_TRY(e.layout(n, W, H, lam, true, true));
-    GCFG_TRY(e.make_groups(n, W, H));
-    // the uploads overwrite buffers that earlier work on st may read
-    GCFG_CK(cudaEventRecord(e.ev_mark, e.st));
-    GCFG_CK(cudaStreamWaitEvent(e.cp_st, e.ev_mark, 0));
-    const int G = (int)e.groups.size();
-    for (int g = 0; g < G; ++g) {
+// Pieces of the host entry points for many images (the layout and groups
+// are in place): uploads of the groups' inputs on cp_st, each group's data
+// term and build on st as soon as its inputs are in, and per group the
+// extraction on st and the download of its labels on `out_st`.
+static gcfg_status stage_uploads(Engine &e, const uint8_t *h_rgb, const uint8_t *h_scrib) {
+    for (int g = 0; g < (int)e.groups.size(); ++g) {
         const Engine::Group &gr = e.groups[g];
         const size_t np = (size_t)(gr.p1 - gr.p0);
         GCFG_CK(cudaMemcpyAsync(e.d_rgb + 3 * gr.p0, h_rgb + 3 * gr.p0, 3 * np, cudaMemcpyHostToDevice, e.cp_st));
         GCFG_CK(cudaMemcpyAsync(e.d_scrib + gr.p0, h_scrib + gr.p0, np, cudaMemcpyHostToDevice, e.cp_st));
         GCFG_CK(cudaEventRecord(e.ev_in[g], e.cp_st));
     }
-    for (int g = 0; g < G; ++g) {
+    return GCFG_OK;
+}
+
+static gcfg_status stage_build(Engine &e) {
+    for (int g = 0; g < (int)e.groups.size(); ++g) {
         const Engine::Group &gr = e.groups[g];
         GCFG_CK(cudaStreamWaitEvent(e.st, e.ev_in[g], 0));
         DtArgs a = e.dt(e.d_rgb, e.d_scrib);
@@ -860,8 +932,11 @@ static gcfg_status run_batch_staged(Engine &e, int n, const int *W, const int *H
         b.n_tlist = gr.t1 - gr.t0;
         GCFG_TRY(dt_build(b, a, e.st));
     }
-    GCFG_TRY(e.solve());
-    for (int g = 0; g < G; ++g) {
+    return GCFG_OK;
+}
+
+static gcfg_status stage_extract(Engine &e, uint8_t *h_smin, uint8_t *h_smax, cudaStream_t out_st) {
+    for (int g = 0; g < (int)e.groups.size(); ++g) {
         const Engine::Group &gr = e.groups[g];
         Batch b = e.batch();
         b.tlist = e.d_iota + gr.t0;
@@ -869,11 +944,36 @@ static gcfg_status run_batch_staged(Engine &e, int n, const int *W, const int *H
         if (h_smin || h_smax)
             GCFG_TRY(launch_extract(b, h_smin ? e.d_smin : nullptr, h_smax ? e.d_smax : nullptr, nullptr, e.st));
         GCFG_CK(cudaEventRecord(e.ev_out[g], e.st));
-        GCFG_CK(cudaStreamWaitEvent(e.cp_st, e.ev_out[g], 0));
+        GCFG_CK(cudaStreamWaitEvent(out_st, e.ev_out[g], 0));
         const size_t np = (size_t)(gr.p1 - gr.p0);
-        if (h_smin) GCFG_CK(cudaMemcpyAsync(h_smin + gr.p0, e.d_smin + gr.p0, np, cudaMemcpyDeviceToHost, e.cp_st));
-        if (h_smax) GCFG_CK(cudaMemcpyAsync(h_smax + gr.p0, e.d_smax + gr.p0, np, cudaMemcpyDeviceToHost, e.cp_st));
+        if (h_smin) GCFG_CK(cudaMemcpyAsync(h_smin + gr.p0, e.d_smin + gr.p0, np, cudaMemcpyDeviceToHost, out_st));
+        if (h_smax) GCFG_CK(cudaMemcpyAsync(h_smax + gr.p0, e.d_smax + gr.p0, np, cudaMemcpyDeviceToHost, out_st));
     }
+    return GCFG_OK;
+}
+
+static void fill_results(const Engine &e, int n, float ms, int64_t *flows, gcfg_result *res) {
+    for (int i = 0; i < n; ++i) {
+        gcfg_result r;
+        e.result(i, &r, ms);
+        if (flows) flows[i] = r.flow;
+        if (res) res[i] = r;
+    }
+}
+
+static gcfg_status run_batch_staged(Engine &e, int n, const int *W, const int *H, const double *lam,
+                                    const uint8_t *h_rgb, const uint8_t *h_scrib, uint8_t *h_smin,
+                                    uint8_t *h_smax, int64_t *flows, gcfg_result *res) {
+    GCFG_CK(cudaEventRecord(e.ev0, e.st));
+    GCFG_TRY(e.layout(n, W, H, lam, true, true));
+    GCFG_TRY(e.make_groups(n, W, H));
+    // the uploads overwrite buffers that earlier work on st may read
+    GCFG_CK(cudaEventRecord(e.ev_mark, e.st));
+    GCFG_CK(cudaStreamWaitEvent(e.cp_st, e.ev_mark, 0));
+    GCFG_TRY(stage_uploads(e, h_rgb, h_scrib));
+    GCFG_TRY(stage_build(e));
+    GCFG_TRY(e.solve());
+    GCFG_TRY(stage_extract(e, h_smin, h_smax, e.cp_st));
     GCFG_TRY(e.readback());
     GCFG_CK(cudaEventRecord(e.ev_mark, e.cp_st));
     GCFG_CK(cudaStreamWaitEvent(e.st, e.ev_mark, 0));
@@ -881,18 +981,91 @@ static gcfg_status run_batch_staged(Engine &e, int n, const int *W, const int *H
     GCFG_CK(cudaStreamSynchronize(e.st));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e.ev0, e.ev1);
-    for (int i = 0; i < n; ++i) {
-        gcfg_result r;
-        e.result(i, &r, ms);
-        if (flows) flows[i] = r.flow;
-        if (res) res[i] = r;
-    }
+    fill_results(e, n, ms, flows, res);
     return e.status();
+}
+
+// Queue one batch of the asynchronous host entry point into the run set that
+// is swapped in.  That set's previous batch has been collected, so nothing in
+// flight reads its staging buffers or host tables.  The whole upload goes
+// first on cp_st, where it overlaps the compute of the batch before; the
+// batch then computes in one pass on st (data term, build, solve, extraction
+// over all its images, as the device-resident path does), and its labels are
+// downloaded on dn_st while the next batch computes.
+static gcfg_status submit_staged(Engine &e, Engine::Flight &f, int n, const int *W, const int *H, const double *lam,
+                                 const uint8_t *h_rgb, const uint8_t *h_scrib, uint8_t *h_smin, uint8_t *h_smax) {
+    GCFG_TRY(grow_host(e.h_ctl, e.ch_ctl, 1));
+    if (!e.ev0) GCFG_CK(cudaEventCreate(&e.ev0));
+    if (!e.ev1) GCFG_CK(cudaEventCreate(&e.ev1));
+    if (!e.cp_st) GCFG_CK(cudaStreamCreateWithFlags(&e.cp_st, cudaStreamNonBlocking));
+    if (!e.dn_st) GCFG_CK(cudaStreamCreateWithFlags(&e.dn_st, cudaStreamNonBlocking));
+    for (cudaEvent_t *ev : {&f.ev_up, &f.ev_ext, &f.ev_dn})
+        if (!*ev) GCFG_CK(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+    GCFG_CK(cudaEventRecord(e.ev0, e.st));
+    GCFG_TRY(e.layout(n, W, H, lam, true, true));
+    GCFG_CK(cudaMemcpyAsync(e.d_rgb, h_rgb, (size_t)e.n_px * 3, cudaMemcpyHostToDevice, e.cp_st));
+    GCFG_CK(cudaMemcpyAsync(e.d_scrib, h_scrib, (size_t)e.n_px, cudaMemcpyHostToDevice, e.cp_st));
+    GCFG_CK(cudaEventRecord(f.ev_up, e.cp_st));
+    GCFG_CK(cudaStreamWaitEvent(e.st, f.ev_up, 0));
+    GCFG_TRY(e.build_images(e.d_rgb, e.d_scrib));
+    GCFG_TRY(e.solve());
+    // the small read-back of the per-image states goes before the label
+    // download is queued: behind it on the copy engine it would stall st
+    GCFG_TRY(e.readback());
+    if (h_smin || h_smax)
+        GCFG_TRY(launch_extract(e.batch(), h_smin ? e.d_smin : nullptr, h_smax ? e.d_smax : nullptr, nullptr, e.st));
+    GCFG_CK(cudaEventRecord(f.ev_ext, e.st));
+    GCFG_CK(cudaStreamWaitEvent(e.dn_st, f.ev_ext, 0));
+    if (h_smin) GCFG_CK(cudaMemcpyAsync(h_smin, e.d_smin, (size_t)e.n_px, cudaMemcpyDeviceToHost, e.dn_st));
+    if (h_smax) GCFG_CK(cudaMemcpyAsync(h_smax, e.d_smax, (size_t)e.n_px, cudaMemcpyDeviceToHost, e.dn_st));
+    GCFG_CK(cudaEventRecord(e.ev1, e.st));
+    GCFG_CK(cudaEventRecord(f.ev_dn, e.dn_st));
+    return GCFG_OK;
+}
+
+static gcfg_status batch_submit(Engine &e, int n, const int *W, const int *H, const double *lam,
+                                const uint8_t *h_rgb, const uint8_t *h_scrib, uint8_t *h_smin, uint8_t *h_smax,
+                                int64_t *ticket) {
+    const int slot = e.next_slot;
+    Engine::Flight &f = e.flight[slot];
+    if (f.busy) return GCFG_ERR_STATE;  // two batches in flight already
+    if (slot == 1) e.swap_set(e.alt);
+    const gcfg_status rc = submit_staged(e, f, n, W, H, lam, h_rgb, h_scrib, h_smin, h_smax);
+    if (slot == 1) e.swap_set(e.alt);
+    if (rc != GCFG_OK) return rc;
+    f.busy = true;
+    f.n = n;
+    f.ticket = e.next_ticket++;
+    e.next_slot ^= 1;
+    *ticket = f.ticket;
+    return GCFG_OK;
+}
+
+static gcfg_status batch_wait(Engine &e, int64_t ticket, int64_t *flows, gcfg_result *res) {
+    int slot = -1;
+    for (int k = 0; k < 2; ++k)
+        if (e.flight[k].busy && e.flight[k].ticket == ticket) slot = k;
+    if (slot < 0) return GCFG_ERR_INVALID;
+    Engine::Flight &f = e.flight[slot];
+    f.busy = false;
+    if (slot == 1) e.swap_set(e.alt);
+    gcfg_status rc = GCFG_OK;
+    if (cudaEventSynchronize(f.ev_dn) != cudaSuccess || cudaEventSynchronize(e.ev1) != cudaSuccess) {
+        rc = GCFG_ERR_CUDA;
+    } else {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e.ev0, e.ev1);
+        fill_results(e, f.n, ms, flows, res);
+        rc = e.status();
+    }
+    if (slot == 1) e.swap_set(e.alt);
+    return rc;
 }
 
 static gcfg_status run_batch(Engine &e, int n, const int *W, const int *H, const double *lam,
                              const uint8_t *rgb, const uint8_t *scrib, uint8_t *smin, uint8_t *smax,
                              int64_t *flows, gcfg_result *res, bool staging) {
+    if (e.in_flight()) return GCFG_ERR_STATE;  // collect the asynchronous batches first
     if (staging && n > 1) return run_batch_staged(e, n, W, H, lam, rgb, scrib, smin, smax, flows, res);
     if (e.graph_on && !e.graph_broken && !prof_on())
         return run_batch_graph(e, n, W, H, lam, rgb, scrib, smin, smax, flows, res, staging);
@@ -958,6 +1131,7 @@ gcfg_status gcfg_batch_create(int max_images, int64_t max_pixels, gcfg_batch **o
 
 gcfg_status gcfg_batch_set_stream(gcfg_batch *b, void *stream) {
     if (!b) return GCFG_ERR_INVALID;
+    if (b->e.in_flight()) return GCFG_ERR_STATE;
     b->e.st = (cudaStream_t)stream;
     return GCFG_OK;
 }
@@ -1010,6 +1184,7 @@ gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const i
                                 const uint8_t *d_rgb, const uint8_t *d_scrib, int reps, gcfg_tuning *out) {
     if (!b || n < 1 || !widths || !heights || !lambdas || !d_rgb || !d_scrib || reps < 1) return GCFG_ERR_INVALID;
     Engine &e = b->e;
+    if (e.in_flight()) return GCFG_ERR_STATE;
     const bool graph = e.graph_on;
     e.graph_on = false;  // time the eager runs; the graph is recaptured afterwards
     e.drop_graphs();
@@ -1106,6 +1281,18 @@ gcfg_status gcfg_batch_run_host(gcfg_batch *b, int n, const int *widths, const i
                                 uint8_t *h_smin, uint8_t *h_smax, int64_t *h_flows, gcfg_result *h_res) {
     if (!b || n < 1 || !widths || !heights || !lambdas || !h_rgb || !h_scrib) return GCFG_ERR_INVALID;
     return run_batch(b->e, n, widths, heights, lambdas, h_rgb, h_scrib, h_smin, h_smax, h_flows, h_res, true);
+}
+
+gcfg_status gcfg_batch_submit_host(gcfg_batch *b, int n, const int *widths, const int *heights,
+                                   const double *lambdas, const uint8_t *h_rgb, const uint8_t *h_scrib,
+                                   uint8_t *h_smin, uint8_t *h_smax, int64_t *ticket) {
+    if (!b || n < 1 || !widths || !heights || !lambdas || !h_rgb || !h_scrib || !ticket) return GCFG_ERR_INVALID;
+    return batch_submit(b->e, n, widths, heights, lambdas, h_rgb, h_scrib, h_smin, h_smax, ticket);
+}
+
+gcfg_status gcfg_batch_wait(gcfg_batch *b, int64_t ticket, int64_t *h_flows, gcfg_result *h_res) {
+    if (!b) return GCFG_ERR_INVALID;
+    return batch_wait(b->e, ticket, h_flows, h_res);
 }
 
 gcfg_status gcfg_batch_destroy(gcfg_batch *b) {

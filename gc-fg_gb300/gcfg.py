@@ -37,7 +37,8 @@ EXPORTS = [
     "gcfg_tlinks", "gcfg_nlinks", "gcfg_seg_create", "gcfg_seg_run", "gcfg_seg_run_host",
     "gcfg_seg_set_stream", "gcfg_seg_destroy", "gcfg_strerror", "gcfg_launch_count",
     "gcfg_profile_enable", "gcfg_profile_read", "gcfg_batch_create", "gcfg_batch_set_stream",
-    "gcfg_batch_set_params", "gcfg_batch_run", "gcfg_batch_run_host", "gcfg_batch_destroy",
+    "gcfg_batch_set_params", "gcfg_batch_run", "gcfg_batch_run_host", "gcfg_batch_submit_host",
+    "gcfg_batch_wait", "gcfg_batch_destroy",
     "gcfg_solve_noalloc", "gcfg_batch_set_graph", "gcfg_batch_graph_info", "gcfg_batch_autotune",
     "gcfg_batch_set_solver",
     "gcfg_init8", "gcfg_set_dataterms8", "gcfg_set_edges8", "gcfg_set_penalty8", "gcfg_set_graph8",
@@ -123,6 +124,8 @@ def load(path: str = LIB_PATH):
         "gcfg_batch_set_params": (S, [P, I, I, I]),
         "gcfg_batch_run": (S, [P, I, P, P, P, P, P, P, P, P, P]),
         "gcfg_batch_run_host": (S, [P, I, P, P, P, P, P, P, P, P, P]),
+        "gcfg_batch_submit_host": (S, [P, I, P, P, P, P, P, P, P, P]),
+        "gcfg_batch_wait": (S, [P, C.c_int64, P, P]),
         "gcfg_batch_destroy": (S, [P]),
         "gcfg_batch_set_graph": (S, [P, I]),
         "gcfg_batch_graph_info": (S, [P, C.POINTER(I), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
@@ -349,6 +352,7 @@ class BatchSolver:
         _check(load().gcfg_batch_create(int(max_images), int(max_pixels), C.byref(h)),
                "gcfg_batch_create")
         self.handle = h
+        self._pending = {}  # ticket -> number of images
 
     def set_stream(self, stream):
         _check(load().gcfg_batch_set_stream(self.handle, _stream_ptr(stream)), "gcfg_batch_set_stream")
@@ -414,6 +418,29 @@ class BatchSolver:
         _check(load().gcfg_batch_run_host(self.handle, n, _ptr(w), _ptr(h), _ptr(lam), _ptr(h_rgb),
                                           _ptr(h_scrib), _ptr(h_smin), _ptr(h_smax), _ptr(flows),
                                           res), "gcfg_batch_run_host")
+        return flows, ([r.as_dict() for r in res] if results else None)
+
+    def submit_host(self, widths, heights, lambdas, h_rgb, h_scrib, h_smin=None, h_smax=None) -> int:
+        """Queue a batch from host memory (gcfg_batch_submit_host); returns its
+        ticket.  The host arrays must stay alive and unchanged until wait()."""
+        w, h, lam = self._arrays(widths, heights, lambdas)
+        ticket = C.c_int64(0)
+        # the size arrays are read during the call; the pixel buffers later
+        _check(load().gcfg_batch_submit_host(self.handle, len(w), _ptr(w), _ptr(h), _ptr(lam), _ptr(h_rgb),
+                                             _ptr(h_scrib), _ptr(h_smin), _ptr(h_smax), C.byref(ticket)),
+               "gcfg_batch_submit_host")
+        self._pending[ticket.value] = len(w)
+        return ticket.value
+
+    def wait(self, ticket, results=False):
+        """Collect a submitted batch: (flows int64[n], results or None)."""
+        import numpy as np
+        n = self._pending.pop(ticket, None)
+        if n is None:
+            raise GcfgError(GCFG_ERR_INVALID, f"gcfg_batch_wait (unknown ticket {ticket})")
+        flows = np.empty(n, np.int64)
+        res = (Result * n)() if results else None
+        _check(load().gcfg_batch_wait(self.handle, ticket, _ptr(flows), res), "gcfg_batch_wait")
         return flows, ([r.as_dict() for r in res] if results else None)
 
     def close(self):

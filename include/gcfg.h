@@ -281,6 +281,20 @@ gcfg_status gcfg_batch_run_host(gcfg_batch *b, int n, const int *widths, const i
                                 const double *lambdas, const uint8_t *h_rgb, const uint8_t *h_scrib,
                                 uint8_t *h_smin, uint8_t *h_smax, int64_t *h_flows,
                                 gcfg_result *h_res);
+/* Asynchronous form of gcfg_batch_run_host for a stream of batches: queue a
+ * batch and return at once with a ticket; gcfg_batch_wait(ticket) blocks
+ * until its labels are in h_smin/h_smax and fills h_flows/h_res as
+ * gcfg_batch_run_host does.  Up to two batches are in flight per handle:
+ * while one computes, the next one's inputs are uploaded and the previous
+ * one's labels are downloaded.  The host buffers of a batch (pinned memory
+ * for the copies to overlap) must stay valid and unchanged until its wait
+ * returns.  A third submit before a wait, and any other run, autotune or
+ * set_stream call while batches are in flight, return GCFG_ERR_STATE; an
+ * unknown ticket GCFG_ERR_INVALID.  Tickets may be collected in any order. */
+gcfg_status gcfg_batch_submit_host(gcfg_batch *b, int n, const int *widths, const int *heights,
+                                   const double *lambdas, const uint8_t *h_rgb, const uint8_t *h_scrib,
+                                   uint8_t *h_smin, uint8_t *h_smax, int64_t *ticket);
+gcfg_status gcfg_batch_wait(gcfg_batch *b, int64_t ticket, int64_t *h_flows, gcfg_result *h_res);
 gcfg_status gcfg_batch_destroy(gcfg_batch *b);
 
 /* CUDA graph replay (off by default).  When on, the device part of a run
