@@ -18,6 +18,8 @@
 // of every pixel pair is evaluated directly; both use a float evaluation
 // whenever it is provably far from a rounding boundary and the oracle's
 // double expression otherwise, so every int32 capacity matches bit for bit.
+#include <cstring>
+
 #include "dataterm.cuh"
 
 namespace gcfg {
@@ -47,18 +49,6 @@ __device__ __forceinline__ int color_binw(uint32_t c) {
     return (((c >> 4) & 0xFu) << 8) | (((c >> 12) & 0xFu) << 4) | ((c >> 20) & 0xFu);
 }
 
-// Image of a global chunk index (chunk_off: prefix sums of chunks per image).
-__device__ __forceinline__ int chunk_image(const long long *__restrict__ chunk_off, int n_img,
-                                           long long chunk) {
-    int lo = 0, hi = n_img - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(chunk_off + mid) <= chunk) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
 // ---------------------------------------------------------------------------
 // Quantised table entries.  The reference value is the double expression
 // the CPU oracle evaluates; a float evaluation decides the rounding whenever
@@ -85,16 +75,21 @@ __device__ __forceinline__ int tlink_quant(int h, long long N) {
     return (int)round(tlink_raw(h, N));
 }
 
-// round(lambda * exp(-d2 / (2 s2))).  Float error of v = lf * expf(a),
-// a = -d2 * inv: d2 is exact; inv = (float)(1 / (2 s2)) and the product each
-// round once, so a is off by <= 2^-23 |a| (1.2e-7 |a|); expf adds <= 2 ulp
-// (2.4e-7), lf = (float)lambda and the final product <= 0.5 ulp each
-// (1.2e-7): v is off by < v * 1.2e-7 * (|a| + 3).  A wrong rounding needs v
-// within that error of some k + 0.5, where v <= lambda and
-// |a| = ln(lambda / (k + 0.5)) <= ln(2 lambda): the error is then
-// < lambda * 1.2e-7 * (ln(2 lambda) + 3).  The margin used is about twice
-// that: lambda * 2.5e-7 * (ln(2 lambda + 1) + 4) + 1e-6, set per image.
-// (Large |a| only make v smaller: it underflows toward 0 and rounds to 0.)
+// round(lambda * exp(-d2 / (2 s2))).  The fast path evaluates
+// v = lf * 2^z, z = -d2 * scale, scale = (float)(log2(e) / (2 s2)), with one
+// ex2.approx.ftz.f32 (the hardware base-2 exponential; PTX documents a
+// maximum relative error of about 2^-22, and gcfg_selftest_ex2 measures it
+// over [-64, 0] on the device, where the tests require <= 2^-21).  Error of
+// v: d2 is exact; scale and the product round once each, so z is off by
+// <= 2^-23 |z|, i.e. 2^z by a relative 1.2e-7 |a| with a = z ln 2 the
+// natural exponent; ex2 adds <= 2^-21 (4.8e-7); lf = (float)lambda and the
+// final product <= 0.5 ulp each (1.2e-7): v is off by < v * (1.2e-7 |a| +
+// 7.2e-7).  A wrong rounding needs v within that error of some k + 0.5,
+// where v <= lambda and |a| = ln(lambda / (k + 0.5)) <= ln(2 lambda): the
+// error is then < lambda * (1.2e-7 ln(2 lambda) + 7.2e-7).  The margin used
+// is about twice that: lambda * (2.5e-7 ln(2 lambda + 1) + 1.5e-6) + 1e-6,
+// set per image.  Within the margin the double expression decides.  (Large
+// |a| only make v smaller: it underflows toward 0 and rounds to 0.)
 //
 // The fast path uses no conversion instructions (they share a slow pipe on
 // this GPU): d2 < 2^23 becomes a float by writing it into the mantissa of
@@ -103,7 +98,7 @@ __device__ __forceinline__ int tlink_quant(int h, long long N) {
 // v is at distance 0.5 - |v - rint(v)| from the nearest k + 0.5, so the
 // margin test reads |v - rint(v)| < 0.5 - margin.
 struct NlinkParams {
-    float lf, inv;       // (float)lambda, (float)(1 / (2 sigma^2))
+    float lf, scale;     // (float)lambda, (float)(log2(e) / (2 sigma^2))
     float margin;        // per image, from the error bound above
     float half_margin;   // 0.5 - margin
     int small;           // lambda < 2^22: the magic-number rounding applies
@@ -129,11 +124,11 @@ __global__ void k_img_params(const int *__restrict__ ilist, const ImgDesc *__res
     const long long count = (long long)(img[im].W - 1) * img[im].H + (long long)img[im].W * (img[im].H - 1);
     const double s2 = (s == 0 || count == 0) ? 0.0 : (double)s / (double)count;
     ist[im].s2 = s2;
-    ist[im].inv2s2 = s2 > 0.0 ? (float)(1.0 / (2.0 * s2)) : 0.f;
+    ist[im].ex2_scale = s2 > 0.0 ? (float)(1.4426950408889634 / (2.0 * s2)) : 0.f;  // log2(e) / (2 s2)
     ist[im].lambda_f = (float)img[im].lambda;
     ist[im].const_w = (int)round(img[im].lambda);
     const double lam = img[im].lambda;
-    ist[im].nl_margin = (float)(lam * 2.5e-7 * (log(2.0 * lam + 1.0) + 4.0) + 1e-6);
+    ist[im].nl_margin = (float)(lam * (2.5e-7 * log(2.0 * lam + 1.0) + 1.5e-6) + 1e-6);
 }
 
 __device__ __forceinline__ NlinkParams nlink_params(double lambda, const ImgState &st) {
@@ -141,8 +136,8 @@ __device__ __forceinline__ NlinkParams nlink_params(double lambda, const ImgStat
     q.lambda = lambda;
     q.s2 = st.s2;
     q.lf = st.lambda_f;
-    q.inv = st.inv2s2;
-    q.constant = st.inv2s2 == 0.f;
+    q.scale = st.ex2_scale;
+    q.constant = st.ex2_scale == 0.f;
     q.const_w = st.const_w;
     q.margin = st.nl_margin;
     q.half_margin = 0.5f - q.margin;
@@ -155,8 +150,14 @@ __device__ __forceinline__ float small_int_to_float(int d2) {
     return __fsub_rn(__int_as_float(0x4B000000 | d2), 8388608.0f);
 }
 
+__device__ __forceinline__ float ex2_approx(float z) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(z));
+    return r;
+}
+
 __device__ __forceinline__ int nlink_quant(int d2, const NlinkParams &q) {
-    const float v = q.lf * expf(-small_int_to_float(d2) * q.inv);
+    const float v = q.lf * ex2_approx(-small_int_to_float(d2) * q.scale);
     if (q.small) {
         const float t = __fadd_rn(v, 12582912.0f);  // 1.5 * 2^23 + rint(v)
         const float rf = __fsub_rn(t, 12582912.0f);
@@ -168,23 +169,130 @@ __device__ __forceinline__ int nlink_quant(int d2, const NlinkParams &q) {
     return nlink_exact(d2, q.lambda, q.s2);
 }
 
-// One pass over a chunk of an image: the scribble colour histograms
-// (privatised per block in shared memory, equal bins of a warp aggregated
-// with __match_any_sync before the shared atomics) and the exact sum of
-// ||dI||^2 over right and down neighbour pairs (for sigma^2).
+// Aligned 32-bit word at a (a % 4 == 0) of the byte range [lo, hi): one load
+// when the word lies inside, else the bytes inside and zeros elsewhere.
+__device__ __forceinline__ uint32_t word_in(uintptr_t a, uintptr_t lo, uintptr_t hi) {
+    if (a >= lo && a + 4 <= hi) return __ldg(reinterpret_cast<const uint32_t *>(a));
+    uint32_t w = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (a + k >= lo && a + k < hi) w |= (uint32_t)__ldg(reinterpret_cast<const uint8_t *>(a + k)) << (8 * k);
+    return w;
+}
+
+// The same for an aligned 16-byte vector (a % 16 == 0).
+__device__ __forceinline__ uint4 vec_in(uintptr_t a, uintptr_t lo, uintptr_t hi) {
+    if (a >= lo && a + 16 <= hi) return __ldg(reinterpret_cast<const uint4 *>(a));
+    return make_uint4(word_in(a, lo, hi), word_in(a + 4, lo, hi), word_in(a + 8, lo, hi), word_in(a + 12, lo, hi));
+}
+
+// Bytes b of a word whose offsets o + b fall in [k0, k1) (32-bit offsets).
+__device__ __forceinline__ uint32_t byte_mask(int o, int k0, int k1) {
+    const int f = k0 - o, l = k1 - o;  // first and one-past-last valid byte
+    const uint32_t upto_l = l <= 0 ? 0u : l >= 4 ? 0xFFFFFFFFu : (1u << (8 * l)) - 1u;
+    const uint32_t upto_f = f <= 0 ? 0u : f >= 4 ? 0xFFFFFFFFu : (1u << (8 * f)) - 1u;
+    return upto_l & ~upto_f;
+}
+
+__device__ __forceinline__ uint32_t sq4(uint32_t a, uint32_t b) {
+    const uint32_t d = __vabsdiffu4(a, b);
+    return __dp4a(d, d, 0u);
+}
+
+// Sum over the byte pairs of one chunk (see k_hist_sigma_b).  The chunk's
+// bytes are offsets [0, L) relative to `c0` (its first byte); a lane takes
+// the aligned 16-byte vector at aw + 16 v, v = lane, lane + 32, ...: its
+// right partners (bytes + 3) come from itself and the next lane's first
+// word, its down partners (bytes + 3W) from the two vectors at
+// + (3W rounded down to 16) shifted by (3W mod 16) bytes: WS whole words
+// and BS bytes, WS fixed per instantiation.  Byte k pairs right when
+// k < kh and down when k < kv (chunk-relative).
+template <int WS>
+__device__ __forceinline__ uint32_t sigma_chunk(uintptr_t lo, uintptr_t hi, uintptr_t c0, uintptr_t aw, int nvec,
+                                                uintptr_t vstep, int bs, int kh, int kv, uint4 *keep) {
+    const int lane = threadIdx.x & 31;
+    uint32_t acc = 0;  // at most 4 vectors of 32 pairs of 65025 per thread
+    for (int v0 = (int)threadIdx.x - lane; v0 < nvec; v0 += blockDim.x) {  // warp-uniform trip count
+        const int vi = v0 + lane;
+        const uintptr_t a = aw + 16 * (uintptr_t)vi;
+        // every lane loads (a lane past the end supplies its neighbour's next
+        // vector); bytes outside the image read as 0
+        uint4 c, u, u31 = make_uint4(0, 0, 0, 0);
+        uint32_t c31 = 0;
+        if (a >= lo && a + vstep + 32 <= hi) {
+            c = __ldg(reinterpret_cast<const uint4 *>(a));
+            u = __ldg(reinterpret_cast<const uint4 *>(a + vstep));
+            if (lane == 31) {
+                c31 = __ldg(reinterpret_cast<const uint32_t *>(a + 16));
+                u31 = __ldg(reinterpret_cast<const uint4 *>(a + vstep + 16));
+            }
+        } else {
+            c = vec_in(a, lo, hi);
+            u = vec_in(a + vstep, lo, hi);
+            if (lane == 31) {
+                c31 = word_in(a + 16, lo, hi);
+                u31 = vec_in(a + vstep + 16, lo, hi);
+            }
+        }
+        uint32_t n0 = __shfl_down_sync(0xffffffffu, c.x, 1);
+        uint32_t un[4];
+        un[0] = __shfl_down_sync(0xffffffffu, u.x, 1);
+        un[1] = WS >= 1 ? __shfl_down_sync(0xffffffffu, u.y, 1) : 0u;
+        un[2] = WS >= 2 ? __shfl_down_sync(0xffffffffu, u.z, 1) : 0u;
+        un[3] = WS >= 3 ? __shfl_down_sync(0xffffffffu, u.w, 1) : 0u;
+        if (lane == 31) {
+            n0 = c31;
+            un[0] = u31.x;
+            un[1] = u31.y;
+            un[2] = u31.z;
+            un[3] = u31.w;
+        }
+        if (vi < nvec) {
+            keep[vi] = c;  // the chunk's colours, for the histogram pass
+            const uint32_t cw[4] = {c.x, c.y, c.z, c.w};
+            const uint32_t hw[5] = {c.x, c.y, c.z, c.w, n0};
+            const uint32_t vw[8] = {u.x, u.y, u.z, u.w, un[0], un[1], un[2], un[3]};
+            const int o = (int)(a - c0);  // chunk-relative offset of the vector's byte 0
+            const bool full = o >= 0 && o + 16 <= kh && o + 16 <= kv;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                uint32_t dh = __vabsdiffu4(cw[j], __funnelshift_r(hw[j], hw[j + 1], 24));
+                uint32_t dv = __vabsdiffu4(cw[j], __funnelshift_r(vw[j + WS], vw[j + WS + 1], bs));
+                if (!full) {
+                    dh &= byte_mask(o + 4 * j, 0, kh);
+                    dv &= byte_mask(o + 4 * j, 0, kv);
+                }
+                acc += __dp4a(dh, dh, 0u) + __dp4a(dv, dv, 0u);
+            }
+        }
+    }
+    return acc;
+}
+
+// One pass over a chunk of an image (CHUNK_PX consecutive pixels, row-major):
+// the exact sum of ||dI||^2 over right and down neighbour pairs (for sigma^2)
+// and the scribble colour histograms (privatised per block in shared memory,
+// equal bins of a warp aggregated with __match_any_sync before the shared
+// atomics).
+//
+// The sum runs on the image's byte stream B (3 bytes per pixel, row-major):
+// right pairs = sum of (B[k] - B[k + 3])^2 over the chunk's bytes k with
+// k + 3 inside the image, minus the pairs that straddle a row end; down pairs
+// = sum of (B[k] - B[k + 3W])^2 over the chunk's bytes above the image's last
+// row.  Per 4 bytes: one __vabsdiffu4 + __dp4a for each direction.
 __global__ void __launch_bounds__(256) k_hist_sigma_b(const uint8_t *__restrict__ rgb,
                                                       const uint8_t *__restrict__ scrib,
                                                       const ImgDesc *__restrict__ img,
-                                                      const long long *__restrict__ chunk_off, int n_img,
-                                                      const int *__restrict__ ilist, int *__restrict__ hist,
-                                                      ImgState *ist) {
+                                                      const int2 *__restrict__ chunk_map,
+                                                      int *__restrict__ hist, ImgState *ist) {
     __shared__ __align__(16) int sh[2 * NBINS];
-    const int li = chunk_image(chunk_off, n_img, blockIdx.x);
-    const int im = ilist ? ilist[li] : li;
+    __shared__ uint4 keep[(3 * CHUNK_PX + 15) / 16 + 1];  // the chunk's bytes from its 16-aligned start
+    const int2 cm = __ldg(chunk_map + blockIdx.x);  // (image, chunk within the image)
+    const int im = cm.x;
     const int W = img[im].W, H = img[im].H;
-    const int rows = img[im].rows_per_chunk;
-    const int y0 = (int)((long long)blockIdx.x - chunk_off[li]) * rows;
-    const int y1 = min(H, y0 + rows);
+    const long long npx = (long long)W * H;
+    const long long p0 = (long long)cm.y * CHUNK_PX;
+    const int n = (int)min((long long)CHUNK_PX, npx - p0);  // pixels of the chunk
     const long long pix0 = img[im].pix0;
     const uint8_t *base = rgb + 3 * pix0;
     const bool do_hist = scrib != nullptr;
@@ -192,55 +300,73 @@ __global__ void __launch_bounds__(256) k_hist_sigma_b(const uint8_t *__restrict_
         int4 *s4 = reinterpret_cast<int4 *>(sh);
         for (int i = threadIdx.x; i < 2 * NBINS / 4; i += blockDim.x) s4[i] = make_int4(0, 0, 0, 0);
     }
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
     unsigned long long acc = 0;
-    // Items are (row, 32-column group) pairs of the chunk in row-major order;
-    // warp w takes items w, w + 8, ...  Two items' loads are issued before
-    // either is used.  Loop bounds are warp-uniform (full-warp collectives).
-    const int nw = blockDim.x >> 5;
-    const int ncg = (W + 31) >> 5;
-    const int items = (y1 - y0) * ncg;
-    int k = warp, y = y0 + warp / ncg, cg = warp % ncg;
-    constexpr int U = 2;
-    while (k < items) {
-        uint32_t c[U], dn[U], r31[U];
-        int sc[U], ys[U], xs[U];
-        bool ok[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            ok[u] = k < items;
-            const int x = cg * 32 + lane;
-            ys[u] = y;
-            xs[u] = x;
-            const bool in = ok[u] && x < W;
-            const long long i = (long long)y * W + x;
-            const uint8_t *p = base + 3 * i;
-            c[u] = in ? pack_rgb(p) : 0u;
-            dn[u] = (in && y + 1 < H) ? pack_rgb(p + 3 * (long long)W) : 0u;
-            r31[u] = (lane == 31 && in && x + 1 < W) ? pack_rgb(p + 3) : 0u;
-            sc[u] = (do_hist && in) ? (int)__ldg(scrib + pix0 + i) : 0;
-            k += nw;
-            cg += nw;
-            while (cg >= ncg) {
-                cg -= ncg;
-                ++y;
-            }
+    {
+        const long long W3 = 3LL * W, b0 = 3 * p0;
+        const uintptr_t lo = (uintptr_t)base, hi = lo + (uintptr_t)(3 * npx);
+        const uintptr_t c0 = lo + (uintptr_t)b0;
+        const uintptr_t aw = c0 & ~(uintptr_t)15;
+        const int L = 3 * n;
+        const int nvec = (int)((c0 + L - aw + 15) >> 4);
+        // chunk-relative limits: k + 3 inside the image; k + 3W inside the image
+        const int kh = (int)min((long long)L, 3 * npx - 3 - b0);
+        const int kv = (int)max(-1LL, min((long long)L, 3 * npx - W3 - b0));
+        const uintptr_t vstep = (uintptr_t)(W3 & ~15LL);
+        const int rem = (int)(W3 & 15);
+        const int bs = (rem & 3) * 8;
+        switch (rem >> 2) {
+            case 0: acc = sigma_chunk<0>(lo, hi, c0, aw, nvec, vstep, bs, kh, kv, keep); break;
+            case 1: acc = sigma_chunk<1>(lo, hi, c0, aw, nvec, vstep, bs, kh, kv, keep); break;
+            case 2: acc = sigma_chunk<2>(lo, hi, c0, aw, nvec, vstep, bs, kh, kv, keep); break;
+            default: acc = sigma_chunk<3>(lo, hi, c0, aw, nvec, vstep, bs, kh, kv, keep); break;
         }
+        // right pairs that straddle a row end: rows y whose last pixel lies in
+        // the chunk, below which another row follows
+        const long long ya = (p0 + W) / W - 1, yb = min((p0 + n) / W - 1, (long long)H - 2);
+        for (long long y = ya + threadIdx.x; y <= yb; y += blockDim.x) {
+            const long long e = (y + 1) * W;  // first pixel of row y + 1
+            acc -= sq4(pack_rgb(base + 3 * (e - 1)), pack_rgb(base + 3 * e));
+        }
+    }
+    if (do_hist) {
+        __syncthreads();  // the cleared histogram and the kept colours
+        const uint8_t *kb = reinterpret_cast<const uint8_t *>(keep) + (int)(((uintptr_t)base + 3 * p0) & 15);
+        // the chunk's scribble bytes, 16 per lane; scribbled pixels are
+        // binned one byte position per round, as long as any lane has one left
+        const uintptr_t slo = (uintptr_t)(scrib + pix0), shi = slo + (uintptr_t)npx;
+        const uintptr_t s0 = slo + (uintptr_t)p0;
+        const uintptr_t saw = s0 & ~(uintptr_t)15;
+        const int nsv = (int)((s0 + n - saw + 15) >> 4);
+        for (int v0 = (int)threadIdx.x - lane; v0 < nsv; v0 += blockDim.x) {
+            const int vi = v0 + lane;
+            const uintptr_t a = saw + 16 * (uintptr_t)vi;
+            uint4 sv = vi < nsv ? vec_in(a, slo, shi) : make_uint4(0, 0, 0, 0);
+            const uint32_t sw[4] = {sv.x, sv.y, sv.z, sv.w};
+            unsigned todo = 0;  // bit b: byte b is a scribble (1 or 2) of this chunk
+            const int o = (int)(a - s0);
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            if (!ok[u]) break;  // warp-uniform
-            const int x = xs[u];
-            uint32_t right = __shfl_down_sync(0xffffffffu, c[u], 1);
-            if (lane == 31) right = r31[u];
-            int key = -1;
-            if (x < W) {
-                if (x + 1 < W) acc += (unsigned)diff2w(c[u], right);
-                if (ys[u] + 1 < H) acc += (unsigned)diff2w(c[u], dn[u]);
-                if (sc[u] == 1 || sc[u] == 2) key = (sc[u] - 1) * NBINS + color_binw(c[u]);
+            for (int j = 0; j < 4; ++j) {
+                uint32_t w = sw[j];
+                if (w) w &= byte_mask(o + 4 * j, 0, n);
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    const uint32_t sc = (w >> (8 * b)) & 0xFFu;
+                    if (sc == 1u || sc == 2u) todo |= 1u << (4 * j + b);
+                }
             }
-            // most warps hold no scribbled pixel: skip the bin matching there
-            if (do_hist && __ballot_sync(0xffffffffu, key >= 0)) {
+            while (__any_sync(0xffffffffu, todo != 0)) {
+                int key = -1;
+                if (todo) {
+                    const int b = __ffs(todo) - 1;
+                    todo &= todo - 1;
+                    const uint32_t wb = b < 8 ? (b < 4 ? sv.x : sv.y) : (b < 12 ? sv.z : sv.w);
+                    const int sc = (int)((wb >> (8 * (b & 3))) & 0xFFu);
+                    const int q = o + b;  // pixel of the chunk
+                    const uint32_t col = (uint32_t)kb[3 * q] | ((uint32_t)kb[3 * q + 1] << 8) |
+                                         ((uint32_t)kb[3 * q + 2] << 16);
+                    key = (sc - 1) * NBINS + color_binw(col);
+                }
                 const unsigned same = __match_any_sync(0xffffffffu, key);
                 if (key >= 0 && lane == __ffs(same) - 1) atomicAdd(&sh[key], __popc(same));
             }
@@ -351,20 +477,66 @@ __global__ void __launch_bounds__(TILE_THREADS) k_build_img_b(Batch b, const uin
     const int *dnl = dn_lut + (size_t)im * NBINS;
     const uint8_t *base = rgb + 3 * d.pix0;
 
-    constexpr int STAGE = (SH * SW + TILE_THREADS - 1) / TILE_THREADS;
-    uint32_t cv[STAGE];
+    // Stage the 34 rows of 34 pixels (tile + 1-pixel halo) as packed colours.
+    // A row's bytes are fetched as aligned 32-bit words, one per lane (at
+    // most 27), instead of three byte loads per pixel; a word that reaches
+    // outside this image's bytes is assembled from the bytes inside.  Each
+    // pixel is then cut out of two adjacent words with a funnel shift.
+    {
+        constexpr int RAWW = 28;
+        __shared__ uint32_t raw[SH][RAWW];
+        __shared__ int phase[SH];
+        const uintptr_t lo = (uintptr_t)base, hi = lo + 3 * (uintptr_t)W * (uintptr_t)H;
+        const int xs = x0 > 0 ? x0 - 1 : 0;
+        const int xe = x0 + TILE_W < W ? x0 + TILE_W : W - 1;
+        constexpr int NW = TILE_THREADS / 32, RPW = (SH + NW - 1) / NW;  // rows per warp
+        uint32_t words[RPW];
+        int phs[RPW];
 #pragma unroll
-    for (int u = 0; u < STAGE; ++u) {  // every load first, then the stores
-        const int k = threadIdx.x + u * TILE_THREADS;
-        const int i = k / SW, j = k - i * SW;
-        const int x = x0 - 1 + j, y = y0 - 1 + i;
-        cv[u] = (k < SH * SW && x >= 0 && y >= 0 && x < W && y < H) ? pack_rgb(base + 3 * ((long long)y * W + x))
-                                                                    : 0u;
-    }
+        for (int r = 0; r < RPW; ++r) {  // every load first, then the stores
+            const int i = warp + NW * r;
+            const int y = y0 - 1 + i;
+            uint32_t word = 0;
+            int ph = 0;
+            if (i < SH && y >= 0 && y < H) {
+                const uintptr_t a0 = lo + 3 * ((uintptr_t)y * W + xs);
+                const uintptr_t a1 = lo + 3 * ((uintptr_t)y * W + xe) + 3;
+                const uintptr_t aw = a0 & ~(uintptr_t)3;
+                ph = (int)(a0 - aw);
+                if (lane < (int)((a1 - aw + 3) >> 2)) {
+                    const uintptr_t wa = aw + 4 * (uintptr_t)lane;
+                    if (wa >= lo && wa + 4 <= hi) {
+                        word = __ldg(reinterpret_cast<const uint32_t *>(wa));
+                    } else {
 #pragma unroll
-    for (int u = 0; u < STAGE; ++u) {
-        const int k = threadIdx.x + u * TILE_THREADS;
-        if (k < SH * SW) col[k / SW][k % SW] = cv[u];
+                        for (int k = 0; k < 4; ++k)
+                            if (wa + k >= lo && wa + k < hi)
+                                word |= (uint32_t)__ldg(reinterpret_cast<const uint8_t *>(wa + k)) << (8 * k);
+                    }
+                }
+            }
+            words[r] = word;
+            phs[r] = ph;
+        }
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) {
+            const int i = warp + NW * r;
+            if (i < SH) {
+                if (lane < RAWW) raw[i][lane] = words[r];
+                if (lane == 0) phase[i] = phs[r];
+            }
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < SH * SW; k += TILE_THREADS) {
+            const int i = k / SW, j = k - i * SW;
+            const int x = x0 - 1 + j, y = y0 - 1 + i;
+            uint32_t v = 0;
+            if (x >= 0 && y >= 0 && x < W && y < H) {
+                const int off = phase[i] + 3 * (x - xs);
+                v = __funnelshift_r(raw[i][off >> 2], raw[i][(off >> 2) + 1], (off & 3) * 8) & 0xFFFFFFu;
+            }
+            col[i][j] = v;
+        }
     }
     __syncthreads();
     // 2048 edges inside the tile's rows and columns, 8 per thread (right
@@ -482,8 +654,8 @@ gcfg_status dt_tables(const DtArgs &a, cudaStream_t st) {
     // (with an image list the caller clears the histograms of those images)
     if (a.scrib && !a.ilist) GCFG_CK(cudaMemsetAsync(a.hist, 0, (size_t)a.n_img * 2 * NBINS * sizeof(int), st));
     GCFG_LAUNCH(GCFG_PK_HIST, st,
-                k_hist_sigma_b<<<a.total_chunks, 256, 0, st>>>(a.rgb, a.scrib, a.img, a.chunk_off, a.n_img,
-                                                               a.ilist, a.hist, a.ist));
+                k_hist_sigma_b<<<a.total_chunks, 256, 0, st>>>(a.rgb, a.scrib, a.img, a.chunk_map, a.hist,
+                                                               a.ist));
     GCFG_LAUNCH(GCFG_PK_TLUT, st, k_img_params<<<div_up(a.n_img, 128), 128, 0, st>>>(a.ilist, a.img, a.n_img, a.ist));
     if (a.scrib)
         GCFG_LAUNCH(GCFG_PK_TLUT, st,
@@ -515,4 +687,38 @@ gcfg_status dt_apply_nlinks(const DtArgs &a, int W, int H, int *up, int *down, i
     return GCFG_OK;
 }
 
+// Largest relative error of ex2_approx against the double 2^z over n
+// evenly spaced z in [-64, 0] (the n-link fast path's error bound assumes
+// <= 2^-21).  Relative errors are non-negative floats, so their bit
+// patterns order like the values and an integer atomicMax finds the largest.
+__global__ void k_selftest_ex2(long long n, int *max_bits) {
+    float worst = 0.f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float z = -64.0f * (float)((double)i / (double)n);
+        const double ref = exp2((double)z);
+        const double rel = fabs((double)ex2_approx(z) - ref) / ref;
+        worst = fmaxf(worst, (float)rel);
+    }
+    atomicMax(max_bits, __float_as_int(worst));
+}
+
 }  // namespace gcfg
+
+extern "C" gcfg_status gcfg_selftest_ex2(int64_t samples, float *max_rel_err) {
+    using namespace gcfg;
+    if (samples < 1 || !max_rel_err) return GCFG_ERR_INVALID;
+    int *d = nullptr;
+    if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return GCFG_ERR_OOM;
+    int bits = 0;
+    cudaError_t e = cudaMemset(d, 0, sizeof(int));
+    if (e == cudaSuccess) {
+        k_selftest_ex2<<<1024, 256>>>((long long)samples, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(&bits, d, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return GCFG_ERR_CUDA;
+    memcpy(max_rel_err, &bits, sizeof(float));
+    return GCFG_OK;
+}

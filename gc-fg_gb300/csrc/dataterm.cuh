@@ -9,7 +9,9 @@ constexpr int NBINS = 4096;                   // 16^3 colour bins per class
 constexpr int CHUNK_PX = 4096;                // pixels per block in per-image passes (about)
 
 // Rows of a W-wide image per block of the histogram / sigma pass.
-inline int rows_per_chunk(int W) { return W >= CHUNK_PX ? 1 : CHUNK_PX / W; }
+// Blocks of the per-image pass over an image: CHUNK_PX consecutive pixels
+// (row-major) each, the last one shorter.
+inline long long image_chunks(int W, int H) { return ((long long)W * H + CHUNK_PX - 1) / CHUNK_PX; }
 
 // Device buffers of the data term for a batch (per image: 2*4096 histogram
 // bins, 4096 dp and dn entries).
@@ -21,7 +23,7 @@ struct DtArgs {
     const uint8_t *scrib;     // packed row-major scribbles (0 none, 1 fg, 2 bg)
     const ImgDesc *img;
     ImgState *ist;
-    const long long *chunk_off;
+    const int2 *chunk_map;    // per chunk of the pass: (image index, chunk index within the image)
     int *hist;
     int *dp_lut, *dn_lut;
     double *raw_dp, *raw_dn;  // optional (NULL): pre-rounding per-bin values

@@ -26,8 +26,6 @@ struct ImgDesc {
     int tile0, n_tiles;
     long long pix0;   // offset of the image in packed row-major inputs/outputs
     double lambda;
-    int rows_per_chunk;  // rows of the image per block in the per-image passes
-    int pad;
     long long out0;   // offset of the image in the packed output label arrays
 };
 
@@ -39,7 +37,7 @@ struct ImgState {
     unsigned long long active;       // active nodes (last count)
     unsigned long long sigma_sum;    // sum of ||dI||^2 over neighbour pairs
     double s2;                       // sigma^2 = sigma_sum / pairs (0: constant image)
-    float inv2s2;                    // (float)(1 / (2 sigma^2))
+    float ex2_scale;                 // (float)(log2(e) / (2 sigma^2)); 0: constant image
     float lambda_f;                  // (float)lambda
     int const_w;                     // round(lambda): every weight of a constant image
     int done;

@@ -50,7 +50,7 @@ struct Engine {
     // device
     ImgDesc *d_img = nullptr; size_t c_img = 0;
     ImgState *d_ist = nullptr; size_t c_ist = 0;
-    long long *d_chunk = nullptr; size_t c_chunk = 0;
+    int2 *d_cmap = nullptr; size_t c_cmap = 0;  // per chunk of the data-term pass: (image, chunk in image)
     int *d_tile_img = nullptr; size_t c_timg = 0;
     int4 *d_cap = nullptr; size_t c_cap = 0;
     int *d_exc = nullptr; size_t c_exc = 0;
@@ -75,7 +75,8 @@ struct Engine {
     // host (pinned)
     ImgDesc *h_img = nullptr; size_t ch_img = 0;
     ImgState *h_ist = nullptr; size_t ch_ist = 0;
-    long long *h_chunk = nullptr; size_t ch_chunk = 0;
+    long long *h_chunk = nullptr; size_t ch_chunk = 0;  // first chunk of each image
+    int2 *h_cmap = nullptr; size_t ch_cmap = 0;
     int *h_tile_img = nullptr; size_t ch_timg = 0;
     Ctl *h_ctl = nullptr; size_t ch_ctl = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -113,8 +114,6 @@ struct Engine {
     cudaStream_t cp_st = nullptr;
     cudaEvent_t ev_in[MAX_GROUPS] = {}, ev_out[MAX_GROUPS] = {}, ev_mark = nullptr;
     int *d_iota = nullptr; size_t c_iota = 0; int iota_n = 0;   // 0, 1, 2, ... (image and tile lists)
-    long long *d_gchunk = nullptr; size_t c_gchunk = 0;         // group-relative chunk offsets
-    long long *h_gchunk = nullptr; size_t ch_gchunk = 0;
     // sizes and lambdas of the layout currently on the device
     std::vector<int> lay_w, lay_h;
     std::vector<double> lay_lam;
@@ -130,8 +129,8 @@ struct Engine {
         ImgDesc *h_img = nullptr; size_t ch_img = 0;
         ImgState *h_ist = nullptr; size_t ch_ist = 0;
         long long *h_chunk = nullptr; size_t ch_chunk = 0;
+        int2 *h_cmap = nullptr; size_t ch_cmap = 0;
         int *h_tile_img = nullptr; size_t ch_timg = 0;
-        long long *h_gchunk = nullptr; size_t ch_gchunk = 0;
         Ctl *h_ctl = nullptr; size_t ch_ctl = 0;
         uint8_t *d_rgb = nullptr; size_t c_rgb = 0;
         uint8_t *d_scrib = nullptr; size_t c_scrib = 0;
@@ -160,7 +159,7 @@ struct Engine {
         std::swap(h_ist, o.h_ist); std::swap(ch_ist, o.ch_ist);
         std::swap(h_chunk, o.h_chunk); std::swap(ch_chunk, o.ch_chunk);
         std::swap(h_tile_img, o.h_tile_img); std::swap(ch_timg, o.ch_timg);
-        std::swap(h_gchunk, o.h_gchunk); std::swap(ch_gchunk, o.ch_gchunk);
+        std::swap(h_cmap, o.h_cmap); std::swap(ch_cmap, o.ch_cmap);
         std::swap(h_ctl, o.h_ctl); std::swap(ch_ctl, o.ch_ctl);
         std::swap(d_rgb, o.d_rgb); std::swap(c_rgb, o.c_rgb);
         std::swap(d_scrib, o.d_scrib); std::swap(c_scrib, o.c_scrib);
@@ -174,7 +173,7 @@ struct Engine {
         if (o.h_ist) cudaFreeHost(o.h_ist);
         if (o.h_chunk) cudaFreeHost(o.h_chunk);
         if (o.h_tile_img) cudaFreeHost(o.h_tile_img);
-        if (o.h_gchunk) cudaFreeHost(o.h_gchunk);
+        if (o.h_cmap) cudaFreeHost(o.h_cmap);
         if (o.h_ctl) cudaFreeHost(o.h_ctl);
         cudaFree(o.d_rgb); cudaFree(o.d_scrib); cudaFree(o.d_smin); cudaFree(o.d_smax);
         if (o.ev0) cudaEventDestroy(o.ev0);
@@ -206,7 +205,7 @@ struct Engine {
         }
         if (dn_st) cudaStreamDestroy(dn_st);
         dn_st = nullptr;
-        cudaFree(d_img); cudaFree(d_ist); cudaFree(d_chunk); cudaFree(d_tile_img);
+        cudaFree(d_img); cudaFree(d_ist); cudaFree(d_cmap); cudaFree(d_tile_img);
         cudaFree(d_cap); cudaFree(d_exc); cudaFree(d_h); cudaFree(d_reach);
         cudaFree(d_tmask); cudaFree(d_tact); cudaFree(d_tpos);
         cudaFree(d_lists);
@@ -216,6 +215,7 @@ struct Engine {
         if (h_img) cudaFreeHost(h_img);
         if (h_ist) cudaFreeHost(h_ist);
         if (h_chunk) cudaFreeHost(h_chunk);
+        if (h_cmap) cudaFreeHost(h_cmap);
         if (h_tile_img) cudaFreeHost(h_tile_img);
         if (h_ctl) cudaFreeHost(h_ctl);
         if (ev0) cudaEventDestroy(ev0);
@@ -233,19 +233,15 @@ struct Engine {
         if (ev_mark) cudaEventDestroy(ev_mark);
         ev_mark = nullptr;
         cudaFree(d_iota);
-        cudaFree(d_gchunk);
-        if (h_gchunk) cudaFreeHost(h_gchunk);
         d_iota = nullptr;
-        d_gchunk = nullptr;
-        h_gchunk = nullptr;
-        d_img = nullptr; d_ist = nullptr; d_chunk = nullptr; d_tile_img = nullptr;
+        d_img = nullptr; d_ist = nullptr; d_cmap = nullptr; d_tile_img = nullptr;
         d_cap = nullptr; d_exc = nullptr; d_h = nullptr; d_reach = nullptr;
         d_tmask = nullptr; d_tact = nullptr; d_tpos = nullptr;
         d_lists = nullptr;
         d_mpush = d_mgr = nullptr; d_ctl = nullptr;
         d_hist = d_dpl = d_dnl = nullptr; d_raw = nullptr;
         d_rgb = d_scrib = d_smin = d_smax = nullptr;
-        h_img = nullptr; h_ist = nullptr; h_chunk = nullptr; h_tile_img = nullptr; h_ctl = nullptr;
+        h_img = nullptr; h_ist = nullptr; h_chunk = nullptr; h_cmap = nullptr; h_tile_img = nullptr; h_ctl = nullptr;
         ev0 = ev1 = nullptr;
     }
 
@@ -268,9 +264,9 @@ struct Engine {
     }
 
     std::vector<const void *> buffers() const {
-        return {d_img, d_ist, d_chunk, d_tile_img, d_cap, d_exc, d_h, d_reach, d_tmask, d_tact, d_tpos,
+        return {d_img, d_ist, d_cmap, d_tile_img, d_cap, d_exc, d_h, d_reach, d_tmask, d_tact, d_tpos,
                 d_lists, d_mpush, d_mgr, d_ctl, d_hist, d_dpl, d_dnl, d_rgb, d_scrib, d_smin, d_smax,
-                h_img, h_ist, h_chunk, h_tile_img, h_ctl};
+                h_img, h_ist, h_chunk, h_cmap, h_tile_img, h_ctl};
     }
 
     // Grow the buffers; any reallocation invalidates the captured graphs.
@@ -284,7 +280,10 @@ struct Engine {
     gcfg_status reserve_(int imgs, int tiles, long long px, bool dataterm, bool staging, bool arena) {
         GCFG_TRY(grow(d_img, c_img, imgs));
         GCFG_TRY(grow(d_ist, c_ist, imgs));
-        GCFG_TRY(grow(d_chunk, c_chunk, (size_t)imgs + 1));
+        // chunks of the data-term pass: at most px / CHUNK_PX + one per image
+        const size_t chunks = (size_t)(px / CHUNK_PX) + (size_t)imgs + 1;
+        GCFG_TRY(grow(d_cmap, c_cmap, chunks));
+        GCFG_TRY(grow_host(h_cmap, ch_cmap, chunks));
         if (arena) {
             GCFG_TRY(grow(d_tile_img, c_timg, tiles));
             GCFG_TRY(grow(d_cap, c_cap, (size_t)tiles * TPX));
@@ -347,19 +346,20 @@ struct Engine {
             d.out0 = p;
             if (arena)
                 for (int k = 0; k < d.n_tiles; ++k) h_tile_img[t + k] = i;
-            d.rows_per_chunk = rows_per_chunk(W[i]);
             h_chunk[i] = ch;
             t += d.n_tiles;
             p += (long long)W[i] * H[i];
-            ch += (H[i] + d.rows_per_chunk - 1) / d.rows_per_chunk;
+            ch += image_chunks(W[i], H[i]);
         }
         h_chunk[n] = ch;
+        for (int i = 0; i < n; ++i)
+            for (long long c = h_chunk[i]; c < h_chunk[i + 1]; ++c) h_cmap[c] = make_int2(i, (int)(c - h_chunk[i]));
         n_img = n;
         n_tiles = t;
         n_px = p;
         total_chunks = ch;
         GCFG_CK(cudaMemcpyAsync(d_img, h_img, n * sizeof(ImgDesc), cudaMemcpyHostToDevice, st));
-        GCFG_CK(cudaMemcpyAsync(d_chunk, h_chunk, (n + 1) * sizeof(long long), cudaMemcpyHostToDevice, st));
+        GCFG_CK(cudaMemcpyAsync(d_cmap, h_cmap, (size_t)ch * sizeof(int2), cudaMemcpyHostToDevice, st));
         if (arena)
             GCFG_CK(cudaMemcpyAsync(d_tile_img, h_tile_img, (size_t)t * sizeof(int), cudaMemcpyHostToDevice, st));
         GCFG_CK(cudaMemsetAsync(d_ist, 0, n * sizeof(ImgState), st));
@@ -413,13 +413,6 @@ struct Engine {
             GCFG_CK(cudaMemcpy(d_iota, iota.data(), iota.size() * sizeof(int), cudaMemcpyHostToDevice));
             iota_n = need_iota;
         }
-        GCFG_TRY(grow(d_gchunk, c_gchunk, (size_t)n + G));
-        GCFG_TRY(grow_host(h_gchunk, ch_gchunk, (size_t)n + G));
-        for (int g = 0; g < G; ++g) {
-            const Group &gr = groups[g];
-            for (int k = gr.i0; k <= gr.i1; ++k) h_gchunk[k + g] = h_chunk[k] - h_chunk[gr.i0];
-        }
-        GCFG_CK(cudaMemcpyAsync(d_gchunk, h_gchunk, ((size_t)n + G) * sizeof(long long), cudaMemcpyHostToDevice, st));
         if (!cp_st) GCFG_CK(cudaStreamCreateWithFlags(&cp_st, cudaStreamNonBlocking));
         for (int g = 0; g < MAX_GROUPS; ++g) {
             if (!ev_in[g]) GCFG_CK(cudaEventCreateWithFlags(&ev_in[g], cudaEventDisableTiming));
@@ -464,7 +457,7 @@ struct Engine {
         a.scrib = scrib;
         a.img = d_img;
         a.ist = d_ist;
-        a.chunk_off = d_chunk;
+        a.chunk_map = d_cmap;
         a.hist = d_hist;
         a.dp_lut = d_dpl;
         a.dn_lut = d_dnl;
@@ -923,7 +916,7 @@ static gcfg_status stage_build(Engine &e) {
         a.n_img = gr.i1 - gr.i0;
         a.ilist = e.d_iota + gr.i0;
         a.total_chunks = gr.c1 - gr.c0;
-        a.chunk_off = e.d_gchunk + gr.i0 + g;
+        a.chunk_map = e.d_cmap + gr.c0;
         GCFG_CK(cudaMemsetAsync(e.d_hist + (size_t)gr.i0 * 2 * NBINS, 0,
                                 (size_t)(gr.i1 - gr.i0) * 2 * NBINS * sizeof(int), e.st));
         GCFG_TRY(dt_tables(a, e.st));

@@ -89,8 +89,6 @@ __global__ void k_noalloc_layout(ImgDesc *img, int *tile_img, int W, int H) {
         d.n_tiles = n;
         d.pix0 = 0;
         d.lambda = 0.0;
-        d.rows_per_chunk = 1;
-        d.pad = 0;
         d.out0 = 0;
         *img = d;
     }

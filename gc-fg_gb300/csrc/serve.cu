@@ -236,7 +236,7 @@ struct Lane {
     int *d_tnew = nullptr, *h_tnew = nullptr;  // tiles of new images
     int *d_tedit = nullptr, *h_tedit = nullptr;  // tiles of edited images
     int *d_il = nullptr, *h_il = nullptr;      // slots of the batch
-    long long *d_chunk = nullptr, *h_chunk = nullptr;
+    int2 *d_cmap = nullptr, *h_cmap = nullptr;  // per chunk: (slot, chunk within the image)
     ImgDesc *h_desc = nullptr;
     ImgState *h_ist = nullptr;
     std::thread th;
@@ -325,9 +325,9 @@ gcfg_status run_batch(Lane &L, std::vector<Req> &batch, const std::vector<Sessio
     for (int k = 0; k < n; ++k) {
         const Session &x = snap[k];
         L.h_il[k] = x.slot;
-        L.h_chunk[k] = ch;
-        const int rows = rows_per_chunk(x.W);
-        ch += (x.H + rows - 1) / rows;
+        const long long nc = image_chunks(x.W, x.H);
+        for (long long c = 0; c < nc; ++c) L.h_cmap[ch + c] = make_int2(x.slot, (int)c);
+        ch += nc;
         for (long long i = 0; i < x.n_tiles; ++i) {
             const int t = (int)(x.tile0 + i);
             L.h_tl[nt++] = t;
@@ -345,8 +345,6 @@ gcfg_status run_batch(Lane &L, std::vector<Req> &batch, const std::vector<Sessio
             d.n_tiles = (int)x.n_tiles;
             d.pix0 = x.pix0;
             d.lambda = x.lambda;
-            d.rows_per_chunk = rows;
-            d.pad = 0;
             d.out0 = x.pix0;
             GCFG_CK(cudaMemcpyAsync(s.img + x.slot, &d, sizeof(ImgDesc), cudaMemcpyHostToDevice, st));
             k_fill_tile_owner<<<div_up((int)x.n_tiles, 256), 256, 0, st>>>(s.tile_img, x.tile0, (int)x.n_tiles, x.slot);
@@ -368,7 +366,7 @@ gcfg_status run_batch(Lane &L, std::vector<Req> &batch, const std::vector<Sessio
         }
     }
     GCFG_CK(cudaMemcpyAsync(L.d_il, L.h_il, n * sizeof(int), cudaMemcpyHostToDevice, st));
-    GCFG_CK(cudaMemcpyAsync(L.d_chunk, L.h_chunk, n * sizeof(long long), cudaMemcpyHostToDevice, st));
+    GCFG_CK(cudaMemcpyAsync(L.d_cmap, L.h_cmap, ch * sizeof(int2), cudaMemcpyHostToDevice, st));
     GCFG_CK(cudaMemcpyAsync(L.d_tl, L.h_tl, nt * sizeof(int), cudaMemcpyHostToDevice, st));
     if (nnew) GCFG_CK(cudaMemcpyAsync(L.d_tnew, L.h_tnew, nnew * sizeof(int), cudaMemcpyHostToDevice, st));
     if (nedit) GCFG_CK(cudaMemcpyAsync(L.d_tedit, L.h_tedit, nedit * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -385,7 +383,7 @@ gcfg_status run_batch(Lane &L, std::vector<Req> &batch, const std::vector<Sessio
     a.scrib = s.scrib;
     a.img = s.img;
     a.ist = s.ist;
-    a.chunk_off = L.d_chunk;
+    a.chunk_map = L.d_cmap;
     a.hist = s.hist;
     a.dp_lut = s.dpl;
     a.dn_lut = s.dnl;
@@ -568,9 +566,9 @@ void shutdown_server(Server *s) {
         if (L->th.joinable()) L->th.join();
         cudaStreamDestroy(L->st);
         cudaFree(L->ctl); cudaFree(L->lists); cudaFree(L->d_tl); cudaFree(L->d_tnew); cudaFree(L->d_tedit);
-        cudaFree(L->d_il); cudaFree(L->d_chunk);
+        cudaFree(L->d_il); cudaFree(L->d_cmap);
         cudaFreeHost(L->h_ctl); cudaFreeHost(L->h_tl); cudaFreeHost(L->h_tnew); cudaFreeHost(L->h_tedit);
-        cudaFreeHost(L->h_il); cudaFreeHost(L->h_chunk); cudaFreeHost(L->h_desc); cudaFreeHost(L->h_ist);
+        cudaFreeHost(L->h_il); cudaFreeHost(L->h_cmap); cudaFreeHost(L->h_desc); cudaFreeHost(L->h_ist);
         delete L;
     }
     cudaFree(s->cap); cudaFree(s->exc); cudaFree(s->h); cudaFree(s->reach); cudaFree(s->tmask); cudaFree(s->tact);
@@ -637,7 +635,8 @@ gcfg_status gcfg_serve_create(const gcfg_serve_config *cfg, gcfg_server **out) {
         chk(dalloc(L->d_tnew, LT)); chk(halloc(L->h_tnew, LT));
         chk(dalloc(L->d_tedit, LT)); chk(halloc(L->h_tedit, LT));
         chk(dalloc(L->d_il, LI)); chk(halloc(L->h_il, LI));
-        chk(dalloc(L->d_chunk, LI + 1)); chk(halloc(L->h_chunk, LI + 1));
+        // chunks of a batch: at most its pixels / CHUNK_PX + one per image
+        chk(dalloc(L->d_cmap, LT * TPX / CHUNK_PX + LI + 1)); chk(halloc(L->h_cmap, LT * TPX / CHUNK_PX + LI + 1));
         chk(halloc(L->h_desc, LI)); chk(halloc(L->h_ist, LI));
         s->lanes.push_back(L);
     }

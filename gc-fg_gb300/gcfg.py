@@ -35,7 +35,7 @@ EXPORTS = [
     "gcfg_init", "gcfg_set_dataterms", "gcfg_set_edges", "gcfg_set_penalty", "gcfg_set_graph",
     "gcfg_optimize", "gcfg_get_cuts", "gcfg_end", "gcfg_set_stream", "gcfg_set_schedule",
     "gcfg_tlinks", "gcfg_nlinks", "gcfg_seg_create", "gcfg_seg_run", "gcfg_seg_run_host",
-    "gcfg_seg_set_stream", "gcfg_seg_destroy", "gcfg_strerror", "gcfg_launch_count",
+    "gcfg_seg_set_stream", "gcfg_seg_destroy", "gcfg_strerror", "gcfg_launch_count", "gcfg_selftest_ex2",
     "gcfg_profile_enable", "gcfg_profile_read", "gcfg_batch_create", "gcfg_batch_set_stream",
     "gcfg_batch_set_params", "gcfg_batch_run", "gcfg_batch_run_host", "gcfg_batch_submit_host",
     "gcfg_batch_wait", "gcfg_batch_destroy",
@@ -119,6 +119,7 @@ def load(path: str = LIB_PATH):
         "gcfg_seg_destroy": (S, [P]),
         "gcfg_strerror": (C.c_char_p, [I]),
         "gcfg_launch_count": (C.c_int64, []),
+        "gcfg_selftest_ex2": (S, [C.c_int64, P]),
         "gcfg_batch_create": (S, [I, C.c_int64, C.POINTER(P)]),
         "gcfg_batch_set_stream": (S, [P, P]),
         "gcfg_batch_set_params": (S, [P, I, I, I]),
@@ -177,6 +178,13 @@ def _ptr(t):
 
 def launch_count() -> int:
     return load().gcfg_launch_count()
+
+
+def selftest_ex2(samples: int = 1 << 24) -> float:
+    """Largest relative error of the device's approximate 2^z on [-64, 0]."""
+    v = C.c_float()
+    _check(load().gcfg_selftest_ex2(int(samples), C.byref(v)), "gcfg_selftest_ex2")
+    return v.value
 
 
 def profile_enable(on: bool = True):

@@ -471,6 +471,10 @@ gcfg_status gcfg_profile_read(gcfg_prof_entry *out, int max_entries, int *n_out)
 const char *gcfg_strerror(gcfg_status s);
 /* Number of kernel launches issued by this library in this process. */
 int64_t gcfg_launch_count(void);
+/* Largest relative error of the device's approximate base-2 exponential
+ * (the n-link fast path) over `samples` evenly spaced points of [-64, 0];
+ * the fast path's error bound assumes <= 2^-21 (no counterpart). */
+gcfg_status gcfg_selftest_ex2(int64_t samples, float *max_rel_err);
 
 #ifdef __cplusplus
 }

@@ -316,3 +316,28 @@ def test_batch256_full_size_cuts_match_per_image():
         W, H, _ = shapes[i]
         o, n = int(offs[i]), W * H
         assert flows[i] == O.segment(rgb[3 * o:3 * (o + n)].reshape(H, W, 3), scrib[o:o + n].reshape(H, W), 50.0)["flow"]
+
+
+def test_ex2_error_within_nlink_bound():
+    """The n-link fast path's margin assumes the device's approximate 2^z is
+    within 2^-21 relative error on the exponents it meets ([-64, 0])."""
+    err = gcfg.selftest_ex2(1 << 24)
+    assert 0.0 <= err <= 2.0 ** -21, err
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+@pytest.mark.parametrize("lam", [0.7, 3.0, 50.0, 255.5, 4096.0, 65536.0, 3.0e6])
+def test_nlinks_bit_exact_random_colours(seed, lam):
+    """Uniform random colours spread the squared distances over the whole
+    range 0 .. 3*255^2 (generated images keep them small); every weight of
+    the float fast path equals the oracle's double evaluation."""
+    rng = np.random.default_rng(77 + seed)
+    W, H = 611, 409
+    rgb = rng.integers(0, 256, size=(H, W, 3), dtype=np.uint8)
+    if seed == 1:  # a few colours only: many equal distances (ties of d2)
+        pal = rng.integers(0, 256, size=(5, 3), dtype=np.uint8)
+        rgb = pal[rng.integers(0, 5, size=(H, W))]
+    outs = [torch.empty((H, W), dtype=torch.int32, device="cuda") for _ in range(4)]
+    gcfg.nlinks(dev(rgb), W, H, lam, *outs)
+    for a, b in zip(outs, O.nlinks(rgb, lam)):
+        assert np.array_equal(a.cpu().numpy(), b)
