@@ -156,17 +156,24 @@ __device__ __forceinline__ float ex2_approx(float z) {
     return r;
 }
 
-__device__ __forceinline__ int nlink_quant(int d2, const NlinkParams &q) {
+// The float fast path: w = the rounded weight, true when v is farther than
+// the margin from a rounding boundary (else the double expression decides).
+__device__ __forceinline__ bool nlink_fast(int d2, const NlinkParams &q, int &w) {
     const float v = q.lf * ex2_approx(-small_int_to_float(d2) * q.scale);
     if (q.small) {
         const float t = __fadd_rn(v, 12582912.0f);  // 1.5 * 2^23 + rint(v)
         const float rf = __fsub_rn(t, 12582912.0f);
-        if (fabsf(__fsub_rn(v, rf)) < q.half_margin) return __float_as_int(t) - 0x4B400000;
-        return nlink_exact(d2, q.lambda, q.s2);
+        w = __float_as_int(t) - 0x4B400000;
+        return fabsf(__fsub_rn(v, rf)) < q.half_margin;
     }
     const float fr = v - floorf(v);
-    if (fabsf(fr - 0.5f) > q.margin) return (int)floorf(v + 0.5f);
-    return nlink_exact(d2, q.lambda, q.s2);
+    w = (int)floorf(v + 0.5f);
+    return fabsf(fr - 0.5f) > q.margin;
+}
+
+__device__ __forceinline__ int nlink_quant(int d2, const NlinkParams &q) {
+    int w;
+    return nlink_fast(d2, q, w) ? w : nlink_exact(d2, q.lambda, q.s2);
 }
 
 // Aligned 32-bit word at a (a % 4 == 0) of the byte range [lo, hi): one load
@@ -457,7 +464,7 @@ __device__ __forceinline__ int nlink_w(int d2, const NlinkParams &q) {
 // down-edge table, and each pixel then reads its four capacities from them.
 // An edge that touches the 1-pixel image border has capacity 0, as in the
 // reference's graph (GraphCutKernels.cu:112-214).
-__global__ void __launch_bounds__(TILE_THREADS) k_build_img_b(Batch b, const uint8_t *__restrict__ rgb,
+__global__ void __launch_bounds__(TILE_THREADS, 5) k_build_img_b(Batch b, const uint8_t *__restrict__ rgb,
                                                                const int *__restrict__ dp_lut,
                                                                const int *__restrict__ dn_lut) {
     constexpr int SW = TILE_W + 2, SH = TILE_H + 2;
@@ -478,31 +485,26 @@ __global__ void __launch_bounds__(TILE_THREADS) k_build_img_b(Batch b, const uin
     const uint8_t *base = rgb + 3 * d.pix0;
 
     // Stage the 34 rows of 34 pixels (tile + 1-pixel halo) as packed colours.
-    // A row's bytes are fetched as aligned 32-bit words, one per lane (at
-    // most 27), instead of three byte loads per pixel; a word that reaches
-    // outside this image's bytes is assembled from the bytes inside.  Each
-    // pixel is then cut out of two adjacent words with a funnel shift.
+    // Warp w takes rows w, w + 8, ...: the row's bytes are fetched as aligned
+    // 32-bit words, one per lane (at most 27; a word that reaches outside
+    // this image's bytes is assembled from the bytes inside), and each lane
+    // cuts its pixel out of two adjacent words (warp shuffles + a funnel
+    // shift); lanes 0 and 1 then cut the row's last two pixels.
     {
-        constexpr int RAWW = 28;
-        __shared__ uint32_t raw[SH][RAWW];
-        __shared__ int phase[SH];
         const uintptr_t lo = (uintptr_t)base, hi = lo + 3 * (uintptr_t)W * (uintptr_t)H;
         const int xs = x0 > 0 ? x0 - 1 : 0;
         const int xe = x0 + TILE_W < W ? x0 + TILE_W : W - 1;
         constexpr int NW = TILE_THREADS / 32, RPW = (SH + NW - 1) / NW;  // rows per warp
         uint32_t words[RPW];
-        int phs[RPW];
 #pragma unroll
-        for (int r = 0; r < RPW; ++r) {  // every load first, then the stores
+        for (int r = 0; r < RPW; ++r) {  // every load first
             const int i = warp + NW * r;
             const int y = y0 - 1 + i;
             uint32_t word = 0;
-            int ph = 0;
             if (i < SH && y >= 0 && y < H) {
                 const uintptr_t a0 = lo + 3 * ((uintptr_t)y * W + xs);
                 const uintptr_t a1 = lo + 3 * ((uintptr_t)y * W + xe) + 3;
                 const uintptr_t aw = a0 & ~(uintptr_t)3;
-                ph = (int)(a0 - aw);
                 if (lane < (int)((a1 - aw + 3) >> 2)) {
                     const uintptr_t wa = aw + 4 * (uintptr_t)lane;
                     if (wa >= lo && wa + 4 <= hi) {
@@ -516,26 +518,26 @@ __global__ void __launch_bounds__(TILE_THREADS) k_build_img_b(Batch b, const uin
                 }
             }
             words[r] = word;
-            phs[r] = ph;
         }
 #pragma unroll
         for (int r = 0; r < RPW; ++r) {
             const int i = warp + NW * r;
-            if (i < SH) {
-                if (lane < RAWW) raw[i][lane] = words[r];
-                if (lane == 0) phase[i] = phs[r];
+            if (i >= SH) break;  // warp-uniform
+            const int y = y0 - 1 + i;
+            const bool row_in = y >= 0 && y < H;
+            const int ph = (int)((lo + 3 * ((uintptr_t)y * W + xs)) & 3);  // first byte's place in its word
+            // pixel j = lane (x = x0 - 1 + lane), then j = 32 + lane for lanes 0, 1
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int j = lane + 32 * h;
+                const int x = x0 - 1 + j;
+                const bool in = row_in && x >= 0 && x < W;
+                const int off = in ? ph + 3 * (x - xs) : 0;  // <= 3 + 3 * 33 = 102: words 0..26
+                const uint32_t wlo = __shfl_sync(0xffffffffu, words[r], off >> 2);
+                const uint32_t whi = __shfl_sync(0xffffffffu, words[r], (off >> 2) + 1);
+                const uint32_t v = in ? __funnelshift_r(wlo, whi, (off & 3) * 8) & 0xFFFFFFu : 0u;
+                if (j < SW) col[i][j] = v;
             }
-        }
-        __syncthreads();
-        for (int k = threadIdx.x; k < SH * SW; k += TILE_THREADS) {
-            const int i = k / SW, j = k - i * SW;
-            const int x = x0 - 1 + j, y = y0 - 1 + i;
-            uint32_t v = 0;
-            if (x >= 0 && y >= 0 && x < W && y < H) {
-                const int off = phase[i] + 3 * (x - xs);
-                v = __funnelshift_r(raw[i][off >> 2], raw[i][(off >> 2) + 1], (off & 3) * 8) & 0xFFFFFFu;
-            }
-            col[i][j] = v;
         }
     }
     __syncthreads();
@@ -543,31 +545,48 @@ __global__ void __launch_bounds__(TILE_THREADS) k_build_img_b(Batch b, const uin
     // edges wr[i][1..32], then down edges wd[1..32][j]), and the 64 edges
     // that reach into the tile from the left and from above (wr[i][0], wd[0][j])
     {
+        // thread (warp, lane): right edges of pixel (x0 + lane, y0 + warp + 8u),
+        // u = 0..3, and down edges of the same pixels, u = 4..7
         constexpr int PER = 2 * TILE_W * TILE_H / TILE_THREADS;
-        int d2[PER];
-        bool use[PER];
+        static_assert(PER == 8 && ROWS_PER_WARP == 4, "edge split assumes 8 warps of 32 lanes");
+        const int x = x0 + lane;
+        const bool xr = x >= 1 && x <= W - 3, xd = x >= 1 && x <= W - 2;
+        // each weight goes to shared memory as soon as it is known; the rare
+        // ones within the margin of a rounding boundary are redone exactly
+        unsigned exact = 0;  // bit u: edge u needs the double expression
 #pragma unroll
         for (int u = 0; u < PER; ++u) {
-            const int k = threadIdx.x + u * TILE_THREADS;
-            if (k < TILE_W * TILE_H) {  // right edge of pixel (x0 + j, y0 + i)
-                const int i = k >> 5, j = k & 31;
-                const int x = x0 + j, y = y0 + i;
-                use[u] = x >= 1 && x <= W - 3 && y >= 1 && y <= H - 2;
-                d2[u] = diff2w(col[i + 1][j + 1], col[i + 1][j + 2]);
-            } else {  // down edge of pixel (x0 + j, y0 + i)
-                const int kk = k - TILE_W * TILE_H;
-                const int i = kk >> 5, j = kk & 31;
-                const int x = x0 + j, y = y0 + i;
-                use[u] = y >= 1 && y <= H - 3 && x >= 1 && x <= W - 2;
-                d2[u] = diff2w(col[i + 1][j + 1], col[i + 2][j + 1]);
+            const int i = warp + 8 * (u & 3);
+            const int y = y0 + i;
+            bool use;
+            int d2;
+            if (u < 4) {
+                use = xr && y >= 1 && y <= H - 2;
+                d2 = diff2w(col[i + 1][lane + 1], col[i + 1][lane + 2]);
+            } else {
+                use = xd && y >= 1 && y <= H - 3;
+                d2 = diff2w(col[i + 1][lane + 1], col[i + 2][lane + 1]);
             }
+            int w = 0;
+            if (q.constant) {
+                w = q.const_w;
+            } else if (!nlink_fast(d2, q, w)) {
+                exact |= 1u << u;
+            }
+            if (!use) {
+                w = 0;
+                exact &= ~(1u << u);
+            }
+            if (u < 4) wr[i][lane + 1] = w;
+            else wd[i + 1][lane] = w;
         }
-#pragma unroll
-        for (int u = 0; u < PER; ++u) {
-            const int k = threadIdx.x + u * TILE_THREADS;
-            const int w = use[u] ? nlink_w(d2[u], q) : 0;
-            if (k < TILE_W * TILE_H) wr[k >> 5][(k & 31) + 1] = w;
-            else wd[((k - TILE_W * TILE_H) >> 5) + 1][k & 31] = w;
+        if (__any_sync(0xffffffffu, exact != 0)) {
+            for (unsigned m = exact; m; m &= m - 1) {
+                const int u = __ffs(m) - 1;
+                const int i = warp + 8 * (u & 3);
+                if (u < 4) wr[i][lane + 1] = nlink_exact(diff2w(col[i + 1][lane + 1], col[i + 1][lane + 2]), q.lambda, q.s2);
+                else wd[i + 1][lane] = nlink_exact(diff2w(col[i + 1][lane + 1], col[i + 2][lane + 1]), q.lambda, q.s2);
+            }
         }
         if (threadIdx.x < 2 * 32) {
             const int j = threadIdx.x & 31;
@@ -585,18 +604,27 @@ __global__ void __launch_bounds__(TILE_THREADS) k_build_img_b(Batch b, const uin
     }
     __syncthreads();
 
-    const long long w32 = (long long)((W + 31) / 32) * 32;
-    unsigned long long idp = 0, rinit = 0, pos = 0;
+    // Per pixel (thread (warp, lane), rows warp + 8k): capacities, excess and
+    // the sums of the tile.  Per-thread sums stay below 2^30 (4 pixels of at
+    // most GCFG_MAX_CAP), so they are 32-bit and each warp adds them exactly
+    // with two 32-bit reductions of their 16-bit halves.
+    __shared__ uint32_t msk[6][TILE_H];  // mask planes of the tile, stored coalesced below
+    __shared__ unsigned long long wsum[3][TILE_THREADS / 32];
+    const long long w32 = (long long)((W + 31) / 32) * 32, npx = (long long)W * H;
+    const int x = x0 + lane;
+    uint32_t idp = 0, rinit = 0, pos = 0;
+    int4 *cap = b.cap + (size_t)t * TPX;
+    int *exc = b.exc + (size_t)t * TPX;
 #pragma unroll
     for (int k = 0; k < ROWS_PER_WARP; ++k) {
         const int r = warp + 8 * k;
-        const int x = x0 + lane, y = y0 + r;
+        const int y = y0 + r;
         int4 c = make_int4(0, 0, 0, 0);
         int e = 0;
         if (x < W && y < H) {
             const int bin = color_binw(col[r + 1][lane + 1]);
             const int vdp = __ldg(dpl + bin);
-            if ((long long)x + (long long)y * w32 < (long long)W * H && vdp > 0) rinit += (unsigned)vdp;
+            if ((long long)x + (long long)y * w32 < npx && vdp > 0) rinit += (unsigned)vdp;
             if (x > 0 && y > 0 && x < W - 1 && y < H - 1) {
                 c.x = wr[r][lane];      // left: edge (x - 1, y)-(x, y)
                 c.y = wr[r][lane + 1];  // right
@@ -606,15 +634,40 @@ __global__ void __launch_bounds__(TILE_THREADS) k_build_img_b(Batch b, const uin
                 idp += (unsigned)vdp;
             }
         }
-        const size_t qi = (size_t)t * TPX + r * 32 + lane;
-        b.cap[qi] = c;
-        b.exc[qi] = e;
-        write_tile_masks(b, t, r, c, e);
+        cap[r * 32 + lane] = c;
+        exc[r * 32 + lane] = e;
+        const unsigned ml = __ballot_sync(0xffffffffu, c.x > 0);
+        const unsigned mr = __ballot_sync(0xffffffffu, c.y > 0);
+        const unsigned mu = __ballot_sync(0xffffffffu, c.z > 0);
+        const unsigned md = __ballot_sync(0xffffffffu, c.w > 0);
+        const unsigned mn = __ballot_sync(0xffffffffu, e < 0);
+        const unsigned mp = __ballot_sync(0xffffffffu, e > 0);
+        if (lane == 0) {
+            msk[0][r] = ml; msk[1][r] = mr; msk[2][r] = mu; msk[3][r] = md; msk[4][r] = mn; msk[5][r] = mp;
+        }
         if (e > 0) pos += (unsigned)e;
     }
-    block_store_sum(b.tile_pos + t, pos);
-    warp_atomic_add_u64(&b.ist[im].interior_dp, idp);
-    warp_atomic_add_u64(&b.ist[im].ref_init, rinit);
+    {
+        const uint32_t v[3] = {idp, rinit, pos};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const unsigned long long lo = __reduce_add_sync(0xffffffffu, v[k] & 0xFFFFu);
+            const unsigned long long hi = __reduce_add_sync(0xffffffffu, v[k] >> 16);
+            if (lane == 0) wsum[k][warp] = (hi << 16) + lo;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6 * TILE_H)
+        b.tmask[(size_t)t * 6 * 32 + threadIdx.x] = msk[threadIdx.x >> 5][threadIdx.x & 31];
+    if (warp == 0) {
+        // lanes 0..2: the tile's three sums
+        unsigned long long tot = 0;
+        if (lane < 3)
+            for (int w8 = 0; w8 < TILE_THREADS / 32; ++w8) tot += wsum[lane][w8];
+        if (lane == 0 && tot) atomicAdd(&b.ist[im].interior_dp, tot);
+        if (lane == 1 && tot) atomicAdd(&b.ist[im].ref_init, tot);
+        if (lane == 2) b.tile_pos[t] = tot;
+    }
 }
 
 // Row-major t-link / n-link arrays of image 0 (the stand-alone data-term API).
