@@ -209,6 +209,75 @@ __device__ unsigned tile_bfs(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd,
     return S;
 }
 
+// The push visits' exact local relabel: the same levels as tile_bfs, but
+// instead of storing each new pixel's level on the spot (a divergent loop on
+// the loop-carried path of a single warp) the k-th expansion (k < NREC)
+// records the reached rows srec[k][row] and its level lv[k]; expansions past
+// NREC store their pixels' levels directly, as tile_bfs does.  sfin gets the
+// final reached rows.  Returns the number of records (warp-uniform); the
+// whole block then fills in the heights (heights_from_records).
+constexpr int NREC = 48;
+__device__ int tile_bfs_rec(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd, unsigned sink, int hl, int hr,
+                            int ht, int hb, int *hs, int stride, unsigned (*srec)[32], int *lv, unsigned *sfin,
+                            int *iters) {
+    const int lane = threadIdx.x & 31;
+    int *row = hs + lane * stride;
+    unsigned S = sink;
+    int lvl = 1, nrec = 0, it = 0;
+    for (; it < BFS_MAX_ITERS; ++it) {
+        const unsigned T = __ballot_sync(FULL, ht <= lvl);
+        const unsigned B = __ballot_sync(FULL, hb <= lvl);
+        unsigned up = __shfl_up_sync(FULL, S, 1);
+        unsigned dn = __shfl_down_sync(FULL, S, 1);
+        if (lane == 0) up = T;
+        if (lane == 31) dn = B;
+        const unsigned lin = (S << 1) | (hl <= lvl ? 1u : 0u);
+        const unsigned rin = (S >> 1) | (hr <= lvl ? 0x80000000u : 0u);
+        unsigned nw = ((Rl & lin) | (Rr & rin) | (Ru & up) | (Rd & dn)) & ~S;
+        if (__any_sync(FULL, nw != 0)) {
+            S |= nw;
+            ++lvl;
+            if (nrec < NREC) {
+                srec[nrec][lane] = S;
+                if (lane == 0) lv[nrec] = lvl;
+                ++nrec;
+            } else {
+                for (; nw; nw &= nw - 1) row[__ffs(nw) - 1] = lvl;
+            }
+        } else {
+            int cand = INF_H;
+            if (hl > lvl) cand = min(cand, hl);
+            if (hr > lvl) cand = min(cand, hr);
+            if (ht > lvl) cand = min(cand, ht);
+            if (hb > lvl) cand = min(cand, hb);
+            const int nxt = __reduce_min_sync(FULL, cand);
+            if (nxt >= INF_H) break;
+            lvl = nxt;
+        }
+    }
+    sfin[lane] = S;
+    *iters = it;
+    return nrec;
+}
+
+// Height of pixel x of row r after tile_bfs_rec: INF outside the final
+// reached set, 1 on the seeds, else the level of the first record that holds
+// it (records are cumulative, so a binary search finds it), else the level
+// stored directly by an expansion past the records.
+__device__ __forceinline__ int height_from_records(int r, int x, unsigned seed, const unsigned (*srec)[32],
+                                                   const int *lv, const unsigned *sfin, int nrec, int stored) {
+    if (!((sfin[r] >> x) & 1u)) return INF_H;
+    if ((seed >> x) & 1u) return 1;
+    if (nrec == 0 || !((srec[nrec - 1][r] >> x) & 1u)) return stored;
+    int lo = 0, hi = nrec - 1;  // smallest k with the bit set lies in [lo, hi]
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if ((srec[mid][r] >> x) & 1u) hi = mid;
+        else lo = mid + 1;
+    }
+    return lv[lo];
+}
+
 // ---------------------------------------------------------------------------
 // Shared memory of the persistent kernel (phases reuse the same bytes)
 // ---------------------------------------------------------------------------
@@ -250,9 +319,12 @@ struct SmemPush {
     int h[TILE_H + 2][TILE_W + 2];
     int halo_in[4][32];
     unsigned m[5][32];  // left, right, up, down, sink row masks
+    unsigned srec[NREC][32];  // local relabel: reached rows after each recorded expansion
+    int lv[NREC];             // and its level
+    unsigned sfin[32];        // final reached rows
+    int nrec;
     unsigned long long part[8];
     int idx;
-    int flag;
 };
 struct SmemWarp {
     int hs[8][32 * 33];
@@ -436,10 +508,24 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
         const long long cb0 = clock64();
         if (warp == 0) {
             int its = 0;
-            tile_bfs(s.m[0][lane], s.m[1][lane], s.m[2][lane], s.m[3][lane], s.m[4][lane],
-                     s.h[lane + 1][0], s.h[lane + 1][TILE_W + 1], s.h[0][lane + 1],
-                     s.h[TILE_H + 1][lane + 1], &s.h[1][1], TILE_W + 2, &its);
-            if (lane == 0) stat_add(st, ST_BFS_IT_PUSH, (unsigned long long)its);
+            const int nrec = tile_bfs_rec(s.m[0][lane], s.m[1][lane], s.m[2][lane], s.m[3][lane], s.m[4][lane],
+                                          s.h[lane + 1][0], s.h[lane + 1][TILE_W + 1], s.h[0][lane + 1],
+                                          s.h[TILE_H + 1][lane + 1], &s.h[1][1], TILE_W + 2, s.srec, s.lv, s.sfin,
+                                          &its);
+            if (lane == 0) {
+                s.nrec = nrec;
+                stat_add(st, ST_BFS_IT_PUSH, (unsigned long long)its);
+            }
+        }
+        __syncthreads();
+        {
+            const int nrec = s.nrec;
+#pragma unroll
+            for (int k = 0; k < ROWS_PER_WARP; ++k) {
+                const int r = warp + 8 * k;
+                s.h[r + 1][lane + 1] =
+                    height_from_records(r, lane, s.m[4][r], s.srec, s.lv, s.sfin, nrec, s.h[r + 1][lane + 1]);
+            }
         }
         __syncthreads();
         cb += clock64() - cb0;
