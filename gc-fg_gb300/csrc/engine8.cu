@@ -63,20 +63,29 @@ __device__ __forceinline__ void set_err8(Ctl8 *c, int code) {
 
 // Grid barrier (bounded spin); the last block to arrive clears frontier
 // size `reset` (>= 0) before releasing the others.
+__device__ __forceinline__ unsigned atom_add_acq_rel8(unsigned *p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+__device__ __forceinline__ unsigned ld_acquire8(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
 __device__ bool sync8(Ctl8 *c, int reset) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned *vgen = &c->bar_gen;
-        const unsigned gen = *vgen;
-        __threadfence();
-        if (atomicAdd(&c->bar_count, 1u) == gridDim.x - 1) {
+        const unsigned gen = ld_acquire8(&c->bar_gen);
+        if (atom_add_acq_rel8(&c->bar_count, 1u) == gridDim.x - 1) {
             if (reset >= 0) c->fsize[reset] = 0;
             c->bar_count = 0;
-            __threadfence();
-            atomicAdd(&c->bar_gen, 1u);
+            atom_add_acq_rel8(&c->bar_gen, 1u);
         } else {
             unsigned long long it = 0;
-            while (*vgen == gen) {
+            while (ld_acquire8(&c->bar_gen) == gen) {
                 if (++it > (1ull << 25)) {
                     set_err8(c, E8_BARRIER);
                     break;
@@ -84,7 +93,6 @@ __device__ bool sync8(Ctl8 *c, int reset) {
                 __nanosleep(32);
             }
         }
-        __threadfence();
     }
     // thread 0's reading of the error word decides for the whole block
     return !__syncthreads_or(threadIdx.x == 0 && *(volatile int *)&c->err != 0);
