@@ -36,6 +36,8 @@ namespace gcfg {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int BFS_MAX_ITERS = TPX + 4 * 32 + 8;
+// lines of a tile's border array (Batch::hb, 128 ints per tile)
+constexpr int HB_TOP = 0, HB_BOT = 32, HB_LFT = 64, HB_RGT = 96;
 constexpr unsigned long long SPIN_LIMIT = 1ull << 25;   // about a second of polling
 
 // ---------------------------------------------------------------------------
@@ -395,10 +397,11 @@ __device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int t
         hl = g.nb[0] >= 0 && (mask_word(b, g.nb[0], 4, lane) >> 31) ? 1 : INF_H;
         hr = g.nb[1] >= 0 && (mask_word(b, g.nb[1], 4, lane) & 1u) ? 1 : INF_H;
     } else {
-        ht = g.nb[2] >= 0 ? __ldcg(b.h + (size_t)g.nb[2] * TPX + 31 * 32 + lane) : INF_H;
-        hb = g.nb[3] >= 0 ? __ldcg(b.h + (size_t)g.nb[3] * TPX + lane) : INF_H;
-        hl = g.nb[0] >= 0 ? __ldcg(b.h + (size_t)g.nb[0] * TPX + lane * 32 + 31) : INF_H;
-        hr = g.nb[1] >= 0 ? __ldcg(b.h + (size_t)g.nb[1] * TPX + lane * 32) : INF_H;
+        // the neighbours' facing border lines (coalesced, from the border array)
+        ht = g.nb[2] >= 0 ? __ldcg(b.hb + (size_t)g.nb[2] * 128 + HB_BOT + lane) : INF_H;
+        hb = g.nb[3] >= 0 ? __ldcg(b.hb + (size_t)g.nb[3] * 128 + HB_TOP + lane) : INF_H;
+        hl = g.nb[0] >= 0 ? __ldcg(b.hb + (size_t)g.nb[0] * 128 + HB_RGT + lane) : INF_H;
+        hr = g.nb[1] >= 0 ? __ldcg(b.hb + (size_t)g.nb[1] * 128 + HB_LFT + lane) : INF_H;
     }
     int o_top, o_bot, o_lft, o_rgt;  // this tile's border before the visit (no other warp writes it meanwhile)
     if (round0) {
@@ -408,10 +411,11 @@ __device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int t
         o_lft = (m[4] & 1u) ? 1 : INF_H;
         o_rgt = (m[4] >> 31) ? 1 : INF_H;
     } else {
-        o_top = __ldcg(b.h + base + lane);
-        o_bot = __ldcg(b.h + base + 31 * 32 + lane);
-        o_lft = __ldcg(b.h + base + lane * 32);
-        o_rgt = __ldcg(b.h + base + lane * 32 + 31);
+        const int *own = b.hb + (size_t)t * 128;
+        o_top = __ldcg(own + HB_TOP + lane);
+        o_bot = __ldcg(own + HB_BOT + lane);
+        o_lft = __ldcg(own + HB_LFT + lane);
+        o_rgt = __ldcg(own + HB_RGT + lane);
     }
     int its = 0;
     const unsigned reached = tile_bfs(m[0], m[1], m[2], m[3], m[4], hl, hr, ht, hb, hs, 33, &its);
@@ -423,6 +427,13 @@ __device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int t
     __syncwarp();
 #pragma unroll 4
     for (int r = 0; r < 32; ++r) b.h[base + r * 32 + lane] = hs[r * 33 + lane];
+    {
+        int *own = b.hb + (size_t)t * 128;
+        own[HB_TOP + lane] = hs[lane];
+        own[HB_BOT + lane] = hs[31 * 33 + lane];
+        own[HB_LFT + lane] = hs[lane * 33];
+        own[HB_RGT + lane] = hs[lane * 33 + 31];
+    }
     const bool ch_top = __any_sync(FULL, hs[lane] != o_top);
     const bool ch_bot = __any_sync(FULL, hs[31 * 33 + lane] != o_bot);
     const bool ch_lft = __any_sync(FULL, hs[lane * 33] != o_lft);
@@ -487,10 +498,10 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
         s.e[r][lane] = __ldcg(b.exc + base + r * 32 + lane);
         s.h[r + 1][lane + 1] = __ldcg(b.h + base + r * 32 + lane);
     }
-    if (warp == 0) s.h[0][lane + 1] = g.nb[2] >= 0 ? __ldcg(b.h + (size_t)g.nb[2] * TPX + 31 * 32 + lane) : INF_H;
-    if (warp == 1) s.h[TILE_H + 1][lane + 1] = g.nb[3] >= 0 ? __ldcg(b.h + (size_t)g.nb[3] * TPX + lane) : INF_H;
-    if (warp == 2) s.h[lane + 1][0] = g.nb[0] >= 0 ? __ldcg(b.h + (size_t)g.nb[0] * TPX + lane * 32 + 31) : INF_H;
-    if (warp == 3) s.h[lane + 1][TILE_W + 1] = g.nb[1] >= 0 ? __ldcg(b.h + (size_t)g.nb[1] * TPX + lane * 32) : INF_H;
+    if (warp == 0) s.h[0][lane + 1] = g.nb[2] >= 0 ? __ldcg(b.hb + (size_t)g.nb[2] * 128 + HB_BOT + lane) : INF_H;
+    if (warp == 1) s.h[TILE_H + 1][lane + 1] = g.nb[3] >= 0 ? __ldcg(b.hb + (size_t)g.nb[3] * 128 + HB_TOP + lane) : INF_H;
+    if (warp == 2) s.h[lane + 1][0] = g.nb[0] >= 0 ? __ldcg(b.hb + (size_t)g.nb[0] * 128 + HB_RGT + lane) : INF_H;
+    if (warp == 3) s.h[lane + 1][TILE_W + 1] = g.nb[1] >= 0 ? __ldcg(b.hb + (size_t)g.nb[1] * 128 + HB_LFT + lane) : INF_H;
     if (warp < 4) s.halo_in[warp][lane] = 0;
     __syncthreads();
     c1 = clock64();
@@ -689,6 +700,12 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
         b.h[base + r * 32 + lane] = s.h[r + 1][lane + 1];
         write_tile_masks(b, t, r, c, e);
         if (e > 0) pos += (unsigned)e;
+    }
+    if (warp < 4) {  // the border lines, for the neighbours' halos
+        int *own = b.hb + (size_t)t * 128;
+        const int v = warp == 0 ? s.h[1][lane + 1] : warp == 1 ? s.h[TILE_H][lane + 1]
+                    : warp == 2 ? s.h[lane + 1][1] : s.h[lane + 1][TILE_W];
+        own[warp * 32 + lane] = v;  // HB_TOP, HB_BOT, HB_LFT, HB_RGT
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) pos += __shfl_down_sync(FULL, pos, o);
