@@ -477,6 +477,9 @@ __global__ void __launch_bounds__(TILE_THREADS, 5) k_build_img_b(Batch b, const 
     const ImgDesc d = b.img[im];
     const int lt = t - d.tile0;
     const int tx = lt % d.tiles_x, ty = lt / d.tiles_x;
+    if (threadIdx.x == 0)  // the tile's neighbours, for the solver
+        b.tile_nb[t] = make_int4(tx > 0 ? t - 1 : -1, tx < d.tiles_x - 1 ? t + 1 : -1, ty > 0 ? t - d.tiles_x : -1,
+                                 ty < d.tiles_y - 1 ? t + d.tiles_x : -1);
     const int W = d.W, H = d.H;
     const int x0 = tx * TILE_W, y0 = ty * TILE_H;
     const NlinkParams q = nlink_params(d.lambda, b.ist[im]);

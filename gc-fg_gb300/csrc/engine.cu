@@ -66,6 +66,17 @@ __device__ __forceinline__ TileGeo tile_geo(const Batch &b, int t) {
     return g;
 }
 
+// Neighbours of tile t from the per-tile table the builds fill (one load).
+__device__ __forceinline__ void tile_nbs(const Batch &b, int t, int nb[4]) {
+    const int4 v = __ldcg(b.tile_nb + t);
+    nb[0] = v.x;
+    nb[1] = v.y;
+    nb[2] = v.z;
+    nb[3] = v.w;
+}
+
+__device__ __forceinline__ int4 nb_of(const TileGeo &g) { return make_int4(g.nb[0], g.nb[1], g.nb[2], g.nb[3]); }
+
 __device__ __forceinline__ void set_error(const Batch &b, int code) {
     atomicExch(&b.ctl->err, 1);
     atomicCAS(&b.ctl->err_code, 0, code);
@@ -374,11 +385,11 @@ struct GrGeo {
     bool skip;
 };
 
-__device__ __forceinline__ void gr_prefetch(const Batch &b, int t, GrGeo &gg) {
-    const TileGeo g = tile_geo(b, t);
-    gg.skip = vload(&b.ist[g.img].done) != 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) gg.nb[k] = g.nb[k];
+__device__ __forceinline__ void gr_prefetch(const Batch &b, int t, GrGeo &gg, bool check_done) {
+    tile_nbs(b, t, gg.nb);
+    // only the first round can meet a finished image: a later round visits
+    // tiles queued by neighbours of the same image, which was visited
+    gg.skip = check_done && vload(&b.ist[__ldg(b.tile_img + t)].done) != 0;
 }
 
 // Exact distances of tile t given its halo; queues neighbours whose halo
@@ -448,7 +459,8 @@ __device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int t
 // Source-side reachability closure of tile t given the halo's reach bits.
 __device__ void reach_tile(const Batch &b, int t, bool round0, int tag_next, int slot_next) {
     const int lane = threadIdx.x & 31;
-    const TileGeo g = tile_geo(b, t);
+    GrGeo g;  // only the neighbours are used
+    tile_nbs(b, t, g.nb);
     unsigned m[6];
     load_tile_masks(b, t, m);
     const unsigned old = round0 ? 0u : __ldcg(b.reach + (size_t)t * 32 + lane);
@@ -489,7 +501,8 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
                           unsigned long long *st) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     long long c0 = clock64(), c1, cb = 0, cs = 0;
-    const TileGeo g = tile_geo(b, t);
+    GrGeo g;  // only the neighbours are used
+    tile_nbs(b, t, g.nb);
     const size_t base = (size_t)t * TPX;
 #pragma unroll
     for (int k = 0; k < ROWS_PER_WARP; ++k) {
@@ -806,7 +819,7 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
         for (int k = gwarp; k < nt; k += nwarps) {
             const int t = batch_tile(b, k);
             GrGeo g;
-            gr_prefetch(b, t, g);
+            gr_prefetch(b, t, g, true);
             if (g.skip) continue;
             const long long c0 = clock64();
             gr_run(b, t, g, true, G + 1, L_GR0 + ((G + 1) & 1), sm.w.hs[warp], st);
@@ -831,7 +844,7 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
                 const int t = b.lists[(size_t)slot * b.list_cap + idx];
                 const long long c0 = clock64();
                 GrGeo g;
-                gr_prefetch(b, t, g);
+                gr_prefetch(b, t, g, false);
                 gr_run(b, t, g, false, G + 1, L_GR0 + ((G + 1) & 1), sm.w.hs[warp], st);
                 if (lane == 0) {
                     stat_add(st, ST_CYC_GR, (unsigned long long)(clock64() - c0));
@@ -977,6 +990,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_build_arrays(Batch b, const in
     const int t = batch_tile(b, blockIdx.x);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const TileGeo g = tile_geo(b, t);
+    if (threadIdx.x == 0) b.tile_nb[t] = nb_of(g);
     const int W = b.img[g.img].W, H = b.img[g.img].H;
     unsigned long long idp = 0, rinit = 0, pos = 0;
     int bad = 0;
