@@ -90,7 +90,7 @@ struct Engine {
         std::vector<int> w, h;
         std::vector<double> lam;
         const void *ptr[4];
-        bool staging;
+        int kind;  // 0 device-resident run, 1 blocking host call, 2 asynchronous host call
         SolveParams prm;
         int grid;
         long long alloc_gen;
@@ -774,20 +774,16 @@ static gcfg_status run_batch_eager(Engine &e, int n, const int *W, const int *H,
     return e.status();
 }
 
-// The device part of a run (per-image counters reset, data term, build,
-// persistent solve, extraction, read-back of the per-image states) captured
-// once into a CUDA graph and replayed while the batch is the same: same
-// sizes, lambdas, buffers and solver settings.  The persistent solver already
-// runs the whole push / local relabel / global relabel loop without host round
-// trips; the graph removes the remaining per-kernel launch work.  Host
-// copies of the host entry points stay outside the graph.
-static gcfg_status run_batch_graph(Engine &e, int n, const int *W, const int *H, const double *lam,
-                                   const uint8_t *rgb, const uint8_t *scrib, uint8_t *smin, uint8_t *smax,
-                                   int64_t *flows, gcfg_result *res, bool staging) {
-    // host inputs are copied in outside the graph; only device buffers are baked in
-    const void *ptr[4] = {staging ? nullptr : rgb, staging ? nullptr : scrib, smin, smax};
+// The cached graph of a batch signature (sizes, lambdas, the buffers `ptr`,
+// the kind of run, solver settings), laying the batch out and capturing the
+// device part (per-image counter reset, data term, build, solve, read-back
+// of the per-image states, extraction) first when needed.  *out is null when
+// the device cannot capture; runs then continue without graphs.
+static gcfg_status graph_for(Engine &e, int n, const int *W, const int *H, const double *lam,
+                             const void *const ptr[4], int kind, bool staging, Engine::GraphEntry **out) {
+    *out = nullptr;
     auto same = [&](const Engine::GraphEntry &g) {
-        if ((int)g.w.size() != n || g.staging != staging || g.grid != e.max_grid || g.alloc_gen != e.alloc_gen)
+        if ((int)g.w.size() != n || g.kind != kind || g.grid != e.max_grid || g.alloc_gen != e.alloc_gen)
             return false;
         if (memcmp(&g.prm, &e.prm, sizeof(SolveParams)) != 0) return false;
         for (int k = 0; k < 4; ++k)
@@ -808,9 +804,11 @@ static gcfg_status run_batch_graph(Engine &e, int n, const int *W, const int *H,
         }
     }
     if (!hit) {
-        const uint8_t *drgb = staging ? e.d_rgb : rgb, *dscrib = staging ? e.d_scrib : scrib;
-        uint8_t *dmin = staging ? (smin ? e.d_smin : nullptr) : smin;
-        uint8_t *dmax = staging ? (smax ? e.d_smax : nullptr) : smax;
+        // the device buffers the graph bakes in
+        const uint8_t *drgb = staging ? e.d_rgb : (const uint8_t *)ptr[0];
+        const uint8_t *dscrib = staging ? e.d_scrib : (const uint8_t *)ptr[1];
+        uint8_t *dmin = staging ? (ptr[2] ? e.d_smin : nullptr) : (uint8_t *)ptr[2];
+        uint8_t *dmax = staging ? (ptr[3] ? e.d_smax : nullptr) : (uint8_t *)ptr[3];
         if (!e.cap_st) GCFG_CK(cudaStreamCreateWithFlags(&e.cap_st, cudaStreamNonBlocking));
         // the layout uploads were queued on the caller's stream; the graph is
         // launched there too, after them
@@ -825,8 +823,10 @@ static gcfg_status run_batch_graph(Engine &e, int n, const int *W, const int *H,
             if (cudaMemsetAsync(e.d_ist, 0, (size_t)n * sizeof(ImgState), e.st) != cudaSuccess) rc = GCFG_ERR_CUDA;
             if (rc == GCFG_OK) rc = e.build_images(drgb, dscrib);
             if (rc == GCFG_OK) rc = e.solve();
-            if (rc == GCFG_OK && (dmin || dmax)) rc = launch_extract(e.batch(), dmin, dmax, nullptr, e.st);
+            // the state read-back first: a label download queued after the
+            // graph must not hold it up on the copy engine
             if (rc == GCFG_OK) rc = e.readback();
+            if (rc == GCFG_OK && (dmin || dmax)) rc = launch_extract(e.batch(), dmin, dmax, nullptr, e.st);
             if (cudaStreamEndCapture(e.cap_st, &g) != cudaSuccess && rc == GCFG_OK) rc = GCFG_ERR_CUDA;
         }
         e.st = user;
@@ -839,11 +839,10 @@ static gcfg_status run_batch_graph(Engine &e, int n, const int *W, const int *H,
         }
         if (g) cudaGraphDestroy(g);
         if (rc != GCFG_OK) {
-            // capture is not available here: run without graphs from now on
             cudaGetLastError();
             e.graph_broken = true;
             e.drop_graphs();
-            return run_batch_eager(e, n, W, H, lam, rgb, scrib, smin, smax, flows, res, staging);
+            return GCFG_OK;
         }
         if ((int)e.graphs.size() >= Engine::MAX_GRAPHS) {  // drop the least recently used
             size_t old = 0;
@@ -857,7 +856,7 @@ static gcfg_status run_batch_graph(Engine &e, int n, const int *W, const int *H,
         ge.h.assign(H, H + n);
         ge.lam.assign(lam, lam + n);
         for (int k = 0; k < 4; ++k) ge.ptr[k] = ptr[k];
-        ge.staging = staging;
+        ge.kind = kind;
         ge.prm = e.prm;
         ge.grid = e.max_grid;
         ge.alloc_gen = e.alloc_gen;
@@ -870,6 +869,25 @@ static gcfg_status run_batch_graph(Engine &e, int n, const int *W, const int *H,
     }
     hit->last_use = ++e.graph_clock;
     e.graph_kernels = hit->kernels;
+    *out = hit;
+    return GCFG_OK;
+}
+
+// The device part of a run (per-image counters reset, data term, build,
+// persistent solve, read-back of the per-image states, extraction) captured
+// once into a CUDA graph and replayed while the batch is the same: same
+// sizes, lambdas, buffers and solver settings.  The persistent solver already
+// runs the whole push / local relabel / global relabel loop without host round
+// trips; the graph removes the remaining per-kernel launch work.  Host
+// copies of the host entry points stay outside the graph.
+static gcfg_status run_batch_graph(Engine &e, int n, const int *W, const int *H, const double *lam,
+                                   const uint8_t *rgb, const uint8_t *scrib, uint8_t *smin, uint8_t *smax,
+                                   int64_t *flows, gcfg_result *res, bool staging) {
+    // host inputs are copied in outside the graph; only device buffers are baked in
+    const void *ptr[4] = {staging ? nullptr : rgb, staging ? nullptr : scrib, smin, smax};
+    Engine::GraphEntry *hit = nullptr;
+    GCFG_TRY(graph_for(e, n, W, H, lam, ptr, staging ? 1 : 0, staging, &hit));
+    if (!hit) return run_batch_eager(e, n, W, H, lam, rgb, scrib, smin, smax, flows, res, staging);
     if (staging) {
         GCFG_CK(cudaMemcpyAsync(e.d_rgb, rgb, (size_t)e.n_px * 3, cudaMemcpyHostToDevice, e.st));
         GCFG_CK(cudaMemcpyAsync(e.d_scrib, scrib, (size_t)e.n_px, cudaMemcpyHostToDevice, e.st));
@@ -895,10 +913,6 @@ static gcfg_status run_batch_graph(Engine &e, int n, const int *W, const int *H,
     return e.status();
 }
 
-// Host-buffer entry point for several images: the groups' uploads (copy
-// stream) overlap the data term and graph build of the groups already on the
-// device, and after the solve each group's extraction is followed by its
-// download while the next group is extracted.
 // Pieces of the host entry points for many images (the layout and groups
 // are in place): uploads of the groups' inputs on cp_st, each group's data
 // term and build on st as soon as its inputs are in, and per group the
@@ -991,8 +1005,9 @@ static gcfg_status run_batch_staged(Engine &e, int n, const int *W, const int *H
 // batch then computes in one pass on st (data term, build, solve, extraction
 // over all its images, as the device-resident path does), and its labels are
 // downloaded on dn_st while the next batch computes.
-static gcfg_status submit_staged(Engine &e, Engine::Flight &f, int n, const int *W, const int *H, const double *lam,
-                                 const uint8_t *h_rgb, const uint8_t *h_scrib, uint8_t *h_smin, uint8_t *h_smax) {
+static gcfg_status submit_staged(Engine &e, Engine::Flight &f, int slot, int n, const int *W, const int *H,
+                                 const double *lam, const uint8_t *h_rgb, const uint8_t *h_scrib, uint8_t *h_smin,
+                                 uint8_t *h_smax) {
     GCFG_TRY(grow_host(e.h_ctl, e.ch_ctl, 1));
     if (!e.ev0) GCFG_CK(cudaEventCreate(&e.ev0));
     if (!e.ev1) GCFG_CK(cudaEventCreate(&e.ev1));
@@ -1000,6 +1015,33 @@ static gcfg_status submit_staged(Engine &e, Engine::Flight &f, int n, const int 
     if (!e.dn_st) GCFG_CK(cudaStreamCreateWithFlags(&e.dn_st, cudaStreamNonBlocking));
     for (cudaEvent_t *ev : {&f.ev_up, &f.ev_ext, &f.ev_dn})
         if (!*ev) GCFG_CK(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+    if (e.graph_on && !e.graph_broken && !prof_on()) {
+        // keyed by the run set and the outputs wanted (the set's buffers may
+        // not exist before its first layout; any reallocation drops every
+        // graph, so the buffers a graph bakes in stay the set's own)
+        const void *ptr[4] = {reinterpret_cast<const void *>((uintptr_t)slot + 1), nullptr,
+                              h_smin ? reinterpret_cast<const void *>(1) : nullptr,
+                              h_smax ? reinterpret_cast<const void *>(1) : nullptr};
+        Engine::GraphEntry *hit = nullptr;
+        GCFG_TRY(graph_for(e, n, W, H, lam, ptr, 2, true, &hit));
+        if (hit) {
+            GCFG_CK(cudaMemcpyAsync(e.d_rgb, h_rgb, (size_t)e.n_px * 3, cudaMemcpyHostToDevice, e.cp_st));
+            GCFG_CK(cudaMemcpyAsync(e.d_scrib, h_scrib, (size_t)e.n_px, cudaMemcpyHostToDevice, e.cp_st));
+            GCFG_CK(cudaEventRecord(f.ev_up, e.cp_st));
+            GCFG_CK(cudaStreamWaitEvent(e.st, f.ev_up, 0));
+            GCFG_CK(cudaEventRecord(e.ev0, e.st));
+            GCFG_CK(cudaGraphLaunch(hit->exec, e.st));
+            g_launches.fetch_add(hit->kernels, std::memory_order_relaxed);
+            e.graph_replays++;
+            GCFG_CK(cudaEventRecord(f.ev_ext, e.st));
+            GCFG_CK(cudaStreamWaitEvent(e.dn_st, f.ev_ext, 0));
+            if (h_smin) GCFG_CK(cudaMemcpyAsync(h_smin, e.d_smin, (size_t)e.n_px, cudaMemcpyDeviceToHost, e.dn_st));
+            if (h_smax) GCFG_CK(cudaMemcpyAsync(h_smax, e.d_smax, (size_t)e.n_px, cudaMemcpyDeviceToHost, e.dn_st));
+            GCFG_CK(cudaEventRecord(e.ev1, e.st));
+            GCFG_CK(cudaEventRecord(f.ev_dn, e.dn_st));
+            return GCFG_OK;
+        }
+    }
     GCFG_CK(cudaEventRecord(e.ev0, e.st));
     GCFG_TRY(e.layout(n, W, H, lam, true, true));
     GCFG_CK(cudaMemcpyAsync(e.d_rgb, h_rgb, (size_t)e.n_px * 3, cudaMemcpyHostToDevice, e.cp_st));
@@ -1029,7 +1071,7 @@ static gcfg_status batch_submit(Engine &e, int n, const int *W, const int *H, co
     Engine::Flight &f = e.flight[slot];
     if (f.busy) return GCFG_ERR_STATE;  // two batches in flight already
     if (slot == 1) e.swap_set(e.alt);
-    const gcfg_status rc = submit_staged(e, f, n, W, H, lam, h_rgb, h_scrib, h_smin, h_smax);
+    const gcfg_status rc = submit_staged(e, f, slot, n, W, H, lam, h_rgb, h_scrib, h_smin, h_smax);
     if (slot == 1) e.swap_set(e.alt);
     if (rc != GCFG_OK) return rc;
     f.busy = true;

@@ -98,3 +98,30 @@ def test_in_flight_rules():
     t = bs.submit_host(*b2[:3], *i2)
     assert np.array_equal(bs.wait(t)[0], r2[0])
     bs.close()
+
+
+def test_two_in_flight_graph_replay():
+    """With CUDA graphs on, each run set replays its own captured graph;
+    results equal the blocking call across alternating batch sizes."""
+    batches = [_batch(20, 5600), _batch(9, 5700)]
+    bs = gcfg.BatchSolver(32, max(b[4].size for b in batches))
+    refs = [_sync_ref(bs, b) for b in batches]
+    bs.set_graph(True)
+    ins = [(_pinned(b[3]), _pinned(b[4])) for b in batches]
+    order = [0, 0, 0, 1, 1, 0, 0, 0, 0]
+    outs = [(_pinned(np.zeros(batches[k][4].size, np.uint8)), _pinned(np.zeros(batches[k][4].size, np.uint8)))
+            for k in order]
+    pending = []
+    for j, k in enumerate(order):
+        Ws, Hs, lams, _, _ = batches[k]
+        pending.append((bs.submit_host(Ws, Hs, lams, ins[k][0], ins[k][1], outs[j][0], outs[j][1]), j, k))
+        if len(pending) == 2:
+            t0, j0, k0 = pending.pop(0)
+            assert np.array_equal(bs.wait(t0)[0], refs[k0][0])
+            assert np.array_equal(outs[j0][0], refs[k0][1]) and np.array_equal(outs[j0][1], refs[k0][2])
+    for t0, j0, k0 in pending:
+        assert np.array_equal(bs.wait(t0)[0], refs[k0][0])
+        assert np.array_equal(outs[j0][0], refs[k0][1]) and np.array_equal(outs[j0][1], refs[k0][2])
+    info = bs.graph_info()
+    assert info["active"] and info["replays"] >= len(order) - 4
+    bs.close()
