@@ -287,12 +287,11 @@ __device__ __forceinline__ uint32_t sigma_chunk(uintptr_t lo, uintptr_t hi, uint
 // k + 3 inside the image, minus the pairs that straddle a row end; down pairs
 // = sum of (B[k] - B[k + 3W])^2 over the chunk's bytes above the image's last
 // row.  Per 4 bytes: one __vabsdiffu4 + __dp4a for each direction.
-__global__ void __launch_bounds__(256) k_hist_sigma_b(const uint8_t *__restrict__ rgb,
+__global__ void __launch_bounds__(256, 6) k_hist_sigma_b(const uint8_t *__restrict__ rgb,
                                                       const uint8_t *__restrict__ scrib,
                                                       const ImgDesc *__restrict__ img,
                                                       const int2 *__restrict__ chunk_map,
                                                       int *__restrict__ hist, ImgState *ist) {
-    __shared__ __align__(16) int sh[2 * NBINS];
     __shared__ uint4 keep[(3 * CHUNK_PX + 15) / 16 + 1];  // the chunk's bytes from its 16-aligned start
     const int2 cm = __ldg(chunk_map + blockIdx.x);  // (image, chunk within the image)
     const int im = cm.x;
@@ -303,10 +302,6 @@ __global__ void __launch_bounds__(256) k_hist_sigma_b(const uint8_t *__restrict_
     const long long pix0 = img[im].pix0;
     const uint8_t *base = rgb + 3 * pix0;
     const bool do_hist = scrib != nullptr;
-    if (do_hist) {
-        int4 *s4 = reinterpret_cast<int4 *>(sh);
-        for (int i = threadIdx.x; i < 2 * NBINS / 4; i += blockDim.x) s4[i] = make_int4(0, 0, 0, 0);
-    }
     const int lane = threadIdx.x & 31;
     unsigned long long acc = 0;
     {
@@ -337,10 +332,15 @@ __global__ void __launch_bounds__(256) k_hist_sigma_b(const uint8_t *__restrict_
         }
     }
     if (do_hist) {
-        __syncthreads();  // the cleared histogram and the kept colours
+        __syncthreads();  // the kept colours
         const uint8_t *kb = reinterpret_cast<const uint8_t *>(keep) + (int)(((uintptr_t)base + 3 * p0) & 15);
-        // the chunk's scribble bytes, 16 per lane; scribbled pixels are
-        // binned one byte position per round, as long as any lane has one left
+        int *dst = hist + (size_t)im * 2 * NBINS;
+        // The chunk's scribble bytes, 16 per lane.  Scribbles come in short
+        // runs (strips, squares), so a lane's 16 bytes are often all marked
+        // while most lanes have none: the warp lists its marked bytes (a
+        // prefix sum of the lanes' counts) and bins them 32 per round, lane k
+        // taking item k of the list.  Equal bins of a round add once, with a
+        // fire-and-forget global add.
         const uintptr_t slo = (uintptr_t)(scrib + pix0), shi = slo + (uintptr_t)npx;
         const uintptr_t s0 = slo + (uintptr_t)p0;
         const uintptr_t saw = s0 & ~(uintptr_t)15;
@@ -348,50 +348,60 @@ __global__ void __launch_bounds__(256) k_hist_sigma_b(const uint8_t *__restrict_
         for (int v0 = (int)threadIdx.x - lane; v0 < nsv; v0 += blockDim.x) {
             const int vi = v0 + lane;
             const uintptr_t a = saw + 16 * (uintptr_t)vi;
-            uint4 sv = vi < nsv ? vec_in(a, slo, shi) : make_uint4(0, 0, 0, 0);
-            const uint32_t sw[4] = {sv.x, sv.y, sv.z, sv.w};
-            unsigned todo = 0;  // bit b: byte b is a scribble (1 or 2) of this chunk
-            const int o = (int)(a - s0);
+            const uint4 sv = vi < nsv ? vec_in(a, slo, shi) : make_uint4(0, 0, 0, 0);
+            const int o = (int)(a - s0);  // chunk pixel of the vector's byte 0
+            // bit b: byte b is 1 or 2 and lies in the chunk (4 bytes at a time:
+            // per-byte equality masks, then the bytes' top bits packed by a multiply)
+            unsigned todo = 0;
+            {
+                const uint32_t sw[4] = {sv.x, sv.y, sv.z, sv.w};
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                uint32_t w = sw[j];
-                if (w) w &= byte_mask(o + 4 * j, 0, n);
-#pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                    const uint32_t sc = (w >> (8 * b)) & 0xFFu;
-                    if (sc == 1u || sc == 2u) todo |= 1u << (4 * j + b);
+                for (int j = 0; j < 4; ++j) {
+                    uint32_t m = __vcmpeq4(sw[j], 0x01010101u) | __vcmpeq4(sw[j], 0x02020202u);
+                    if (o < 0 || o + 16 > n) m &= byte_mask(o + 4 * j, 0, n);
+                    const uint32_t x = (m >> 7) & 0x01010101u;
+                    todo |= ((x * 0x01020408u) >> 24) << (4 * j);
                 }
             }
-            while (__any_sync(0xffffffffu, todo != 0)) {
+            const int cnt = __popc(todo);
+            int incl = cnt;  // inclusive prefix sum of the counts over the warp
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += v;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            for (int r0 = 0; r0 < total; r0 += 32) {  // warp-uniform
+                const int k = r0 + lane;
+                // owner: the first lane whose inclusive sum exceeds k
+                int lo = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int probe = __shfl_sync(0xffffffffu, incl, lo + step - 1);
+                    if (probe <= k) lo += step;
+                }
+                const unsigned om = __shfl_sync(0xffffffffu, todo, lo);
+                const int oincl = __shfl_sync(0xffffffffu, incl, lo);
+                const int oo = __shfl_sync(0xffffffffu, o, lo);
+                const uint32_t w0 = __shfl_sync(0xffffffffu, sv.x, lo), w1 = __shfl_sync(0xffffffffu, sv.y, lo);
+                const uint32_t w2 = __shfl_sync(0xffffffffu, sv.z, lo), w3 = __shfl_sync(0xffffffffu, sv.w, lo);
                 int key = -1;
-                if (todo) {
-                    const int b = __ffs(todo) - 1;
-                    todo &= todo - 1;
-                    const uint32_t wb = b < 8 ? (b < 4 ? sv.x : sv.y) : (b < 12 ? sv.z : sv.w);
+                if (k < total) {
+                    // the (k - owner's exclusive sum)-th marked byte of the owner
+                    const int b = __fns(om, 0, k - (oincl - __popc(om)) + 1);
+                    const uint32_t wb = b < 8 ? (b < 4 ? w0 : w1) : (b < 12 ? w2 : w3);
                     const int sc = (int)((wb >> (8 * (b & 3))) & 0xFFu);
-                    const int q = o + b;  // pixel of the chunk
+                    const int q = oo + b;  // pixel of the chunk
                     const uint32_t col = (uint32_t)kb[3 * q] | ((uint32_t)kb[3 * q + 1] << 8) |
                                          ((uint32_t)kb[3 * q + 2] << 16);
                     key = (sc - 1) * NBINS + color_binw(col);
                 }
                 const unsigned same = __match_any_sync(0xffffffffu, key);
-                if (key >= 0 && lane == __ffs(same) - 1) atomicAdd(&sh[key], __popc(same));
+                if (key >= 0 && lane == __ffs(same) - 1) atomicAdd(dst + key, __popc(same));
             }
         }
     }
     warp_atomic_add_u64(&ist[im].sigma_sum, acc);
-    if (do_hist) {
-        __syncthreads();
-        int *dst = hist + (size_t)im * 2 * NBINS;
-        const int4 *s4 = reinterpret_cast<const int4 *>(sh);
-        for (int i = threadIdx.x; i < 2 * NBINS / 4; i += blockDim.x) {
-            const int4 v = s4[i];
-            if (v.x) atomicAdd(dst + 4 * i + 0, v.x);
-            if (v.y) atomicAdd(dst + 4 * i + 1, v.y);
-            if (v.z) atomicAdd(dst + 4 * i + 2, v.z);
-            if (v.w) atomicAdd(dst + 4 * i + 3, v.w);
-        }
-    }
 }
 
 // Per-bin t-link tables (one block per image, double precision).
