@@ -431,6 +431,7 @@ __device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int t
     int its = 0;
     const unsigned reached = tile_bfs(m[0], m[1], m[2], m[3], m[4], hl, hr, ht, hb, hs, 33, &its);
     if (lane == 0) stat_add(st, ST_BFS_IT_GR, (unsigned long long)its);
+    b.hfin[(size_t)t * 32 + lane] = reached;  // finite heights of this row (the extraction's S_max)
     int act = __popc(m[5] & reached);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) act += __shfl_down_sync(FULL, act, o);
@@ -1049,10 +1050,10 @@ __global__ void __launch_bounds__(TILE_THREADS) k_extract(Batch b, uint8_t *smin
         const int r = warp + 8 * k;
         const int x = g.tx * TILE_W + lane, y = g.ty * TILE_H + r;
         if (x >= W || y >= H) continue;
-        const size_t p = (size_t)t * TPX + r * 32 + lane;
         const size_t i = (size_t)out0 + (size_t)y * W + x;
         const bool inside = x > 0 && y > 0 && x < W - 1 && y < H - 1;
-        const uint8_t sm = inside && b.h[p] >= INF_H;
+        // h == INF: not reached by the last global relabel of this tile
+        const uint8_t sm = inside && !((b.hfin[(size_t)t * 32 + r] >> lane) & 1u);
         if (smin) smin[i] = (uint8_t)((b.reach[(size_t)t * 32 + r] >> lane) & 1u);
         if (smax) smax[i] = sm;
         if (label) label[i] = sm;

@@ -88,6 +88,7 @@ struct Batch {
     int *h;
     int *hb;                 // per tile, its border heights [4][32]: top row, bottom row, left, right column
     int4 *tile_nb;           // per tile: left, right, upper, lower neighbour tile (-1: image edge); set by the builds
+    unsigned *hfin;          // per tile, 32 row masks: finite height after its last global-relabel visit
     unsigned *reach;         // 32 row masks per tile (source-side reachability)
     // Per-tile row bitmask planes, kept exact by every writer of cap/exc:
     // tmask[(t*6 + k)*32 + row], k = 0..3 residual capacity toward left,

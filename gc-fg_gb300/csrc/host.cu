@@ -57,6 +57,7 @@ struct Engine {
     int *d_h = nullptr; size_t c_h = 0;
     int *d_hb = nullptr; size_t c_hb = 0;
     int4 *d_tnb = nullptr; size_t c_tnb = 0;
+    unsigned *d_hfin = nullptr; size_t c_hfin = 0;
     unsigned *d_reach = nullptr; size_t c_reach = 0;
     unsigned *d_tmask = nullptr; size_t c_tmask = 0;
     int *d_tact = nullptr; size_t c_tact = 0;
@@ -208,7 +209,7 @@ struct Engine {
         if (dn_st) cudaStreamDestroy(dn_st);
         dn_st = nullptr;
         cudaFree(d_img); cudaFree(d_ist); cudaFree(d_cmap); cudaFree(d_tile_img);
-        cudaFree(d_cap); cudaFree(d_exc); cudaFree(d_h); cudaFree(d_hb); cudaFree(d_tnb); cudaFree(d_reach);
+        cudaFree(d_cap); cudaFree(d_exc); cudaFree(d_h); cudaFree(d_hb); cudaFree(d_tnb); cudaFree(d_hfin); cudaFree(d_reach);
         cudaFree(d_tmask); cudaFree(d_tact); cudaFree(d_tpos);
         cudaFree(d_lists);
         cudaFree(d_mpush); cudaFree(d_mgr); cudaFree(d_ctl);
@@ -237,7 +238,7 @@ struct Engine {
         cudaFree(d_iota);
         d_iota = nullptr;
         d_img = nullptr; d_ist = nullptr; d_cmap = nullptr; d_tile_img = nullptr;
-        d_cap = nullptr; d_exc = nullptr; d_h = nullptr; d_hb = nullptr; d_tnb = nullptr; d_reach = nullptr;
+        d_cap = nullptr; d_exc = nullptr; d_h = nullptr; d_hb = nullptr; d_tnb = nullptr; d_hfin = nullptr; d_reach = nullptr;
         d_tmask = nullptr; d_tact = nullptr; d_tpos = nullptr;
         d_lists = nullptr;
         d_mpush = d_mgr = nullptr; d_ctl = nullptr;
@@ -266,7 +267,7 @@ struct Engine {
     }
 
     std::vector<const void *> buffers() const {
-        return {d_img, d_ist, d_cmap, d_tile_img, d_cap, d_exc, d_h, d_hb, d_tnb, d_reach, d_tmask, d_tact, d_tpos,
+        return {d_img, d_ist, d_cmap, d_tile_img, d_cap, d_exc, d_h, d_hb, d_tnb, d_hfin, d_reach, d_tmask, d_tact, d_tpos,
                 d_lists, d_mpush, d_mgr, d_ctl, d_hist, d_dpl, d_dnl, d_rgb, d_scrib, d_smin, d_smax,
                 h_img, h_ist, h_chunk, h_cmap, h_tile_img, h_ctl};
     }
@@ -293,6 +294,7 @@ struct Engine {
             GCFG_TRY(grow(d_h, c_h, (size_t)tiles * TPX));
             GCFG_TRY(grow(d_hb, c_hb, (size_t)tiles * 4 * 32));
             GCFG_TRY(grow(d_tnb, c_tnb, (size_t)tiles));
+            GCFG_TRY(grow(d_hfin, c_hfin, (size_t)tiles * 32));
             GCFG_TRY(grow(d_reach, c_reach, (size_t)tiles * 32));
             GCFG_TRY(grow(d_tmask, c_tmask, (size_t)tiles * 6 * 32));
             GCFG_TRY(grow(d_tact, c_tact, tiles));
@@ -442,6 +444,7 @@ struct Engine {
         b.h = d_h;
         b.hb = d_hb;
         b.tile_nb = d_tnb;
+        b.hfin = d_hfin;
         b.reach = d_reach;
         b.tmask = d_tmask;
         b.tile_act = d_tact;

@@ -39,7 +39,8 @@ constexpr size_t OFF_EXC = OFF_CAP + align256(T * TPX * sizeof(int4));
 constexpr size_t OFF_H = OFF_EXC + align256(T * TPX * sizeof(int));
 constexpr size_t OFF_HB = OFF_H + align256(T * TPX * sizeof(int));
 constexpr size_t OFF_TNB = OFF_HB + align256(T * 4 * 32 * sizeof(int));
-constexpr size_t OFF_REACH = OFF_TNB + align256(T * sizeof(int4));
+constexpr size_t OFF_HFIN = OFF_TNB + align256(T * sizeof(int4));
+constexpr size_t OFF_REACH = OFF_HFIN + align256(T * 32 * sizeof(unsigned));
 constexpr size_t OFF_TMASK = OFF_REACH + align256(T * 32 * sizeof(unsigned));
 constexpr size_t OFF_TACT = OFF_TMASK + align256(T * 6 * 32 * sizeof(unsigned));
 constexpr size_t OFF_TPOS = OFF_TACT + align256(T * sizeof(int));
@@ -130,6 +131,7 @@ extern "C" gcfg_status gcfg_solve_noalloc(int w, int h, const int32_t *d_dp, con
     b.h = reinterpret_cast<int *>(base + OFF_H);
     b.hb = reinterpret_cast<int *>(base + OFF_HB);
     b.tile_nb = reinterpret_cast<int4 *>(base + OFF_TNB);
+    b.hfin = reinterpret_cast<unsigned *>(base + OFF_HFIN);
     b.reach = reinterpret_cast<unsigned *>(base + OFF_REACH);
     b.tmask = reinterpret_cast<unsigned *>(base + OFF_TMASK);
     b.tile_act = reinterpret_cast<int *>(base + OFF_TACT);

@@ -39,9 +39,9 @@ namespace gcfg {
 namespace {
 
 // Device bytes per tile of a resident image: tile arena (cap, exc, h, border
-// heights, neighbours, reach, mask planes, counters, marks, owner) + its 1024 pixel slots
+// heights, neighbours, finite-height masks, reach, mask planes, counters, marks, owner) + its 1024 pixel slots
 // of RGB, scribble and two label maps.
-constexpr size_t ARENA_TILE_BYTES = sizeof(int4) * TPX + 2 * sizeof(int) * TPX + 4 * 32 * sizeof(int) + sizeof(int4) + 32 * 4 +
+constexpr size_t ARENA_TILE_BYTES = sizeof(int4) * TPX + 2 * sizeof(int) * TPX + 4 * 32 * sizeof(int) + sizeof(int4) + 32 * 4 + 32 * 4 +
                                     6 * 32 * 4 + sizeof(int) + sizeof(unsigned long long) + 3 * sizeof(int);
 constexpr size_t PX_BYTES = 3 + 1 + 2;
 constexpr size_t TILE_BYTES = ARENA_TILE_BYTES + TPX * PX_BYTES;
@@ -200,6 +200,7 @@ struct Server {
     int4 *cap = nullptr;
     int *exc = nullptr, *h = nullptr, *hb = nullptr;
     int4 *tnb = nullptr;
+    unsigned *hfin = nullptr;
     unsigned *reach = nullptr, *tmask = nullptr;
     int *tact = nullptr;
     unsigned long long *tpos = nullptr;
@@ -267,6 +268,7 @@ Batch arena_batch(Server &s) {
     b.h = s.h;
     b.hb = s.hb;
     b.tile_nb = s.tnb;
+    b.hfin = s.hfin;
     b.reach = s.reach;
     b.tmask = s.tmask;
     b.tile_act = s.tact;
@@ -574,7 +576,7 @@ void shutdown_server(Server *s) {
         cudaFreeHost(L->h_il); cudaFreeHost(L->h_cmap); cudaFreeHost(L->h_desc); cudaFreeHost(L->h_ist);
         delete L;
     }
-    cudaFree(s->cap); cudaFree(s->exc); cudaFree(s->h); cudaFree(s->hb); cudaFree(s->tnb); cudaFree(s->reach); cudaFree(s->tmask); cudaFree(s->tact);
+    cudaFree(s->cap); cudaFree(s->exc); cudaFree(s->h); cudaFree(s->hb); cudaFree(s->tnb); cudaFree(s->hfin); cudaFree(s->reach); cudaFree(s->tmask); cudaFree(s->tact);
     cudaFree(s->tpos); cudaFree(s->mpush); cudaFree(s->mgr); cudaFree(s->tile_img);
     cudaFree(s->rgb); cudaFree(s->scrib); cudaFree(s->smin); cudaFree(s->smax);
     cudaFree(s->img); cudaFree(s->ist); cudaFree(s->hist); cudaFree(s->dpl); cudaFree(s->dnl);
@@ -608,7 +610,7 @@ gcfg_status gcfg_serve_create(const gcfg_serve_config *cfg, gcfg_server **out) {
     const size_t T = (size_t)s->tiles_cap, NS = (size_t)cfg->max_sessions;
     gcfg_status rc = GCFG_OK;
     auto chk = [&](gcfg_status r) { if (rc == GCFG_OK) rc = r; };
-    chk(dalloc(s->cap, T * TPX)); chk(dalloc(s->exc, T * TPX)); chk(dalloc(s->h, T * TPX)); chk(dalloc(s->hb, T * 4 * 32)); chk(dalloc(s->tnb, T));
+    chk(dalloc(s->cap, T * TPX)); chk(dalloc(s->exc, T * TPX)); chk(dalloc(s->h, T * TPX)); chk(dalloc(s->hb, T * 4 * 32)); chk(dalloc(s->tnb, T)); chk(dalloc(s->hfin, T * 32));
     chk(dalloc(s->reach, T * 32)); chk(dalloc(s->tmask, T * 6 * 32)); chk(dalloc(s->tact, T));
     chk(dalloc(s->tpos, T)); chk(dalloc(s->mpush, T)); chk(dalloc(s->mgr, T)); chk(dalloc(s->tile_img, T));
     chk(dalloc(s->rgb, 3 * (size_t)s->px_cap)); chk(dalloc(s->scrib, (size_t)s->px_cap));
