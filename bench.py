@@ -30,9 +30,14 @@ roofline: the kernel with the largest device time in a profiled step;
         / its CUDA-event time; peak = MEASURED_PEAKS.json hbm_gbs.
 cpu_baseline: the oracle's Boykov-Kolmogorov solver (oracle/, the CPU
         checker) on a bounded sample of the same images, one host thread.
---impl reference: the reference has no CPU implementation of this path and
-        its CUDA path cannot be built on the GPU host, so this arm times the
-        CPU port (oracle BK) on all host threads, one image per thread.
+reference_cuda: the reference's own CUDA path on the same GPU (its kernels
+        compiled from its sources into a cubin, launched in GC_Optimize's
+        order by oracle/refgpu/ref_gpu.cpp), one image at a time, on a bounded
+        sample of the workload; its labels are compared with this build's
+        S_max.
+--impl reference: the reference has no CPU implementation of this path, so
+        this arm times the CPU port (oracle BK) on all host threads, one image
+        per thread.
 """
 from __future__ import annotations
 
@@ -199,6 +204,48 @@ def cpu_baseline(views, lams, budget_s=10.0):
             break
     dt = time.perf_counter() - t0
     return px / dt / 1e6, k, dt, flows
+
+
+def reference_cuda_leg(views, lams, smax_all, offs, budget_s=15.0):
+    """The reference's own CUDA path (its kernels compiled from its sources,
+    oracle/ref_cuda.py) on the same GPU: GC_Init -> GC_SetGraph ->
+    GC_Optimize -> GC_End per image, one image at a time as the reference's
+    applications run it, on a bounded sample of the workload's images (in
+    workload order until budget_s of reference solve time).  The t-links and
+    n-links are computed on the host by the oracle (outside every timed span).
+    value = pixels / the sum of the GC_SetGraph + GC_Optimize wall times; the
+    reference's labels are compared with this build's S_max."""
+    import oracle as O
+    import ref_cuda
+    why = ref_cuda.unavailable()
+    if why:
+        return {"unavailable": why}
+    px, ms_solve, ms_loop, ms_all, its, n_eq, n_conv, k = 0, 0.0, 0.0, 0.0, [], 0, 0, 0
+    for i, (rgb, scrib) in enumerate(views):
+        dp, dn = O.tlinks(rgb, scrib)
+        up, down, left, right = O.nlinks(rgb, float(lams[i]))
+        r = ref_cuda.solve(dp, dn, up=up, down=down, left=left, right=right, max_seconds=30.0)
+        k += 1
+        if r["rc"] != 0:
+            return {"unavailable": f"image {i}: {r['status']}", "images": k}
+        H, W = scrib.shape
+        o = int(offs[i])
+        n_eq += bool(np.array_equal(r["label"].astype(np.uint8).reshape(-1), smax_all[o:o + W * H]))
+        n_conv += r["converged"]
+        px += W * H
+        ms_solve += r["ms_solve"]
+        ms_loop += r["ms_loop"]
+        ms_all += r["ms_init"] + r["ms_solve"] + r["ms_end"]
+        its.append(r["iterations"])
+        if ms_solve > budget_s * 1e3:
+            break
+    return {"value": px / (ms_solve / 1e3) / 1e6, "unit": UNIT, "images": k, "pixels": px,
+            "ms_per_image": ms_solve / k, "loop_only_mpixel_s": px / (ms_loop / 1e3) / 1e6,
+            "with_init_end_mpixel_s": px / (ms_all / 1e3) / 1e6,
+            "iterations_median": float(np.median(its)), "converged": n_conv, "labels_equal_smax": n_eq,
+            "how": "the reference's kernels (GraphCutKernels.cu, compiled from its sources for sm_103a) "
+                   "launched in GC_Optimize's order with its blocking flag copies; one image at a time, "
+                   "wall clock of GC_SetGraph + GC_Optimize (labels to the host included)"}
 
 
 def _sleep_until(now, ta):
@@ -443,8 +490,8 @@ def run_reference_arm(args, spec, rank, world):
             "config": {"workload": args.workload, "desc": spec["desc"]},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                              "sample": f"{len(views)} image(s) x {reps} per step, oracle Boykov-Kolmogorov, "
-                                       "one image per host thread; the reference has no CPU solver and its "
-                                       "CUDA path cannot be built on the GPU host"},
+                                       "one image per host thread; the reference has no CPU solver (its CUDA "
+                                       "path is timed in the reference_cuda leg of the default arm)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -466,6 +513,8 @@ def main():
                     help="push_rounds,max_sweeps,sweeps_per_local_relabel[,blocks_per_sm[,relabel_first"
                          "[,push_only]]] for the batch (skips the autotuner)")
     ap.add_argument("--serve-requests", type=int, default=1200)
+    ap.add_argument("--ref-cuda-budget", type=float, default=15.0,
+                    help="seconds of reference CUDA solve time for the reference_cuda leg (0 skips it)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_info()
@@ -716,6 +765,9 @@ def main():
                                 "sample": f"{n_chk} image(s) of the workload in {secs:.1f} s, oracle "
                                           "Boykov-Kolmogorov, 1 thread"}
         line["parity"] = {"flows_equal_oracle": ok, "images_checked": len(set(i for i, _ in cflows))}
+        if args.ref_cuda_budget > 0:
+            line["reference_cuda"] = reference_cuda_leg(views, lams, d_smax.cpu().numpy(), offs,
+                                                        budget_s=args.ref_cuda_budget)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

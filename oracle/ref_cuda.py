@@ -1,0 +1,96 @@
+"""The reference's own CUDA path on the GPU (test and benchmark infrastructure).
+
+The reference's kernels (GraphCutKernels.cu) are compiled from the reference
+checkout into ``oracle/_ref/gc_ref_kernels.cubin`` by
+``oracle/refgpu/build_ref_gpu.sh``; ``oracle/refgpu/ref_gpu.cpp`` restates
+the reference's host code (GC_Init / GC_SetGraph / GC_Optimize / GC_End,
+GraphCut.cu:187-568) launch for launch over those kernels, with every loop
+bounded.  It is the reference's CUDA path timed beside this repository's on
+the same GPU; it is never part of the product.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "refgpu", "ref_gpu.cpp")
+LIB_PATH = os.path.join(HERE, "librefgpu.so")
+CUBIN = os.path.join(HERE, "_ref", "gc_ref_kernels.cubin")
+
+STATUS = {0: "ok", 1: "invalid", 2: "cuda error", 3: "iteration or time cap reached", 4: "kernels not loaded"}
+
+
+class Stats(C.Structure):
+    _fields_ = [("iterations", C.c_longlong), ("global_relabels", C.c_longlong),
+                ("gr_launches", C.c_longlong), ("spread_launches", C.c_longlong),
+                ("initial_energy", C.c_int), ("final_energy", C.c_int), ("converged", C.c_int),
+                ("pad", C.c_int), ("ms_init", C.c_double), ("ms_solve", C.c_double),
+                ("ms_loop", C.c_double), ("ms_end", C.c_double)]
+
+
+def build(force: bool = False) -> str:
+    """Compile the host driver (plain C++ against the CUDA runtime, static
+    cudart) into oracle/librefgpu.so.  Needs no reference source."""
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(SRC):
+        return LIB_PATH
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    subprocess.check_call([os.environ.get("NVCC", "nvcc"), "-O2", "-std=c++17", "-Xcompiler", "-fPIC",
+                           "-shared", "-o", tmp, SRC])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def unavailable() -> str | None:
+    """None when the reference's CUDA path can run here, else why not."""
+    if not os.path.exists(CUBIN):
+        return ("the reference's kernels were not compiled (oracle/_ref/gc_ref_kernels.cubin is built "
+                "from the reference checkout)")
+    return None
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        why = unavailable()
+        if why:
+            raise RuntimeError(why)
+        build()
+        L = C.CDLL(LIB_PATH)
+        P = C.c_void_p
+        L.refgpu_load.argtypes = [C.c_char_p]
+        L.refgpu_solve.argtypes = [C.c_int, C.c_int, P, P, C.c_int, P, P, P, P, P, C.c_longlong, C.c_double,
+                                   C.POINTER(Stats)]
+        rc = L.refgpu_load(CUBIN.encode())
+        if rc:
+            raise RuntimeError(f"loading the reference's kernels failed: {STATUS.get(rc, rc)}")
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def solve(dp, dn, penalty=0, up=None, down=None, left=None, right=None, max_iters=5_000_000,
+          max_seconds=60.0):
+    """Runs the reference's GC_Init -> GC_SetGraph -> GC_Optimize -> GC_End on
+    host arrays (H, W) int32.  Returns dict(label, energy (the printed final
+    energy level), status, converged, stats...)."""
+    dp = np.ascontiguousarray(dp, np.int32)
+    dn = np.ascontiguousarray(dn, np.int32)
+    H, W = dp.shape
+    arrs = [None if a is None else np.ascontiguousarray(a, np.int32) for a in (up, down, left, right)]
+    label = np.zeros((H, W), np.int32)
+    st = Stats()
+    rc = lib().refgpu_solve(W, H, _p(dp), _p(dn), int(penalty), *[_p(a) for a in arrs], _p(label),
+                            int(max_iters), float(max_seconds), C.byref(st))
+    out = {k: getattr(st, k) for k, _ in Stats._fields_ if k != "pad"}
+    out.update(status=STATUS.get(rc, rc), rc=rc, label=label, energy=st.final_energy)
+    return out
