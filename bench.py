@@ -58,9 +58,12 @@ METRIC = "exact-min-cut Mpixel/s"
 UNIT = "Mpixel/s"
 
 # Algorithmic bytes per pixel per unit of work (int32 layout):
-#   global-relabel tile visit: read 4 caps + excess (20 B), write height (4 B)
-#   push tile visit: read 4 caps + excess + height (24 B), write the same (24 B)
-#   reach tile visit: read 4 caps + excess (20 B)
+#   global relabel: read 4 caps + excess (20 B), write height (4 B), once per
+#     pixel per global relabel; a tile that the BFS frontier visits again in
+#     a later round of the same relabel is overhead, not algorithmic bytes
+#   push tile visit (a tile active in a push round; push and local relabel
+#     fused): read 4 caps + excess + height (24 B), write the same (24 B)
+#   source reachability (cut): read 4 caps + excess (20 B), once per pixel at most
 #   count pass: read excess + height (8 B)
 #   build: read RGB (3 B), write 4 caps + excess (20 B)
 #   extract: read height (4 B) + reach bit, write two label bytes (2 B)
@@ -705,11 +708,10 @@ def main():
     tiles_total = int(sum(((int(w) + 31) // 32) * ((int(h) + 31) // 32) for w, h in zip(Ws, Hs)))
     recs = pres if isinstance(pres, list) else [pres]
     solve_bytes = 0
-    for r in (recs[:1] if batched else recs):
-        solve_bytes += 1024 * (B_GR * r["gr_tiles"] + B_PUSH * r["push_tiles"] + B_REACH * r["reach_tiles"])
-        solve_bytes += 1024 * B_COUNT * r["global_relabels"] * (tiles_total if batched else
-                                                                 ((int(Ws[recs.index(r)]) + 31) // 32) *
-                                                                 ((int(Hs[recs.index(r)]) + 31) // 32))
+    for j, r in enumerate(recs[:1] if batched else recs):
+        nt = tiles_total if batched else ((int(Ws[j]) + 31) // 32) * ((int(Hs[j]) + 31) // 32)
+        solve_bytes += 1024 * (B_GR * min(r["gr_tiles"], nt * r["global_relabels"]) + B_PUSH * r["push_tiles"] +
+                               B_REACH * min(r["reach_tiles"], nt) + B_COUNT * nt * r["global_relabels"])
     alg = {"solve": solve_bytes, "build": B_BUILD * 1024 * tiles_total, "extract": B_EXTRACT * px_per_step,
            "hist": 4 * px_per_step, "sigma": 3 * px_per_step}
     launches_dom = max(prof[dom]["launches"], 1)
