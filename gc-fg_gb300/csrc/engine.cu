@@ -194,9 +194,43 @@ struct PhaseClock {
 // Rl/Rr/Ru/Rd: row masks of residual capacity toward left/right/up/down.
 // sink: nodes of this row at level 1 (e < 0).
 // hl/hr: level of this row's left/right halo node; ht/hb: level of the halo
-// node above/below column `lane`.  Levels of the tile are written to
-// hs[row * stride + col]; unreachable nodes get INF.  Returns this row's
-// reached set.
+// node above/below column `lane`.
+
+// One BFS expansion: the nodes outside S that have a residual edge into S or
+// into a halo node of level <= lvl (they get level lvl + 1).
+__device__ __forceinline__ unsigned bfs_expand(unsigned S, int lvl, unsigned Rl, unsigned Rr, unsigned Ru,
+                                               unsigned Rd, int hl, int hr, int ht, int hb, int lane) {
+    const unsigned T = __ballot_sync(FULL, ht <= lvl);
+    const unsigned B = __ballot_sync(FULL, hb <= lvl);
+    unsigned up = __shfl_up_sync(FULL, S, 1);
+    unsigned dn = __shfl_down_sync(FULL, S, 1);
+    if (lane == 0) up = T;
+    if (lane == 31) dn = B;
+    const unsigned lin = (S << 1) | (hl <= lvl ? 1u : 0u);
+    const unsigned rin = (S >> 1) | (hr <= lvl ? 0x80000000u : 0u);
+    return ((Rl & lin) | (Rr & rin) | (Ru & up) | (Rd & dn)) & ~S;
+}
+
+// Smallest halo level above lvl (warp-uniform), INF when there is none.
+__device__ __forceinline__ int bfs_next_halo(int lvl, int hl, int hr, int ht, int hb) {
+    int cand = INF_H;
+    if (hl > lvl) cand = min(cand, hl);
+    if (hr > lvl) cand = min(cand, hr);
+    if (ht > lvl) cand = min(cand, ht);
+    if (hb > lvl) cand = min(cand, hb);
+    return __reduce_min_sync(FULL, cand);
+}
+
+// Both BFS loops below take two levels per round (lvl -> lvl + 1 -> lvl + 2,
+// the second expansion from the first's result) and decide once, so the
+// loop-carried path holds one vote and one branch per two levels.  When
+// neither level grows the frontier, the level jumps to the next halo level
+// above lvl + 1; when only the first grows, the next round's expansions at
+// lvl + 2 and lvl + 3 find what a jump would (halo levels <= lvl + 1 have
+// already been used).
+
+// Levels of the tile are written to hs[row * stride + col]; unreachable nodes
+// get INF.  Returns this row's reached set.
 __device__ unsigned tile_bfs(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd, unsigned sink, int hl,
                          int hr, int ht, int hb, int *hs, int stride, int *iters) {
     const int lane = threadIdx.x & 31;
@@ -208,26 +242,16 @@ __device__ unsigned tile_bfs(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd,
     int lvl = 1;
     int it = 0;
     for (; it < BFS_MAX_ITERS; ++it) {
-        const unsigned T = __ballot_sync(FULL, ht <= lvl);
-        const unsigned B = __ballot_sync(FULL, hb <= lvl);
-        unsigned up = __shfl_up_sync(FULL, S, 1);
-        unsigned dn = __shfl_down_sync(FULL, S, 1);
-        if (lane == 0) up = T;
-        if (lane == 31) dn = B;
-        const unsigned lin = (S << 1) | (hl <= lvl ? 1u : 0u);
-        const unsigned rin = (S >> 1) | (hr <= lvl ? 0x80000000u : 0u);
-        unsigned nw = ((Rl & lin) | (Rr & rin) | (Ru & up) | (Rd & dn)) & ~S;
-        if (__any_sync(FULL, nw != 0)) {
-            S |= nw;
-            ++lvl;
-            for (; nw; nw &= nw - 1) row[__ffs(nw) - 1] = lvl;
+        unsigned nw1 = bfs_expand(S, lvl, Rl, Rr, Ru, Rd, hl, hr, ht, hb, lane);
+        const unsigned S1 = S | nw1;
+        unsigned nw2 = bfs_expand(S1, lvl + 1, Rl, Rr, Ru, Rd, hl, hr, ht, hb, lane);
+        if (__any_sync(FULL, (nw1 | nw2) != 0)) {
+            S = S1 | nw2;
+            for (; nw1; nw1 &= nw1 - 1) row[__ffs(nw1) - 1] = lvl + 1;
+            for (; nw2; nw2 &= nw2 - 1) row[__ffs(nw2) - 1] = lvl + 2;
+            lvl += 2;
         } else {
-            int cand = INF_H;
-            if (hl > lvl) cand = min(cand, hl);
-            if (hr > lvl) cand = min(cand, hr);
-            if (ht > lvl) cand = min(cand, ht);
-            if (hb > lvl) cand = min(cand, hb);
-            const int nxt = __reduce_min_sync(FULL, cand);
+            const int nxt = bfs_next_halo(lvl + 1, hl, hr, ht, hb);
             if (nxt >= INF_H) break;
             lvl = nxt;
         }
@@ -238,11 +262,12 @@ __device__ unsigned tile_bfs(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd,
 
 // The push visits' exact local relabel: the same levels as tile_bfs, but
 // instead of storing each new pixel's level on the spot (a divergent loop on
-// the loop-carried path of a single warp) the k-th expansion (k < NREC)
-// records the reached rows srec[k][row] and its level lv[k]; expansions past
-// NREC store their pixels' levels directly, as tile_bfs does.  sfin gets the
-// final reached rows.  Returns the number of records (warp-uniform); the
-// whole block then fills in the heights (heights_from_records).
+// the loop-carried path of a single warp) the k-th expansion that grows the
+// frontier records the reached rows srec[k][row] and its level lv[k], while
+// two more records fit (k < NREC); later expansions store their pixels'
+// levels directly, as tile_bfs does.  sfin gets the final reached rows.  Returns the number of
+// records (warp-uniform); the whole block then fills in the heights
+// (heights_from_records).
 constexpr int NREC = 48;
 __device__ int tile_bfs_rec(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd, unsigned sink, int hl, int hr,
                             int ht, int hb, int *hs, int stride, unsigned (*srec)[32], int *lv, unsigned *sfin,
@@ -252,32 +277,31 @@ __device__ int tile_bfs_rec(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd, 
     unsigned S = sink;
     int lvl = 1, nrec = 0, it = 0;
     for (; it < BFS_MAX_ITERS; ++it) {
-        const unsigned T = __ballot_sync(FULL, ht <= lvl);
-        const unsigned B = __ballot_sync(FULL, hb <= lvl);
-        unsigned up = __shfl_up_sync(FULL, S, 1);
-        unsigned dn = __shfl_down_sync(FULL, S, 1);
-        if (lane == 0) up = T;
-        if (lane == 31) dn = B;
-        const unsigned lin = (S << 1) | (hl <= lvl ? 1u : 0u);
-        const unsigned rin = (S >> 1) | (hr <= lvl ? 0x80000000u : 0u);
-        unsigned nw = ((Rl & lin) | (Rr & rin) | (Ru & up) | (Rd & dn)) & ~S;
-        if (__any_sync(FULL, nw != 0)) {
-            S |= nw;
-            ++lvl;
-            if (nrec < NREC) {
-                srec[nrec][lane] = S;
-                if (lane == 0) lv[nrec] = lvl;
-                ++nrec;
+        const unsigned nw1 = bfs_expand(S, lvl, Rl, Rr, Ru, Rd, hl, hr, ht, hb, lane);
+        const unsigned S1 = S | nw1;
+        const unsigned nw2 = bfs_expand(S1, lvl + 1, Rl, Rr, Ru, Rd, hl, hr, ht, hb, lane);
+        const bool a1 = __any_sync(FULL, nw1 != 0);
+        const bool a2 = __any_sync(FULL, nw2 != 0);
+        if (a1 || a2) {
+            S = S1 | nw2;
+            if (nrec + 2 <= NREC) {  // the usual case: both levels recorded
+                if (a1) {
+                    srec[nrec][lane] = S1;
+                    if (lane == 0) lv[nrec] = lvl + 1;
+                    ++nrec;
+                }
+                if (a2) {
+                    srec[nrec][lane] = S;
+                    if (lane == 0) lv[nrec] = lvl + 2;
+                    ++nrec;
+                }
             } else {
-                for (; nw; nw &= nw - 1) row[__ffs(nw) - 1] = lvl;
+                for (unsigned m = nw1; m; m &= m - 1) row[__ffs(m) - 1] = lvl + 1;
+                for (unsigned m = nw2; m; m &= m - 1) row[__ffs(m) - 1] = lvl + 2;
             }
+            lvl += 2;
         } else {
-            int cand = INF_H;
-            if (hl > lvl) cand = min(cand, hl);
-            if (hr > lvl) cand = min(cand, hr);
-            if (ht > lvl) cand = min(cand, ht);
-            if (hb > lvl) cand = min(cand, hb);
-            const int nxt = __reduce_min_sync(FULL, cand);
+            const int nxt = bfs_next_halo(lvl + 1, hl, hr, ht, hb);
             if (nxt >= INF_H) break;
             lvl = nxt;
         }
