@@ -42,7 +42,7 @@ static gcfg_status grow_host(T *&p, size_t &cap, size_t need) {
 
 struct Engine {
     cudaStream_t st = nullptr;
-    SolveParams prm{64, 4, 64, 16, 0, 1 << 20, 0};
+    SolveParams prm = kDefaultSolveParams;
 
     int n_img = 0, n_tiles = 0;
     long long n_px = 0, total_chunks = 0;
@@ -1268,11 +1268,11 @@ gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const i
     if (rc == GCFG_OK) rc = time_cfg(cur, cur_bps, &ms_default);
     float best = ms_default;
     static const int c_push[] = {2, 4, 8, 16};
-    static const int c_sweeps[] = {16, 32, 64, 128};
+    static const int c_sweeps[] = {16, 24, 32, 64, 128};
     static const int c_bfs[] = {2, 4, 8, 16, 32};
     for (int pass = 0; pass < 2 && rc == GCFG_OK; ++pass) {
         for (int which = 0; which < 6 && rc == GCFG_OK; ++which) {
-            const int nc = which == 3 ? per_sm : which == 2 ? 5 : which >= 4 ? 2 : 4;
+            const int nc = which == 3 ? per_sm : which == 1 || which == 2 ? 5 : which >= 4 ? 2 : 4;
             for (int c = 0; c < nc && rc == GCFG_OK; ++c) {
                 SolveParams p = cur;
                 int bps = cur_bps;

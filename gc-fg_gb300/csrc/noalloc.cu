@@ -156,7 +156,7 @@ extern "C" gcfg_status gcfg_solve_noalloc(int w, int h, const int32_t *d_dp, con
     if (err) return GCFG_ERR_INVALID;  // capacities outside [0, GCFG_MAX_CAP]
 
     GCFG_CK(cudaMemsetAsync(base + OFF_CTL, 0, sizeof(Ctl), st));
-    SolveParams prm{64, 4, 64, 16, 0, 1 << 20, 0};
+    SolveParams prm = kDefaultSolveParams;
     GCFG_TRY(launch_solve(b, prm, (int)tiles, st));
     GCFG_TRY(launch_extract(b, nullptr, nullptr, d_label, st));
     ImgState s;

@@ -419,7 +419,7 @@ gcfg_status run_batch(Lane &L, std::vector<Req> &batch, const std::vector<Sessio
     b.ilist = L.d_il;
     b.n_ilist = n;
     GCFG_CK(cudaMemsetAsync(L.ctl, 0, sizeof(Ctl), st));
-    SolveParams prm{64, 4, 64, 16, 0, 1 << 20, 0};
+    SolveParams prm = kDefaultSolveParams;
     GCFG_TRY(launch_solve(b, prm, nt, st, s.cfg.lanes > 1 ? solve_grid_blocks(1 << 30) / s.cfg.lanes : 0));
     GCFG_TRY(launch_extract(b, s.smin, s.smax, nullptr, st));
     for (int k = 0; k < n; ++k) {

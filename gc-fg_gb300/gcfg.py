@@ -380,7 +380,7 @@ class BatchSolver:
                "gcfg_batch_graph_info")
         return {"active": bool(a.value), "captures": c.value, "replays": r.value, "kernels_per_replay": k.value}
 
-    def set_solver(self, push_rounds_per_gr=4, max_tile_sweeps=64, sweeps_per_local_relabel=16,
+    def set_solver(self, push_rounds_per_gr=2, max_tile_sweeps=24, sweeps_per_local_relabel=4,
                    blocks_per_sm=0, local_relabel_first=0, push_only=0, **_ignored):
         """Solver settings (keys as autotune() returns them)."""
         t = Tuning(push_rounds_per_gr=int(push_rounds_per_gr), max_tile_sweeps=int(max_tile_sweeps),
