@@ -731,6 +731,17 @@ def main():
                 "avg_launch_us": prof[dom]["ms"] / launches_dom * 1e3,
                 "share_of_step": prof[dom]["ms"] / step_prof_ms if step_prof_ms else None,
                 "kernels_ms": {k: round(v["ms"], 4) for k, v in prof.items() if v["launches"]}}
+    # the solver's two main phases on their own (device timers of the phases; same byte accounting)
+    r_ph = recs[0]
+    nt0 = tiles_total if batched else ((int(Ws[0]) + 31) // 32) * ((int(Hs[0]) + 31) // 32)
+    ph = {}
+    for name, nbytes, ms in (("global_relabel", 1024 * B_GR * min(r_ph["gr_tiles"], nt0 * r_ph["global_relabels"]),
+                              r_ph["t_global_relabel_ms"]),
+                             ("push", 1024 * B_PUSH * r_ph["push_tiles"], r_ph["t_push_ms"])):
+        if ms > 0:
+            gbs = nbytes / (ms / 1e3) / 1e9
+            ph[name] = {"achieved": round(gbs, 1), "frac": round(gbs / peak, 4), "ms": ms, "bytes": nbytes}
+    roofline["solve_phases"] = ph
 
     r0 = recs[0]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

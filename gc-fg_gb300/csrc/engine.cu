@@ -522,8 +522,11 @@ __device__ void reach_tile(const Batch &b, int t, bool round0, int tag_next, int
 // Push/relabel on one tile (whole block)
 // ---------------------------------------------------------------------------
 
+// The block's next queue entry is taken (thread 0, from take_ctr) when the
+// sweeps end, so that the atomic overlaps the write-back; it is left in s.idx
+// for the caller.
 __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int phase, SmemPush &s,
-                          unsigned long long *st) {
+                          unsigned long long *st, int *take_ctr) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     long long c0 = clock64(), c1, cb = 0, cs = 0;
     GrGeo g;  // only the neighbours are used
@@ -725,6 +728,8 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
         need_bfs = !pushed_any;  // stalled: nothing was pushed in this sweep
     }
     const long long c2 = clock64();
+    int next_idx = 0;
+    if (threadIdx.x == 0) next_idx = atomicAdd(take_ctr, 1);
     cs = c2 - c1 - cb;
     // ---- write back (and refresh the tile's mask planes and excess sum) ----
     unsigned long long pos = 0;
@@ -784,6 +789,7 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
             enqueue(b, b.mark_push, (phase + 1) % 3, phase + 1, nt);
     }
     if (any && threadIdx.x == 0) enqueue(b, b.mark_push, (phase + 2) % 3, phase + 2, t);
+    if (threadIdx.x == 0) s.idx = next_idx;
     __syncthreads();
     if (threadIdx.x == 0) {
         stat_add(st, ST_PUSH_TILES, 1ull);
@@ -947,17 +953,21 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
                 const int slot = p % 3;
                 last = p;
                 const int n = vload(&ctl->size[slot]);
-                for (;;) {
+                {
                     const long long ct = clock64();
                     if (threadIdx.x == 0) sm.p.idx = atomicAdd(&ctl->take[slot], 1);
                     __syncthreads();
-                    const int idx = sm.p.idx;
-                    __syncthreads();
                     if (threadIdx.x == 0) stat_add(st, ST_CYC_TAKE, (unsigned long long)(clock64() - ct));
-                    if (idx >= n) break;
-                    push_tile(b, b.lists[(size_t)slot * b.list_cap + idx], prm, p, sm.p, st);
-                    __syncthreads();
                 }
+                for (;;) {
+                    // the entry taken before (the first one above, later ones by
+                    // the previous visit); no thread writes s.idx again before
+                    // every thread has read it (push_tile's barriers come first)
+                    const int idx = sm.p.idx;
+                    if (idx >= n) break;
+                    push_tile(b, b.lists[(size_t)slot * b.list_cap + idx], prm, p, sm.p, st, &ctl->take[slot]);
+                }
+                __syncthreads();
                 if (!grid_sync(b, 1u << slot)) return;
                 if (gtid == 0) ctl->push_phases++;
                 if (vload(&ctl->size[(p + 1) % 3]) == 0 && vload(&ctl->size[(p + 2) % 3]) == 0) {
