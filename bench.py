@@ -67,6 +67,8 @@ UNIT = "Mpixel/s"
 #   push tile visit (a tile active in a push round; push and local relabel
 #     fused): read 4 caps + excess + height (24 B), write the same (24 B)
 #   source reachability (cut): read 4 caps + excess (20 B), once per pixel at most
+#   sink reachability (the termination check after push rounds, which also
+#     gives S_max): the same 20 B, once per pixel per check
 #   count pass: read excess + height (8 B)
 #   build: read RGB (3 B), write 4 caps + excess (20 B)
 #   extract: read height (4 B) + reach bit, write two label bytes (2 B)
@@ -715,7 +717,8 @@ def main():
     for j, r in enumerate(recs[:1] if batched else recs):
         nt = tiles_total if batched else ((int(Ws[j]) + 31) // 32) * ((int(Hs[j]) + 31) // 32)
         solve_bytes += 1024 * (B_GR * min(r["gr_tiles"], nt * r["global_relabels"]) + B_PUSH * r["push_tiles"] +
-                               B_REACH * min(r["reach_tiles"], nt) + B_COUNT * nt * r["global_relabels"])
+                               B_REACH * min(r["reach_tiles"], nt) + B_COUNT * nt * r["global_relabels"] +
+                               B_REACH * nt * r.get("closure_checks", 0))
     alg = {"solve": solve_bytes, "build": B_BUILD * 1024 * tiles_total, "extract": B_EXTRACT * px_per_step,
            "hist": 4 * px_per_step, "sigma": 3 * px_per_step}
     launches_dom = max(prof[dom]["launches"], 1)
@@ -735,7 +738,8 @@ def main():
     r_ph = recs[0]
     nt0 = tiles_total if batched else ((int(Ws[0]) + 31) // 32) * ((int(Hs[0]) + 31) // 32)
     ph = {}
-    for name, nbytes, ms in (("global_relabel", 1024 * B_GR * min(r_ph["gr_tiles"], nt0 * r_ph["global_relabels"]),
+    for name, nbytes, ms in (("global_relabel", 1024 * (B_GR * min(r_ph["gr_tiles"], nt0 * r_ph["global_relabels"]) +
+                                                     B_REACH * nt0 * r_ph.get("closure_checks", 0)),
                               r_ph["t_global_relabel_ms"]),
                              ("push", 1024 * B_PUSH * r_ph["push_tiles"], r_ph["t_push_ms"])):
         if ms > 0:
@@ -763,7 +767,8 @@ def main():
                          "api": "one blocking host call per step (gcfg_batch_run_host / gcfg_seg_run_host)"},
             "roofline": roofline, "clocks": clk, "gpu_launches": launches,
             "solver": {k: (round(r0[k], 4) if isinstance(r0[k], float) else r0[k])
-                       for k in ("global_relabels", "gr_sweeps", "push_rounds", "cut_sweeps", "push_tiles",
+                       for k in ("global_relabels", "closure_checks", "closure_ends", "gr_sweeps", "push_rounds",
+                                 "cut_sweeps", "push_tiles",
                                  "gr_tiles", "reach_tiles", "push_sweeps", "push_local_relabels",
                                  "t_global_relabel_ms", "t_count_ms", "t_push_ms", "t_reach_ms",
                                  "cyc_load", "cyc_local_relabel", "cyc_sweeps", "cyc_writeback",

@@ -518,6 +518,49 @@ __device__ void reach_tile(const Batch &b, int t, bool round0, int tag_next, int
     enqueue_warp(b, b.mark_gr, slot_next, tag_next, nbt, lane < 4 && out && nbt >= 0);
 }
 
+// Sink-side reachability closure of tile t: the pixels that can reach a
+// sink-connected pixel (e < 0) along residual edges, written to hfin (the
+// complement of S_max inside the image).  The expansion of tile_bfs without
+// levels.  round0: the neighbours' sets are not known yet, so the halo starts
+// from their sink-connected pixels; later rounds read their hfin rows, all
+// written by this pass.  A neighbour is queued when this tile's set grows on
+// the border it shares (the sets only grow, so the rounds converge).
+__device__ void sink_reach_tile(const Batch &b, int t, bool round0, int tag_next, int slot_next) {
+    const int lane = threadIdx.x & 31;
+    int nb[4];
+    tile_nbs(b, t, nb);
+    unsigned m[6];
+    load_tile_masks(b, t, m);
+    const unsigned old = round0 ? 0u : __ldcg(b.hfin + (size_t)t * 32 + lane);
+    auto halo_row = [&](int nt, int row) -> unsigned {
+        if (nt < 0) return 0u;
+        return round0 ? mask_word(b, nt, 4, row) : __ldcg(b.hfin + (size_t)nt * 32 + row);
+    };
+    const unsigned T = halo_row(nb[2], 31), B = halo_row(nb[3], 0);
+    const unsigned lbit = halo_row(nb[0], lane) >> 31;         // left tile, column 31
+    const unsigned rbit = (halo_row(nb[1], lane) & 1u) << 31;  // right tile, column 0
+    const unsigned Rl = m[0], Rr = m[1], Ru = m[2], Rd = m[3];
+    unsigned S = m[4] | old;
+    for (int it = 0; it < BFS_MAX_ITERS; ++it) {
+        unsigned up = __shfl_up_sync(FULL, S, 1);
+        unsigned dn = __shfl_down_sync(FULL, S, 1);
+        if (lane == 0) up = T;
+        if (lane == 31) dn = B;
+        const unsigned nw = ((Rl & ((S << 1) | lbit)) | (Rr & ((S >> 1) | rbit)) | (Ru & up) | (Rd & dn)) & ~S;
+        if (!__any_sync(FULL, nw != 0)) break;
+        S |= nw;
+    }
+    b.hfin[(size_t)t * 32 + lane] = S;
+    const unsigned fresh = S & ~old;
+    const bool out_l = __any_sync(FULL, (fresh & 1u) != 0);
+    const bool out_r = __any_sync(FULL, (fresh & 0x80000000u) != 0);
+    const bool out_u = __any_sync(FULL, lane == 0 && fresh != 0);
+    const bool out_d = __any_sync(FULL, lane == 31 && fresh != 0);
+    const int nbt = lane == 0 ? nb[0] : lane == 1 ? nb[1] : lane == 2 ? nb[2] : nb[3];
+    const bool out = lane == 0 ? out_l : lane == 1 ? out_r : lane == 2 ? out_u : out_d;
+    enqueue_warp(b, b.mark_gr, slot_next, tag_next, nbt, lane < 4 && out && nbt >= 0);
+}
+
 // ---------------------------------------------------------------------------
 // Push/relabel on one tile (whole block)
 // ---------------------------------------------------------------------------
@@ -806,6 +849,96 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
 // The persistent solve kernel
 // ---------------------------------------------------------------------------
 
+// Termination check without distances, run after push rounds.  An image
+// whose pixels with excess can none of them reach the sink is finished: its
+// preflow is maximum.  A sink-side reachability closure (bit-parallel, no
+// heights) decides that and gives S_max, far more cheaply than the exact
+// global relabel that would otherwise find it; images that fail the check go
+// on to that relabel.  Also leaves each checked image's exact sum of positive
+// excess.  Returns 1 when every image is finished, 0 when some are not, -1
+// on an error (recorded in the control block).  Called by every thread of the
+// grid; kept out of line so that its registers do not add to the solver's.
+__device__ __noinline__ int closure_check(const Batch &b, const SolveParams &prm, int &G, unsigned long long *st) {
+    Ctl *ctl = b.ctl;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gwarp = blockIdx.x * 8 + warp, nwarps = gridDim.x * 8;
+    const int swarp = warp * gridDim.x + blockIdx.x;
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+    const int nt = batch_ntiles(b);
+    (void)st;
+    for (int k = gtid; k < batch_nimg(b); k += nthreads) {
+        const int i = batch_img(b, k);
+        if (!b.ist[i].done) {
+            b.ist[i].pos_excess = 0;
+            b.ist[i].active = 0;
+        }
+    }
+    if (gtid == 0) ctl->open_images = 0;
+    for (int k = gwarp; k < nt; k += nwarps) {
+        const int t = batch_tile(b, k);
+        if (vload(&b.ist[__ldg(b.tile_img + t)].done)) continue;  // warp-uniform
+        sink_reach_tile(b, t, true, G + 1, L_GR0 + ((G + 1) & 1));
+    }
+    if (!grid_sync(b, 0)) return -1;
+    ++G;
+    for (int k = 1;; ++k) {
+        const int slot = L_GR0 + (G & 1);
+        const int n = vload(&ctl->size[slot]);
+        if (n == 0) break;
+        if (k > prm.max_rounds) {
+            if (gtid == 0) set_error(b, ERRC_GR_ROUNDS);
+            return -1;
+        }
+        for (int idx = swarp; idx < n; idx += nwarps)
+            sink_reach_tile(b, b.lists[(size_t)slot * b.list_cap + idx], false, G + 1, L_GR0 + ((G + 1) & 1));
+        if (!grid_sync(b, 1u << slot)) return -1;
+        ++G;
+    }
+    // per image: any pixel with excess inside the closure (warp per tile), and
+    // the exact sum of positive excess (lane per tile)
+    for (int k = gwarp; k < nt; k += nwarps) {
+        const int t = batch_tile(b, k);
+        const int img = __ldg(b.tile_img + t);
+        if (vload(&b.ist[img].done)) continue;  // warp-uniform
+        const unsigned live = __ldcg(b.hfin + (size_t)t * 32 + lane) & mask_word(b, t, 5, lane);
+        if (__any_sync(FULL, live != 0) && lane == 0) b.ist[img].active = 1;
+    }
+    for (int kb = gtid - lane; kb < nt; kb += nthreads) {  // warp-uniform
+        const int k = kb + lane;
+        int img = -1;
+        unsigned long long pos = 0;
+        if (k < nt) {
+            const int t = batch_tile(b, k);
+            img = __ldg(b.tile_img + t);
+            if (vload(&b.ist[img].done)) img = -1;
+            else pos = __ldcg(b.tile_pos + t);
+        }
+        unsigned todo = __ballot_sync(FULL, img >= 0 && pos != 0);
+        while (todo) {
+            const int leader = __ffs(todo) - 1;
+            const int limg = __shfl_sync(FULL, img, leader);
+            const bool mine = ((todo >> lane) & 1u) && img == limg;
+            unsigned long long vp = mine ? pos : 0ull;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) vp += __shfl_xor_sync(FULL, vp, o);
+            if (lane == leader) atomicAdd(&b.ist[limg].pos_excess, vp);
+            todo &= ~__ballot_sync(FULL, mine);
+        }
+    }
+    if (!grid_sync(b, 0)) return -1;
+    for (int k = gtid; k < batch_nimg(b); k += nthreads) {
+        const int i = batch_img(b, k);
+        if (b.ist[i].done) continue;
+        if (*(volatile unsigned long long *)&b.ist[i].active == 0) b.ist[i].done = 1;
+        else atomicAdd(&ctl->open_images, 1);
+    }
+    if (gtid == 0) ctl->closure_checks++;
+    if (!grid_sync(b, 0)) return -1;
+    if (vload(&ctl->open_images) != 0) return 0;
+    if (gtid == 0) ctl->closure_ends++;
+    return 1;
+}
+
 #ifndef GCFG_SOLVE_MIN_BLOCKS
 #define GCFG_SOLVE_MIN_BLOCKS 4   // blocks of the persistent kernel per SM (register budget)
 #endif
@@ -838,6 +971,15 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
     int G = 0;  // global relabel round counter (tags of the tile frontier)
     bool finished = false;
     for (int outer = 0; outer < prm.max_outer; ++outer) {
+        if (outer > 0) {
+            const int rc = closure_check(b, prm, G, st);
+            if (rc < 0) return;
+            clk.charge(&ctl->t_gr);
+            if (rc > 0) {
+                finished = true;
+                break;
+            }
+        }
         // ------------------------ exact global relabel ------------------------
         for (int k = gtid; k < batch_nimg(b); k += nthreads) {
             const int i = batch_img(b, k);

@@ -59,7 +59,9 @@ struct Ctl {
     unsigned long long push_tiles, gr_tiles, reach_tiles;
     int gr_rounds, push_phases, reach_rounds, outer_iters;
     int global_relabels;
-    int pad[3];
+    int open_images;     // images left open by the last termination check
+    int closure_checks;  // termination checks by sink-side closure
+    int closure_ends;    // solves that the closure check ended (no final global relabel)
     // device time per phase (ns, %globaltimer read by block 0 at barriers)
     unsigned long long t_init, t_gr, t_count, t_push, t_reach;
     unsigned long long push_sweeps, push_bfs;

@@ -512,6 +512,8 @@ struct Engine {
         r->ref_energy = (int32_t)((uint32_t)s.ref_init - (uint32_t)s.pos_excess);
         r->status = status();
         r->global_relabels = h_ctl->global_relabels;
+        r->closure_checks = h_ctl->closure_checks;
+        r->closure_ends = h_ctl->closure_ends;
         r->gr_sweeps = h_ctl->gr_rounds;
         r->push_rounds = h_ctl->push_phases;
         r->cut_sweeps = h_ctl->reach_rounds;

@@ -69,6 +69,10 @@ typedef struct {
     /* tile-BFS loop iterations summed over push visits' local relabels and
      * over global-relabel visits; SM cycles summed over global-relabel visits */
     int64_t bfs_iters_push, bfs_iters_gr, cyc_global_relabel;
+    /* termination checks by a sink-side reachability closure (run after push
+     * rounds instead of a global relabel when no pixel with excess can reach
+     * the sink any more), and 1 when such a check ended the solve */
+    int32_t closure_checks, closure_ends;
 } gcfg_result;
 
 /* ---------------- graph API (drop-in for GraphCut.cu) ---------------- */
