@@ -222,6 +222,40 @@ def test_batch_vs_oracle(n, seed0):
     assert np.array_equal(hmin, smin) and np.array_equal(hmax, smax)
 
 
+def test_termination_check_ends_solve_exactly():
+    """After its push rounds a typical batch is finished by the sink-side
+    reachability check (no final global relabel); flows and both cuts still
+    equal the oracle's, and so do those of a heavier image, which can fail a
+    check and go on to another global relabel."""
+    imgs = _batch_images(16, 1100)
+    Ws = [s.shape[1] for _, s in imgs]
+    Hs = [s.shape[0] for _, s in imgs]
+    rgb = np.concatenate([r.reshape(-1) for r, _ in imgs])
+    scrib = np.concatenate([s.reshape(-1) for _, s in imgs])
+    bs = gcfg.BatchSolver(16, scrib.size)
+    smin = torch.zeros(scrib.size, dtype=torch.uint8, device="cuda")
+    smax = torch.zeros(scrib.size, dtype=torch.uint8, device="cuda")
+    flows, res = bs.run(Ws, Hs, [50.0] * 16, dev(rgb), dev(scrib), smin, smax, results=True)
+    r0 = res[0] if isinstance(res, list) else res
+    assert r0["closure_checks"] >= 1 and r0["closure_ends"] == 1
+    smin, smax = smin.cpu().numpy(), smax.cpu().numpy()
+    off = 0
+    for i, (r, s) in enumerate(imgs):
+        o = O.segment(r, s, 50.0)
+        k = s.size
+        assert flows[i] == o["flow"], i
+        assert np.array_equal(smin[off:off + k].reshape(s.shape), o["smin"]), i
+        assert np.array_equal(smax[off:off + k].reshape(s.shape), o["smax"]), i
+        off += k
+    rgb, scrib = O.generate(2, 2048, 2048, 2)
+    smin_h, smax_h, res = gpu_segment(rgb, scrib, 100.0)
+    o = O.segment(rgb, scrib, 100.0)
+    # every global relabel after the first follows a failed check
+    assert res["closure_checks"] >= res["global_relabels"] - 1
+    assert res["flow"] == o["flow"]
+    assert np.array_equal(smin_h, o["smin"]) and np.array_equal(smax_h, o["smax"])
+
+
 @pytest.mark.parametrize("params", [(1, 1, 1), (1, 8, 2), (2, 64, 16), (8, 256, 64)])
 def test_batch_params_do_not_change_result(params):
     imgs = _batch_images(12, 900)
