@@ -265,9 +265,9 @@ __device__ unsigned tile_bfs(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd,
 // the loop-carried path of a single warp) the k-th expansion that grows the
 // frontier records the reached rows srec[k][row] and its level lv[k], while
 // two more records fit (k < NREC); later expansions store their pixels'
-// levels directly, as tile_bfs does.  sfin gets the final reached rows.  Returns the number of
-// records (warp-uniform); the whole block then fills in the heights
-// (heights_from_records).
+// levels directly, as tile_bfs does.  sfin gets the final reached rows.
+// Returns the number of records (warp-uniform); the whole block then fills in
+// the heights (heights_from_records).
 constexpr int NREC = 48;
 __device__ int tile_bfs_rec(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd, unsigned sink, int hl, int hr,
                             int ht, int hb, int *hs, int stride, unsigned (*srec)[32], int *lv, unsigned *sfin,
@@ -416,9 +416,15 @@ __device__ __forceinline__ void gr_prefetch(const Batch &b, int t, GrGeo &gg, bo
     gg.skip = check_done && vload(&b.ist[__ldg(b.tile_img + t)].done) != 0;
 }
 
-// Exact distances of tile t given its halo; queues neighbours whose halo
-// (our border) changed.  round0: the heights of every tile are stale, so the
-// halo and "old" border values come from the sink-connected bits.
+// Exact distances of tile t given its halo.  round0: the heights of every
+// tile are stale, so the halo comes from the neighbours' sink-connected
+// pixels and no neighbour is queued (gr_pull_check decides the first
+// frontier round once every tile has its round-0 distances).  Later rounds
+// queue a neighbour only when this tile's new border gives one of the
+// neighbour's facing pixels, through its residual edge into this tile, a
+// shorter path than its current height; the heights read for that are at
+// least current (distances only fall during a relabel), so no needed visit is
+// missed.
 __device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int tag_next, int slot_next, int *hs,
                        unsigned long long *st) {
     const int lane = threadIdx.x & 31;
@@ -426,6 +432,10 @@ __device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int t
     unsigned m[6];
     load_tile_masks(b, t, m);
     int ht, hb, hl, hr;
+    // the neighbours' facing pixels with a residual edge into this tile: upper
+    // row 31 downward, lower row 0 upward (bit = column); left column 31
+    // rightward, right column 0 leftward (this lane's row)
+    unsigned fu = 0, fd = 0, fl = 0, fr = 0;
     if (round0) {
         ht = g.nb[2] >= 0 && ((mask_word(b, g.nb[2], 4, 31) >> lane) & 1u) ? 1 : INF_H;
         hb = g.nb[3] >= 0 && ((mask_word(b, g.nb[3], 4, 0) >> lane) & 1u) ? 1 : INF_H;
@@ -437,20 +447,10 @@ __device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int t
         hb = g.nb[3] >= 0 ? __ldcg(b.hb + (size_t)g.nb[3] * 128 + HB_TOP + lane) : INF_H;
         hl = g.nb[0] >= 0 ? __ldcg(b.hb + (size_t)g.nb[0] * 128 + HB_RGT + lane) : INF_H;
         hr = g.nb[1] >= 0 ? __ldcg(b.hb + (size_t)g.nb[1] * 128 + HB_LFT + lane) : INF_H;
-    }
-    int o_top, o_bot, o_lft, o_rgt;  // this tile's border before the visit (no other warp writes it meanwhile)
-    if (round0) {
-        const unsigned n0 = __shfl_sync(FULL, m[4], 0), n31 = __shfl_sync(FULL, m[4], 31);
-        o_top = (n0 >> lane) & 1u ? 1 : INF_H;
-        o_bot = (n31 >> lane) & 1u ? 1 : INF_H;
-        o_lft = (m[4] & 1u) ? 1 : INF_H;
-        o_rgt = (m[4] >> 31) ? 1 : INF_H;
-    } else {
-        const int *own = b.hb + (size_t)t * 128;
-        o_top = __ldcg(own + HB_TOP + lane);
-        o_bot = __ldcg(own + HB_BOT + lane);
-        o_lft = __ldcg(own + HB_LFT + lane);
-        o_rgt = __ldcg(own + HB_RGT + lane);
+        fu = g.nb[2] >= 0 ? mask_word(b, g.nb[2], 3, 31) : 0u;
+        fd = g.nb[3] >= 0 ? mask_word(b, g.nb[3], 2, 0) : 0u;
+        fl = g.nb[0] >= 0 ? mask_word(b, g.nb[0], 1, lane) >> 31 : 0u;
+        fr = g.nb[1] >= 0 ? mask_word(b, g.nb[1], 0, lane) & 1u : 0u;
     }
     int its = 0;
     const unsigned reached = tile_bfs(m[0], m[1], m[2], m[3], m[4], hl, hr, ht, hb, hs, 33, &its);
@@ -463,24 +463,50 @@ __device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int t
     __syncwarp();
 #pragma unroll 4
     for (int r = 0; r < 32; ++r) b.h[base + r * 32 + lane] = hs[r * 33 + lane];
+    const int vt = hs[lane], vb = hs[31 * 33 + lane], vl = hs[lane * 33], vr = hs[lane * 33 + 31];
     {
         int *own = b.hb + (size_t)t * 128;
-        own[HB_TOP + lane] = hs[lane];
-        own[HB_BOT + lane] = hs[31 * 33 + lane];
-        own[HB_LFT + lane] = hs[lane * 33];
-        own[HB_RGT + lane] = hs[lane * 33 + 31];
+        own[HB_TOP + lane] = vt;
+        own[HB_BOT + lane] = vb;
+        own[HB_LFT + lane] = vl;
+        own[HB_RGT + lane] = vr;
     }
-    const bool ch_top = __any_sync(FULL, hs[lane] != o_top);
-    const bool ch_bot = __any_sync(FULL, hs[31 * 33 + lane] != o_bot);
-    const bool ch_lft = __any_sync(FULL, hs[lane * 33] != o_lft);
-    const bool ch_rgt = __any_sync(FULL, hs[lane * 33 + 31] != o_rgt);
-    // lanes 0..3 queue the left, right, upper and lower neighbour
-    const int nbt = lane == 0 ? g.nb[0] : lane == 1 ? g.nb[1] : lane == 2 ? g.nb[2] : g.nb[3];
-    const bool ch = lane == 0 ? ch_lft : lane == 1 ? ch_rgt : lane == 2 ? ch_top : ch_bot;
-    enqueue_warp(b, b.mark_gr, slot_next, tag_next, nbt, lane < 4 && ch && nbt >= 0);
+    if (!round0) {
+        const bool up_t = __any_sync(FULL, ((fu >> lane) & 1u) && vt < INF_H && vt + 1 < ht);
+        const bool up_b = __any_sync(FULL, ((fd >> lane) & 1u) && vb < INF_H && vb + 1 < hb);
+        const bool up_l = __any_sync(FULL, fl && vl < INF_H && vl + 1 < hl);
+        const bool up_r = __any_sync(FULL, fr && vr < INF_H && vr + 1 < hr);
+        // lanes 0..3 queue the left, right, upper and lower neighbour
+        const int nbt = lane == 0 ? g.nb[0] : lane == 1 ? g.nb[1] : lane == 2 ? g.nb[2] : g.nb[3];
+        const bool up = lane == 0 ? up_l : lane == 1 ? up_r : lane == 2 ? up_t : up_b;
+        enqueue_warp(b, b.mark_gr, slot_next, tag_next, nbt, lane < 4 && up && nbt >= 0);
+    }
     __syncwarp();
 }
 
+// After round 0 of a global relabel: tile t joins the first frontier round
+// when a neighbour's border, as round 0 left it, gives one of t's border
+// pixels (through its residual edge out of the tile) a shorter path than its
+// own round-0 distance.
+__device__ void gr_pull_check(const Batch &b, int t, int tag_next, int slot_next) {
+    const int lane = threadIdx.x & 31;
+    int nb[4];
+    tile_nbs(b, t, nb);
+    const int *own = b.hb + (size_t)t * 128;
+    const int ot = __ldcg(own + HB_TOP + lane), ob = __ldcg(own + HB_BOT + lane);
+    const int ol = __ldcg(own + HB_LFT + lane), orr = __ldcg(own + HB_RGT + lane);
+    const unsigned ru = mask_word(b, t, 2, 0), rd = mask_word(b, t, 3, 31);  // bit = column
+    const unsigned rl = mask_word(b, t, 0, lane) & 1u, rr = mask_word(b, t, 1, lane) >> 31;
+    const int ht = nb[2] >= 0 ? __ldcg(b.hb + (size_t)nb[2] * 128 + HB_BOT + lane) : INF_H;
+    const int hb = nb[3] >= 0 ? __ldcg(b.hb + (size_t)nb[3] * 128 + HB_TOP + lane) : INF_H;
+    const int hl = nb[0] >= 0 ? __ldcg(b.hb + (size_t)nb[0] * 128 + HB_RGT + lane) : INF_H;
+    const int hr = nb[1] >= 0 ? __ldcg(b.hb + (size_t)nb[1] * 128 + HB_LFT + lane) : INF_H;
+    const bool imp = (((ru >> lane) & 1u) && ht < INF_H && ht + 1 < ot) ||
+                     (((rd >> lane) & 1u) && hb < INF_H && hb + 1 < ob) || (rl && hl < INF_H && hl + 1 < ol) ||
+                     (rr && hr < INF_H && hr + 1 < orr);
+    const bool any = __any_sync(FULL, imp);
+    enqueue_warp(b, b.mark_gr, slot_next, tag_next, t, lane == 0 && any);
+}
 // Source-side reachability closure of tile t given the halo's reach bits.
 __device__ void reach_tile(const Batch &b, int t, bool round0, int tag_next, int slot_next) {
     const int lane = threadIdx.x & 31;
@@ -858,14 +884,13 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
 // excess.  Returns 1 when every image is finished, 0 when some are not, -1
 // on an error (recorded in the control block).  Called by every thread of the
 // grid; kept out of line so that its registers do not add to the solver's.
-__device__ __noinline__ int closure_check(const Batch &b, const SolveParams &prm, int &G, unsigned long long *st) {
+__device__ __noinline__ int closure_check(const Batch &b, const SolveParams &prm, int &G) {
     Ctl *ctl = b.ctl;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int gwarp = blockIdx.x * 8 + warp, nwarps = gridDim.x * 8;
     const int swarp = warp * gridDim.x + blockIdx.x;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
     const int nt = batch_ntiles(b);
-    (void)st;
     for (int k = gtid; k < batch_nimg(b); k += nthreads) {
         const int i = batch_img(b, k);
         if (!b.ist[i].done) {
@@ -972,7 +997,7 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
     bool finished = false;
     for (int outer = 0; outer < prm.max_outer; ++outer) {
         if (outer > 0) {
-            const int rc = closure_check(b, prm, G, st);
+            const int rc = closure_check(b, prm, G);
             if (rc < 0) return;
             clk.charge(&ctl->t_gr);
             if (rc > 0) {
@@ -1002,6 +1027,12 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
             }
         }
         if (!grid_sync(b, (1u << L_PUSH0) | (1u << L_PUSH1) | (1u << L_PUSH2))) return;
+        for (int k = gwarp; k < nt; k += nwarps) {
+            const int t = batch_tile(b, k);
+            if (vload(&b.ist[__ldg(b.tile_img + t)].done)) continue;  // warp-uniform
+            gr_pull_check(b, t, G + 1, L_GR0 + ((G + 1) & 1));
+        }
+        if (!grid_sync(b, 0)) return;
         ++G;
         for (int k = 1;; ++k) {
             const int slot = L_GR0 + (G & 1);
