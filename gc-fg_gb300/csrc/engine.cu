@@ -549,8 +549,7 @@ __device__ void reach_tile(const Batch &b, int t, bool round0, int tag_next, int
 // complement of S_max inside the image).  The expansion of tile_bfs without
 // levels.  round0: the neighbours' sets are not known yet, so the halo starts
 // from their sink-connected pixels; later rounds read their hfin rows, all
-// written by this pass.  A neighbour is queued when this tile's set grows on
-// the border it shares (the sets only grow, so the rounds converge).
+// written by this pass (the sets only grow, so the rounds converge).
 __device__ void sink_reach_tile(const Batch &b, int t, bool round0, int tag_next, int slot_next) {
     const int lane = threadIdx.x & 31;
     int nb[4];
@@ -577,11 +576,18 @@ __device__ void sink_reach_tile(const Batch &b, int t, bool round0, int tag_next
         S |= nw;
     }
     b.hfin[(size_t)t * 32 + lane] = S;
+    // a neighbour is queued when a pixel new in this tile's set has a facing
+    // pixel with a residual edge into it that the neighbour's set (as read
+    // above, never ahead of the truth) does not hold yet
     const unsigned fresh = S & ~old;
-    const bool out_l = __any_sync(FULL, (fresh & 1u) != 0);
-    const bool out_r = __any_sync(FULL, (fresh & 0x80000000u) != 0);
-    const bool out_u = __any_sync(FULL, lane == 0 && fresh != 0);
-    const bool out_d = __any_sync(FULL, lane == 31 && fresh != 0);
+    const unsigned in_u = nb[2] >= 0 ? mask_word(b, nb[2], 3, 31) & ~T : 0u;         // bit = column
+    const unsigned in_d = nb[3] >= 0 ? mask_word(b, nb[3], 2, 0) & ~B : 0u;
+    const unsigned in_l = nb[0] >= 0 ? (mask_word(b, nb[0], 1, lane) >> 31) & ~lbit : 0u;  // this row
+    const unsigned in_r = nb[1] >= 0 ? (mask_word(b, nb[1], 0, lane) & 1u) & ~(rbit >> 31) : 0u;
+    const bool out_l = __any_sync(FULL, (fresh & 1u) && in_l);
+    const bool out_r = __any_sync(FULL, (fresh >> 31) && in_r);
+    const bool out_u = __any_sync(FULL, lane == 0 && (fresh & in_u) != 0);
+    const bool out_d = __any_sync(FULL, lane == 31 && (fresh & in_d) != 0);
     const int nbt = lane == 0 ? nb[0] : lane == 1 ? nb[1] : lane == 2 ? nb[2] : nb[3];
     const bool out = lane == 0 ? out_l : lane == 1 ? out_r : lane == 2 ? out_u : out_d;
     enqueue_warp(b, b.mark_gr, slot_next, tag_next, nbt, lane < 4 && out && nbt >= 0);
