@@ -838,7 +838,7 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
     if (warp < 4) {
         const int f = s.halo_in[warp][lane];
         const int nt = warp == 0 ? g.nb[0] : warp == 1 ? g.nb[1] : warp == 2 ? g.nb[2] : g.nb[3];
-        bool sent = false;
+        bool activated = false;  // a pixel of nt now has excess: nt needs a visit
         if (f && nt >= 0) {
             int px, comp;
             if (warp == 0) { px = lane * 32 + 31; comp = 1; }       // left tile, its RIGHT edge
@@ -858,9 +858,11 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
             if (old_e <= 0 && new_e > 0) atomicOr(mt + 5 * 32 + row, bit);
             const int dpos = max(new_e, 0) - max(old_e, 0);
             if (dpos) atomicAdd(b.tile_pos + nt, (unsigned long long)dpos);
-            sent = true;
+            // flow that only fills sink capacity (the excess stays <= 0) leaves
+            // nothing to push there
+            activated = new_e > 0;
         }
-        if (__any_sync(FULL, sent) && lane == 0)
+        if (__any_sync(FULL, activated) && lane == 0)
             enqueue(b, b.mark_push, (phase + 1) % 3, phase + 1, nt);
     }
     if (any && threadIdx.x == 0) enqueue(b, b.mark_push, (phase + 2) % 3, phase + 2, t);
