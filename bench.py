@@ -745,6 +745,9 @@ def main():
         if ms > 0:
             gbs = nbytes / (ms / 1e3) / 1e9
             ph[name] = {"achieved": round(gbs, 1), "frac": round(gbs / peak, 4), "ms": ms, "bytes": nbytes}
+    ph["note"] = ("int32-layout bytes per unit as for the whole kernel; the global relabel and the termination "
+                  "check read 1-bit residual planes (0.75 B/px) instead of the int32 capacities and write 4-byte "
+                  "heights, so their figure can pass the HBM peak")
     roofline["solve_phases"] = ph
 
     r0 = recs[0]
