@@ -468,6 +468,20 @@ def run_n8(args, rank, world):
                              "sample": f"one solve of the same graph, oracle 8-connected push-relabel, {cpu_s:.2f} s"},
             "parity": {"flow_equal_oracle": bool(r["flow"] == o["flow"]),
                        "labels_equal_oracle": bool((label.reshape(H, W) == o["smax"]).all())}}
+    # the reference's own NEIGHBORHOOD 8 build of its kernels on the same GPU and graph
+    import ref_cuda
+    why = ref_cuda.unavailable(8)
+    if why:
+        line["reference_cuda"] = {"unavailable": why}
+    else:
+        rr = [ref_cuda.solve8(hdp, hdn, penalty=pen, max_seconds=30.0) for _ in range(3)]
+        best = min(x["ms_solve"] for x in rr)
+        line["reference_cuda"] = {
+            "value": W * H / (best / 1e3) / 1e6, "unit": UNIT, "ms_per_image": best,
+            "status": rr[-1]["status"], "iterations": rr[-1]["iterations"],
+            "labels_equal": bool(np.array_equal(rr[-1]["label"], label.reshape(H, W))),
+            "how": "the reference's kernels built with NEIGHBORHOOD 8 (GraphCutKernels.cu, sm_103a), launched in "
+                   "GC_Optimize's order; best of 3 solves, wall clock of GC_SetGraph + GC_Optimize"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0

@@ -295,9 +295,10 @@ struct gcfg_graph8 {
     Ctl8 *ctl = nullptr, *h_ctl = nullptr;
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    // schedule (measured on a 640x480 graph: 64 pulses per global relabel and
-    // 2 blocks per SM take 5.6 ms; 16 and all that fit 10.3 ms)
-    int pulses = 64, max_outer = 100000, blocks_per_sm = 2;
+    // schedule (measured on a 640x480 graph with a constant penalty of 600:
+    // 64 pulses per global relabel take 6.4 / 6.3 / 5.5 / 7.5 ms at 1 / 2 / 3 /
+    // 4 blocks per SM; 8, 16, 32 and 128 pulses take longer at every count)
+    int pulses = 64, max_outer = 100000, blocks_per_sm = 3;
 
     G8 g() const {
         G8 x;

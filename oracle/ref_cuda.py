@@ -20,6 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "refgpu", "ref_gpu.cpp")
 LIB_PATH = os.path.join(HERE, "librefgpu.so")
 CUBIN = os.path.join(HERE, "_ref", "gc_ref_kernels.cubin")
+CUBIN8 = os.path.join(HERE, "_ref", "gc_ref_kernels8.cubin")  # the NEIGHBORHOOD 8 build
 
 STATUS = {0: "ok", 1: "invalid", 2: "cuda error", 3: "iteration or time cap reached", 4: "kernels not loaded"}
 
@@ -44,33 +45,40 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def unavailable() -> str | None:
+def unavailable(neighborhood: int = 4) -> str | None:
     """None when the reference's CUDA path can run here, else why not."""
-    if not os.path.exists(CUBIN):
-        return ("the reference's kernels were not compiled (oracle/_ref/gc_ref_kernels.cubin is built "
+    path = CUBIN8 if neighborhood == 8 else CUBIN
+    if not os.path.exists(path):
+        return (f"the reference's kernels were not compiled (oracle/_ref/{os.path.basename(path)} is built "
                 "from the reference checkout)")
     return None
 
 
 _lib = None
+_loaded = set()
 
 
-def lib():
+def lib(neighborhood: int = 4):
     global _lib
+    why = unavailable(neighborhood)
+    if why:
+        raise RuntimeError(why)
     if _lib is None:
-        why = unavailable()
-        if why:
-            raise RuntimeError(why)
         build()
         L = C.CDLL(LIB_PATH)
         P = C.c_void_p
         L.refgpu_load.argtypes = [C.c_char_p]
+        L.refgpu_load8.argtypes = [C.c_char_p]
         L.refgpu_solve.argtypes = [C.c_int, C.c_int, P, P, C.c_int, P, P, P, P, P, C.c_longlong, C.c_double,
                                    C.POINTER(Stats)]
-        rc = L.refgpu_load(CUBIN.encode())
+        L.refgpu_solve8.argtypes = [C.c_int, C.c_int, P, P, C.c_int, P, P, C.c_longlong, C.c_double,
+                                    C.POINTER(Stats)]
+        _lib = L
+    if neighborhood not in _loaded:
+        rc = (_lib.refgpu_load8(CUBIN8.encode()) if neighborhood == 8 else _lib.refgpu_load(CUBIN.encode()))
         if rc:
             raise RuntimeError(f"loading the reference's kernels failed: {STATUS.get(rc, rc)}")
-        _lib = L
+        _loaded.add(neighborhood)
     return _lib
 
 
@@ -91,6 +99,30 @@ def solve(dp, dn, penalty=0, up=None, down=None, left=None, right=None, max_iter
     st = Stats()
     rc = lib().refgpu_solve(W, H, _p(dp), _p(dn), int(penalty), *[_p(a) for a in arrs], _p(label),
                             int(max_iters), float(max_seconds), C.byref(st))
+    return _result(st, rc, label)
+
+
+def _result(st, rc, label):
     out = {k: getattr(st, k) for k, _ in Stats._fields_ if k != "pad"}
     out.update(status=STATUS.get(rc, rc), rc=rc, label=label, energy=st.final_energy)
     return out
+
+
+def solve8(dp, dn, penalty=0, arrays=None, max_iters=5_000_000, max_seconds=60.0):
+    """The reference's NEIGHBORHOOD 8 solver: arrays = None (constant penalty)
+    or the eight (H, W) int32 arrays up, down, left, right, upleft, upright,
+    downleft, downright."""
+    dp = np.ascontiguousarray(dp, np.int32)
+    dn = np.ascontiguousarray(dn, np.int32)
+    H, W = dp.shape
+    label = np.zeros((H, W), np.int32)
+    st = Stats()
+    ptrs = None
+    keep = None
+    if arrays is not None:
+        keep = [np.ascontiguousarray(a, np.int32) for a in arrays]
+        assert len(keep) == 8
+        ptrs = (C.c_void_p * 8)(*[a.ctypes.data for a in keep])
+    rc = lib(8).refgpu_solve8(W, H, _p(dp), _p(dn), int(penalty), ptrs, _p(label), int(max_iters),
+                              float(max_seconds), C.byref(st))
+    return _result(st, rc, label)

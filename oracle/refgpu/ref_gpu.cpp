@@ -1,12 +1,14 @@
 /* The reference's CUDA path on the GPU: test and benchmark infrastructure.
  *
  * The device code is the reference's own (GraphCutKernels.cu, compiled from
- * the reference checkout into gc_ref_kernels.cubin by build_ref_gpu.sh).  The
- * reference's host code (GraphCut.cu) is compiled into every application
- * and cannot be rebuilt where its sources are absent, so this file restates
- * it, launch for launch, over the cubin's kernels:
+ * the reference checkout into gc_ref_kernels.cubin, and with its
+ * NEIGHBORHOOD switch set to 8 into gc_ref_kernels8.cubin, by
+ * build_ref_gpu.sh).  The reference's host code (GraphCut.cu) is compiled
+ * into every application and cannot be rebuilt where its sources are absent,
+ * so this file restates it, launch for launch, over the cubins' kernels:
  *
- *   refgpu_solve  = GC_Init (GraphCut.cu:187-263: padded sizes, eleven
+ *   refgpu_solve / refgpu_solve8
+ *                 = GC_Init (GraphCut.cu:187-263: padded sizes, the graph's
  *                   allocations) + GC_SetGraph (:301-319) + GC_Optimize
  *                   (:385-534) + GC_End (:542-568)
  *   get_energy    = getEnergy (GraphCut.cu:359-376)
@@ -19,9 +21,10 @@
  * iterations and around every GlobalRelabel / SpreadLabels launch, and the
  * global-relabel schedule are the reference's.
  *
- * The kernels take the reference's KernelWrapper by value; RKernel below has
- * the same members in the same order (GraphCut.h:60-105, NEIGHBORHOOD 4),
- * hence the same 120-byte layout on every LP64 host and on the device.
+ * The kernels take the reference's KernelWrapper by value; RKernel<NB> below
+ * has the same members in the same order (GraphCut.h:60-105), hence the same
+ * layout (120 bytes with NEIGHBORHOOD 4, 152 with 8) on every LP64 host and
+ * on the device.
  */
 #include <cuda_runtime.h>
 
@@ -31,48 +34,75 @@
 
 namespace {
 
+// NodeWrapper / GraphWrapper / KernelWrapper (GraphCut.h:60-105): the edge
+// arrays l, r, u, d, then with NEIGHBORHOOD 8 ul, dr, ur, dl
+template <int NB>
 struct RNode {
-    int *edge_l, *edge_r, *edge_u, *edge_d;
+    int *edge[NB];
     int *height, *excess, *status, *comp_h, *comp_n, *energy_sum;
 };
+template <int NB>
 struct RGraph {
     int width, height, size, width_ex, height_ex, size_ex;
-    RNode n;
+    RNode<NB> n;
 };
+template <int NB>
 struct RKernel {
     int block_x;
     int *active;
-    RGraph g;
+    RGraph<NB> g;
 };
-static_assert(sizeof(RKernel) == 120, "KernelWrapper layout (GraphCut.h:60-105)");
+static_assert(sizeof(RKernel<4>) == 120, "KernelWrapper layout (GraphCut.h:60-105)");
+static_assert(sizeof(RKernel<8>) == 152, "KernelWrapper layout with NEIGHBORHOOD 8");
 
 // GraphCut.h:43-48 and :144-157
 constexpr int TX = 32, TY = 8;
 constexpr int ACTIVITY_CHECK = 10, GR_FREQUENCY = 100, GR_FIRST = 100;
 
-cudaLibrary_t g_lib = nullptr;
-cudaKernel_t k_init, k_init_var, k_relabel, k_push, k_activity, k_init_gr, k_gr, k_energy,
-    k_init_labels, k_spread;
+// The reference's kernels of one NEIGHBORHOOD build (one cubin each).
+struct Kernels {
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t init, init_var, relabel, push, activity, init_gr, gr, energy, init_labels, spread;
+};
+Kernels g_k4, g_k8;
 
-// Itanium-mangled names of the reference's kernels (GraphCutKernels.cu)
+// Itanium-mangled names of the reference's kernels (GraphCutKernels.cu);
+// InitGraphVarEdges takes 6 int* arrays with NEIGHBORHOOD 4 and 10 with 8.
 struct Named {
-    cudaKernel_t *k;
+    cudaKernel_t Kernels::*k;
     const char *name;
 };
 const Named kNames[] = {
-    {&k_init, "_Z9InitGraph13KernelWrapperPiS0_i"},
-    {&k_init_var, "_Z17InitGraphVarEdges13KernelWrapperPiS0_S0_S0_S0_S0_"},
-    {&k_relabel, "_Z7Relabel13KernelWrapperi"},
-    {&k_push, "_Z8WavePush13KernelWrapperiPi"},
-    {&k_activity, "_Z14UpdateActivityPiS_iiS_"},
-    {&k_init_gr, "_Z17InitGlobalRelabel13KernelWrapper"},
-    {&k_gr, "_Z13GlobalRelabel13KernelWrapperPi"},
-    {&k_energy, "_Z11EnergyLevel13KernelWrapperiiPiS0_b"},
-    {&k_init_labels, "_Z10InitLabels13KernelWrapperPi"},
-    {&k_spread, "_Z12SpreadLabels13KernelWrapperPiS0_"},
+    {&Kernels::init, "_Z9InitGraph13KernelWrapperPiS0_i"},
+    {&Kernels::relabel, "_Z7Relabel13KernelWrapperi"},
+    {&Kernels::push, "_Z8WavePush13KernelWrapperiPi"},
+    {&Kernels::activity, "_Z14UpdateActivityPiS_iiS_"},
+    {&Kernels::init_gr, "_Z17InitGlobalRelabel13KernelWrapper"},
+    {&Kernels::gr, "_Z13GlobalRelabel13KernelWrapperPi"},
+    {&Kernels::energy, "_Z11EnergyLevel13KernelWrapperiiPiS0_b"},
+    {&Kernels::init_labels, "_Z10InitLabels13KernelWrapperPi"},
+    {&Kernels::spread, "_Z12SpreadLabels13KernelWrapperPiS0_"},
 };
+const char *const kInitVar4 = "_Z17InitGraphVarEdges13KernelWrapperPiS0_S0_S0_S0_S0_";
+const char *const kInitVar8 = "_Z17InitGraphVarEdges13KernelWrapperPiS0_S0_S0_S0_S0_S0_S0_S0_S0_";
 
 enum { OK = 0, ERR_INVALID = 1, ERR_CUDA = 2, ERR_CAP = 3, ERR_NOT_LOADED = 4 };
+
+int load(Kernels &K, const char *path, const char *init_var_name) {
+    if (K.lib) return OK;
+    if (!path) return ERR_INVALID;
+    cudaLibrary_t lib;
+    if (cudaLibraryLoadFromFile(&lib, path, nullptr, nullptr, 0, nullptr, nullptr, 0) != cudaSuccess)
+        return ERR_CUDA;
+    bool ok = cudaLibraryGetKernel(&K.init_var, lib, init_var_name) == cudaSuccess;
+    for (const Named &n : kNames) ok = ok && cudaLibraryGetKernel(&(K.*n.k), lib, n.name) == cudaSuccess;
+    if (!ok) {
+        cudaLibraryUnload(lib);
+        return ERR_CUDA;
+    }
+    K.lib = lib;
+    return OK;
+}
 
 // GraphCut.cu:165-170 (float ceil, as the reference computes it)
 int round_up(int a, int b) { return (int)std::ceil((float)a / (float)b); }
@@ -96,14 +126,15 @@ cudaError_t launch(cudaKernel_t k, dim3 grid, void **args) {
 
 // getEnergy (GraphCut.cu:359-376): tree sum of the positive part of source
 // in energy_sum; the first 8 ints are copied to dest.
-cudaError_t get_energy(RKernel k, dim3 grid, int *source, int *dest, bool limited) {
+template <int NB>
+cudaError_t get_energy(const Kernels &K, RKernel<NB> k, dim3 grid, int *source, int *dest, bool limited) {
     int odd = 0;
     int stride = limited ? k.g.size : k.g.size_ex;
     int *out = k.g.n.energy_sum;
     for (;; odd = stride % 2, stride = (stride + 1) / 2) {
         if (stride == 1) odd = 0;
         void *a[] = {&k, &stride, &odd, &source, &out, &limited};
-        cudaError_t e = launch(k_energy, grid, a);
+        cudaError_t e = launch(K.energy, grid, a);
         if (e != cudaSuccess) return e;
         if (stride == 1) return cudaMemcpy(dest, out, 8 * sizeof(int), cudaMemcpyDeviceToHost);
     }
@@ -128,56 +159,41 @@ struct refgpu_stats {
     double ms_end;              // GC_End's frees
 };
 
-/* Loads the reference's kernels from the cubin.  Returns 0, or 2 when the
- * file cannot be loaded or a kernel is missing. */
-int refgpu_load(const char *cubin_path) {
-    if (g_lib) return OK;
-    if (!cubin_path) return ERR_INVALID;
-    cudaLibrary_t lib;
-    if (cudaLibraryLoadFromFile(&lib, cubin_path, nullptr, nullptr, 0, nullptr, nullptr, 0) != cudaSuccess)
-        return ERR_CUDA;
-    for (const Named &n : kNames) {
-        if (cudaLibraryGetKernel(n.k, lib, n.name) != cudaSuccess) {
-            cudaLibraryUnload(lib);
-            return ERR_CUDA;
-        }
-    }
-    g_lib = lib;
-    return OK;
-}
+}  // extern "C"
 
-/* One solve through the reference's CUDA path.  dp/dn (and up/down/left/right
- * when up != NULL, else the constant penalty) are HOST arrays of w*h int32,
- * row-major; they are uploaded first (outside every timed span, as the
- * reference's callers do before GC_Init, solveMRF.cu:70-86).  label (host,
- * w*h int32) receives the reference's labels.  Returns 0 when the
- * reference's termination test ended the solve, 3 when max_iters main-loop
- * iterations or max_seconds passed first (labels then not computed). */
-int refgpu_solve(int w, int h, const int *dp, const int *dn, int penalty, const int *up,
-                 const int *down, const int *left, const int *right, int *label,
-                 long long max_iters, double max_seconds, refgpu_stats *st) {
-    if (!g_lib) return ERR_NOT_LOADED;
+namespace {
+
+// One solve: edges == NULL selects the constant penalty (InitGraph), else
+// edges[0 .. NB-1] are the NB host arrays in InitGraphVarEdges' order (up,
+// down, left, right, then upleft, upright, downleft, downright).
+template <int NB>
+int solve(const Kernels &K, int w, int h, const int *dp, const int *dn, int penalty, const int *const *edges,
+          int *label, long long max_iters, double max_seconds, refgpu_stats *st) {
+    if (!K.lib) return ERR_NOT_LOADED;
     if (w < 1 || h < 1 || !dp || !dn || !label || !st) return ERR_INVALID;
     if ((long long)w * h > (1LL << 28)) return ERR_INVALID;
     std::memset(st, 0, sizeof(*st));
-    const bool var = up != nullptr;
-    if (var && (!down || !left || !right)) return ERR_INVALID;
+    const bool var = edges != nullptr;
+    if (var)
+        for (int i = 0; i < NB; ++i)
+            if (!edges[i]) return ERR_INVALID;
     const size_t n = (size_t)w * h;
+    const int n_in = var ? 2 + NB : 2;
     int rc = OK;
-    int *d_in[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    const int *h_in[6] = {dp, dn, up, down, left, right};
-    int *owned[11] = {};
+    int *d_in[2 + NB] = {};
+    int *owned[NB + 7] = {};
     int *d_alive = nullptr, *d_label = nullptr;
     int zero_arr[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int h_alive[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    RKernel k;
+    RKernel<NB> k;
     std::memset(&k, 0, sizeof(k));
     dim3 grid;
     Clock::time_point t0;
 
-    for (int i = 0; i < (var ? 6 : 2); ++i) {
+    for (int i = 0; i < n_in; ++i) {
+        const int *src = i == 0 ? dp : i == 1 ? dn : edges[i - 2];
         TRY(cudaMalloc((void **)&d_in[i], n * sizeof(int)));
-        TRY(cudaMemcpy(d_in[i], h_in[i], n * sizeof(int), cudaMemcpyHostToDevice));
+        TRY(cudaMemcpy(d_in[i], src, n * sizeof(int), cudaMemcpyHostToDevice));
     }
     TRY(cudaDeviceSynchronize());
 
@@ -194,14 +210,20 @@ int refgpu_solve(int w, int h, const int *dp, const int *dn, int penalty, const 
         const int block_y = round_up(k.g.height_ex, TY);
         const int block_count = round_up(k.g.size_ex, TX * TY);
         grid = dim3(k.block_x, block_y, 1);
-        int **fields[10] = {&k.g.n.edge_u, &k.g.n.edge_d, &k.g.n.edge_l, &k.g.n.edge_r, &k.g.n.height,
-                            &k.g.n.excess, &k.g.n.status, &k.g.n.comp_h, &k.g.n.comp_n, &k.g.n.energy_sum};
-        for (int i = 0; i < 10; ++i) {
+        int **fields[NB + 6];
+        for (int i = 0; i < NB; ++i) fields[i] = &k.g.n.edge[i];
+        fields[NB + 0] = &k.g.n.height;
+        fields[NB + 1] = &k.g.n.excess;
+        fields[NB + 2] = &k.g.n.status;
+        fields[NB + 3] = &k.g.n.comp_h;
+        fields[NB + 4] = &k.g.n.comp_n;
+        fields[NB + 5] = &k.g.n.energy_sum;
+        for (int i = 0; i < NB + 6; ++i) {
             TRY(cudaMalloc((void **)fields[i], sizeof(int) * k.g.size_ex));
             owned[i] = *fields[i];
         }
         TRY(cudaMalloc((void **)&k.active, sizeof(int) * block_count));
-        owned[10] = k.active;
+        owned[NB + 6] = k.active;
     }
     TRY(cudaDeviceSynchronize());
     st->ms_init = ms_since(t0);
@@ -209,14 +231,15 @@ int refgpu_solve(int w, int h, const int *dp, const int *dn, int penalty, const 
     // ---- GC_SetGraph (GraphCut.cu:301-319) + GC_Optimize (:385-534)
     t0 = Clock::now();
     if (var) {
-        void *a[] = {&k, &d_in[0], &d_in[1], &d_in[2], &d_in[3], &d_in[4], &d_in[5]};
-        TRY(launch(k_init_var, grid, a));
+        void *a[3 + NB] = {&k, &d_in[0], &d_in[1]};
+        for (int i = 0; i < NB; ++i) a[3 + i] = &d_in[2 + i];
+        TRY(launch(K.init_var, grid, a));
     } else {
         void *a[] = {&k, &d_in[0], &d_in[1], &penalty};
-        TRY(launch(k_init, grid, a));
+        TRY(launch(K.init, grid, a));
     }
     TRY(cudaMalloc((void **)&d_alive, 8 * sizeof(int)));
-    TRY(get_energy(k, grid, d_in[0], h_alive, true));
+    TRY(get_energy(K, k, grid, d_in[0], h_alive, true));
     st->initial_energy = h_alive[0];
     {
         const Clock::time_point t_loop = Clock::now();
@@ -228,35 +251,35 @@ int refgpu_solve(int w, int h, const int *dp, const int *dn, int penalty, const 
             {
                 int s = skip;
                 void *a[] = {&k, &s};
-                TRY(launch(k_relabel, grid, a));
+                TRY(launch(K.relabel, grid, a));
             }
             {
                 int s = skip;
                 void *a[] = {&k, &s, &d_alive};
-                TRY(launch(k_push, grid, a));
+                TRY(launch(K.push, grid, a));
             }
             if (!skip) {
                 int bx = k.block_x, wex = k.g.width_ex;
                 void *a[] = {&k.g.n.status, &k.active, &bx, &wex, &d_alive};
-                TRY(launch(k_activity, grid, a));
+                TRY(launch(K.activity, grid, a));
                 TRY(cudaMemcpy(h_alive, d_alive, 8 * sizeof(int), cudaMemcpyDeviceToHost));
             }
             if (!h_alive[0]) {
                 TRY(cudaDeviceSynchronize());
                 st->ms_loop = ms_since(t_loop);
-                TRY(get_energy(k, grid, k.g.n.excess, h_alive, false));
+                TRY(get_energy(K, k, grid, k.g.n.excess, h_alive, false));
                 st->final_energy = st->initial_energy - h_alive[0];
                 st->converged = 1;
                 break;
             }
             if (!((counter - GR_FIRST) % GR_FREQUENCY)) {
                 void *a0[] = {&k};
-                TRY(launch(k_init_gr, grid, a0));
+                TRY(launch(K.init_gr, grid, a0));
                 st->global_relabels++;
                 for (;;) {
                     TRY(cudaMemcpy(d_alive, zero_arr, 8 * sizeof(int), cudaMemcpyHostToDevice));
                     void *a[] = {&k, &d_alive};
-                    TRY(launch(k_gr, grid, a));
+                    TRY(launch(K.gr, grid, a));
                     st->gr_launches++;
                     TRY(cudaMemcpy(h_alive, d_alive, 8 * sizeof(int), cudaMemcpyDeviceToHost));
                     if (!h_alive[0]) break;
@@ -281,12 +304,12 @@ int refgpu_solve(int w, int h, const int *dp, const int *dn, int penalty, const 
     TRY(cudaMemcpy(d_label, label, sizeof(int) * n, cudaMemcpyHostToDevice));
     {
         void *a[] = {&k, &d_label};
-        TRY(launch(k_init_labels, grid, a));
+        TRY(launch(K.init_labels, grid, a));
     }
     for (;;) {
         TRY(cudaMemcpy(d_alive, zero_arr, 8 * sizeof(int), cudaMemcpyHostToDevice));
         void *a[] = {&k, &d_label, &d_alive};
-        TRY(launch(k_spread, grid, a));
+        TRY(launch(K.spread, grid, a));
         st->spread_launches++;
         TRY(cudaMemcpy(h_alive, d_alive, 8 * sizeof(int), cudaMemcpyDeviceToHost));
         if (!h_alive[0]) break;
@@ -316,6 +339,40 @@ done:
         if (p) cudaFree(p);
     if (rc == OK && cudaGetLastError() != cudaSuccess) rc = ERR_CUDA;
     return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+/* Loads the reference's kernels (NEIGHBORHOOD 4) from the cubin.  Returns 0,
+ * or 2 when the file cannot be loaded or a kernel is missing. */
+int refgpu_load(const char *cubin_path) { return load(g_k4, cubin_path, kInitVar4); }
+
+/* The same for the NEIGHBORHOOD 8 build of the kernels. */
+int refgpu_load8(const char *cubin_path) { return load(g_k8, cubin_path, kInitVar8); }
+
+/* One solve through the reference's CUDA path.  dp/dn (and up/down/left/right
+ * when up != NULL, else the constant penalty) are HOST arrays of w*h int32,
+ * row-major; they are uploaded first (outside every timed span, as the
+ * reference's callers do before GC_Init, solveMRF.cu:70-86).  label (host,
+ * w*h int32) receives the reference's labels.  Returns 0 when the
+ * reference's termination test ended the solve, 3 when max_iters main-loop
+ * iterations or max_seconds passed first (labels then not computed), 4 when
+ * the kernels were not loaded. */
+int refgpu_solve(int w, int h, const int *dp, const int *dn, int penalty, const int *up, const int *down,
+                 const int *left, const int *right, int *label, long long max_iters, double max_seconds,
+                 refgpu_stats *st) {
+    const int *edges[4] = {up, down, left, right};
+    return solve<4>(g_k4, w, h, dp, dn, penalty, up ? edges : nullptr, label, max_iters, max_seconds, st);
+}
+
+/* The same with NEIGHBORHOOD 8: edges8 == NULL selects the constant penalty,
+ * else it points to the eight host arrays up, down, left, right, upleft,
+ * upright, downleft, downright (GraphCut.cu:187-194). */
+int refgpu_solve8(int w, int h, const int *dp, const int *dn, int penalty, const int *const *edges8, int *label,
+                  long long max_iters, double max_seconds, refgpu_stats *st) {
+    return solve<8>(g_k8, w, h, dp, dn, penalty, edges8, label, max_iters, max_seconds, st);
 }
 
 }  // extern "C"

@@ -65,3 +65,26 @@ def test_reference_cuda_matches_product_on_segmentation(cfg, W, H, seed, lam):
     assert r["energy"] == res["ref_energy"]
     assert np.array_equal(r["label"], label)
     assert np.array_equal(r["label"].astype(np.uint8), smax)
+
+
+META8 = json.load(open(os.path.join(GOLDEN, "reference_pins8.json")))["cases"]
+DATA8 = np.load(os.path.join(GOLDEN, "reference_pins8.npz"))
+REF_ORDER8 = ("up", "down", "left", "right", "upleft", "upright", "downleft", "downright")
+
+
+@pytest.mark.parametrize("case", META8, ids=[c["name"] for c in META8])
+def test_reference_cuda8_reproduces_pins(case):
+    """The NEIGHBORHOOD 8 build of the reference's kernels on the GPU gives the
+    labels and printed energy the reference gave on the CPU emulator."""
+    if ref_cuda.unavailable(8):
+        pytest.skip(ref_cuda.unavailable(8))
+    name = case["name"]
+    dp = DATA8[f"{name}__dp"].astype(np.int32)
+    dn = DATA8[f"{name}__dn"].astype(np.int32)
+    arrays = [DATA8[f"{name}__{k}"].astype(np.int32) for k in REF_ORDER8] if case["arrays"] else None
+    n = case["W"] * case["H"]
+    labels = np.unpackbits(DATA8[f"{name}__ref_labels"])[:n].reshape(case["H"], case["W"]).astype(np.int32)
+    r = ref_cuda.solve8(dp, dn, penalty=case["penalty"], arrays=arrays, max_seconds=20.0)
+    assert r["rc"] == 0, r["status"]
+    assert r["energy"] == case["ref_energy"]
+    assert np.array_equal(r["label"], labels)
