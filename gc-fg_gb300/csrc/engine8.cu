@@ -12,9 +12,9 @@
 //   * count: pixels with excess that can still reach the sink; none left
 //     after an exact global relabel means the preflow is maximum (an exact
 //     termination test);
-//   * pulses: a push half (heights fixed; an edge pair (u, v) is used by at
-//     most one side in a half, since h(u) = h(v) + 1 and h(v) = h(u) + 1
-//     cannot both hold) and a relabel half (heights only increase);
+//   * tile rounds: every 32x8 tile once per round, each visit a few
+//     block-local push/relabel sweeps in shared memory (tile8_visit), the
+//     results added back as deltas;
 //   * cuts: S_max = pixels at height INF after the last exact global
 //     relabel, S_min = the forward closure of the pixels with excess.
 // Every spin is bounded; a timeout or an iteration cap sets an error that
@@ -51,7 +51,8 @@ struct G8 {
 
 struct P8 {
     int max_outer;   // global relabels at most
-    int pulses;      // push/relabel pulses between global relabels
+    int pulses;      // tile rounds between global relabels
+    int sweeps;      // push/relabel sweeps per tile visit
 };
 
 enum { E8_BARRIER = 1, E8_OUTER = 2, E8_QUEUE = 3 };
@@ -149,6 +150,114 @@ __global__ void k8_build(G8 g, const int *__restrict__ dp, const int *__restrict
     if (rinit) atomicAdd(&g.ctl->ref_init, rinit);
 }
 
+// One push visit of a 32x8 tile (one pixel per thread): the tile's
+// capacities, excess and heights and a one-pixel ring of heights (corners
+// included) are staged in shared memory, up to `sweeps` push/relabel sweeps
+// run with block barriers only, and the results go back as additive deltas.
+// Every tile of the image is visited concurrently in a round, so a tile's
+// ring heights are a snapshot and its neighbours change its pixels meanwhile;
+// that stays safe because every concurrent update is an addition: a pixel's
+// own capacity toward a neighbour falls only by its own pushes (never more
+// than the value it read, which others can only have raised), excess falls
+// only by its owner's pushes, and flow into another tile is added with
+// global atomics to the receiver's excess and reverse capacity.  Heights are
+// written only by their owner.  Stale ring heights can only make labels
+// inexact, never a flow invalid; the exact global relabel and its count
+// decide termination.
+constexpr int T8W = 32, T8H = 8;
+#ifndef GCFG_N8_ROUNDS
+#define GCFG_N8_ROUNDS 32   // tile rounds between global relabels
+#endif
+#ifndef GCFG_N8_SWEEPS
+#define GCFG_N8_SWEEPS 8    // sweeps per tile visit
+#endif
+__device__ void tile8_visit(const G8 &g, int t, int tiles_x, int sweeps) {
+    __shared__ int sh[T8H + 2][T8W + 2];
+    __shared__ int se[T8H][T8W];
+    __shared__ int sc[ND][T8H][T8W];
+    const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
+    const int x = (t % tiles_x) * T8W + lx, y = (t / tiles_x) * T8H + ly;
+    const bool inb = x < g.W && y < g.H;
+    const long long i = (long long)y * g.W + x;
+    int c0[ND];
+    const int e0 = inb ? g.e[i] : 0;
+#pragma unroll
+    for (int d = 0; d < ND; ++d) {
+        c0[d] = inb ? g.cap[(long long)d * g.n + i] : 0;
+        sc[d][ly][lx] = c0[d];
+    }
+    se[ly][lx] = e0;
+    auto hat = [&](int xx, int yy) -> int {
+        return xx >= 0 && yy >= 0 && xx < g.W && yy < g.H ? g.h[(long long)yy * g.W + xx] : INF_H;
+    };
+    sh[ly + 1][lx + 1] = inb ? g.h[i] : INF_H;
+    if (ly == 0) sh[0][lx + 1] = hat(x, y - 1);
+    if (ly == T8H - 1) sh[T8H + 1][lx + 1] = hat(x, y + 1);
+    if (lx == 0) sh[ly + 1][0] = hat(x - 1, y);
+    if (lx == T8W - 1) sh[ly + 1][T8W + 1] = hat(x + 1, y);
+    if (lx == 0 && ly == 0) sh[0][0] = hat(x - 1, y - 1);
+    if (lx == T8W - 1 && ly == 0) sh[0][T8W + 1] = hat(x + 1, y - 1);
+    if (lx == 0 && ly == T8H - 1) sh[T8H + 1][0] = hat(x - 1, y + 1);
+    if (lx == T8W - 1 && ly == T8H - 1) sh[T8H + 1][T8W + 1] = hat(x + 1, y + 1);
+    int hh = sh[ly + 1][lx + 1];
+    if (!__syncthreads_or(e0 > 0 && hh < INF_H)) return;  // nothing to push here
+    for (int s = 0; s < sweeps; ++s) {
+        // push half: heights fixed
+        bool pushed = false;
+        int e = se[ly][lx];
+        if (e > 0 && hh < INF_H) {
+            const int e_in = e;
+#pragma unroll
+            for (int d = 0; d < ND; ++d) {
+                const int dx = dxd(d), dy = dyd(d);
+                const int cd = sc[d][ly][lx];
+                if (e <= 0 || cd <= 0 || sh[ly + 1 + dy][lx + 1 + dx] != hh - 1) continue;
+                const int f = min(e, cd);
+                sc[d][ly][lx] = cd - f;
+                e -= f;
+                const int nx = lx + dx, ny = ly + dy;
+                if (nx >= 0 && ny >= 0 && nx < T8W && ny < T8H) {
+                    atomicAdd(&se[ny][nx], f);
+                    atomicAdd(&sc[opp(d)][ny][nx], f);
+                } else {
+                    const long long j = (long long)(y + dy) * g.W + (x + dx);
+                    atomicAdd(&g.e[j], f);
+                    atomicAdd(&g.cap[(long long)opp(d) * g.n + j], f);
+                }
+            }
+            if (e != e_in) {
+                atomicSub(&se[ly][lx], e_in - e);
+                pushed = true;
+            }
+        }
+        __syncthreads_or(pushed);
+        // relabel half: capacities and excess fixed
+        e = se[ly][lx];
+        if (e > 0 && hh < INF_H) {
+            int m = INF_H;
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+                if (sc[d][ly][lx] > 0) m = min(m, sh[ly + 1 + dyd(d)][lx + 1 + dxd(d)]);
+            if (m >= hh) {
+                hh = m >= INF_H - 1 ? INF_H : m + 1;
+                sh[ly + 1][lx + 1] = hh;
+            }
+        }
+        if (!__syncthreads_or(e > 0 && hh < INF_H)) break;
+    }
+    if (inb) {
+        g.h[i] = hh;
+        const int de = se[ly][lx] - e0;
+        if (de) atomicAdd(&g.e[i], de);
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+            const int dc = sc[d][ly][lx] - c0[d];
+            if (dc) atomicAdd(&g.cap[(long long)d * g.n + i], dc);
+        }
+    }
+    __syncthreads();  // the shared arrays are reused by the block's next tile
+}
+
 __global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
     Ctl8 *c = g.ctl;
     const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -193,37 +302,11 @@ __global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
             finished = true;
             break;
         }
-        // ---- push / relabel pulses ----
+        // ---- tile rounds: every tile once per round, block-local sweeps ----
+        const int tiles_x = (g.W + T8W - 1) / T8W;
+        const int ntiles = tiles_x * ((g.H + T8H - 1) / T8H);
         for (int p = 0; p < prm.pulses; ++p) {
-            for (long long i = gtid; i < g.n; i += nth) {
-                int e = g.e[i];
-                const int hi = g.h[i];
-                if (e <= 0 || hi >= INF_H) continue;
-                const int e0 = e;
-                for (int d = 0; d < ND && e > 0; ++d) {
-                    const int cd = g.cap[(long long)d * g.n + i];
-                    int j;
-                    if (cd <= 0 || !nbr(g, (int)i, d, j) || g.h[j] != hi - 1) continue;
-                    const int f = min(e, cd);
-                    g.cap[(long long)d * g.n + i] = cd - f;
-                    atomicAdd(&g.cap[(long long)opp(d) * g.n + j], f);
-                    atomicAdd(&g.e[j], f);
-                    e -= f;
-                }
-                if (e != e0) atomicSub(&g.e[i], e0 - e);
-            }
-            if (!sync8(c, -1)) return;
-            for (long long i = gtid; i < g.n; i += nth) {
-                const int e = g.e[i];
-                const int hi = g.h[i];
-                if (e <= 0 || hi >= INF_H) continue;
-                int m = INF_H;
-                for (int d = 0; d < ND; ++d) {
-                    int j;
-                    if (g.cap[(long long)d * g.n + i] > 0 && nbr(g, (int)i, d, j)) m = min(m, g.h[j]);
-                }
-                if (m >= hi) g.h[i] = m >= INF_H - 1 ? INF_H : m + 1;
-            }
+            for (int t = blockIdx.x; t < ntiles; t += gridDim.x) tile8_visit(g, t, tiles_x, prm.sweeps);
             if (gtid == 0) c->pulses++;
             if (!sync8(c, -1)) return;
         }
@@ -295,10 +378,10 @@ struct gcfg_graph8 {
     Ctl8 *ctl = nullptr, *h_ctl = nullptr;
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    // schedule (measured on a 640x480 graph with a constant penalty of 600:
-    // 64 pulses per global relabel take 6.4 / 6.3 / 5.5 / 7.5 ms at 1 / 2 / 3 /
-    // 4 blocks per SM; 8, 16, 32 and 128 pulses take longer at every count)
-    int pulses = 64, max_outer = 100000, blocks_per_sm = 3;
+    // schedule (measured on a 640x480 graph with a constant penalty of 600,
+    // 3 blocks per SM: 32 tile rounds per global relabel with 8 sweeps per
+    // visit take 3.0 ms; 16 rounds 3.7 ms, 64 rounds 4.1 ms, 8 rounds 4.2 ms)
+    int pulses = GCFG_N8_ROUNDS, max_outer = 100000, blocks_per_sm = 3, sweeps = GCFG_N8_SWEEPS;
 
     G8 g() const {
         G8 x;
@@ -429,7 +512,7 @@ gcfg_status gcfg_optimize8(gcfg_graph8 *g, int32_t *host_label, gcfg_result *res
     long long grid = (long long)(per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
     if (want < grid) grid = want > 0 ? want : 1;
     G8 gg = g->g();
-    P8 prm{g->max_outer, g->pulses};
+    P8 prm{g->max_outer, g->pulses, g->sweeps};
     void *args[] = {&gg, &prm};
     GCFG_CK(cudaEventRecord(g->ev0, g->st));
     GCFG_CK(cudaLaunchCooperativeKernel((const void *)k8_solve, dim3((unsigned)grid), dim3(256), args, 0, g->st));

@@ -139,9 +139,10 @@ gcfg_status gcfg_optimize8(gcfg_graph8 *g, int32_t *host_label, gcfg_result *res
 gcfg_status gcfg_get_cuts8(gcfg_graph8 *g, uint8_t *d_smin, uint8_t *d_smax);
 gcfg_status gcfg_end8(gcfg_graph8 *g);
 gcfg_status gcfg_set_stream8(gcfg_graph8 *g, void *stream);
-/* Push/relabel pulses between exact global relabels (default 64) and blocks
- * of the cooperative launch per SM (default 2; 0 = as many as fit); the
- * solver schedule only, results do not depend on it. */
+/* Tile rounds between exact global relabels (default 32; every 32x8 tile is
+ * visited once per round, with up to 8 block-local push/relabel sweeps) and
+ * blocks of the cooperative launch per SM (default 3; 0 = as many as fit);
+ * the solver schedule only, results do not depend on it. */
 gcfg_status gcfg_set_schedule8(gcfg_graph8 *g, int pulses_per_gr, int blocks_per_sm);
 
 /* ---------------- data term + n-links ---------------- */
