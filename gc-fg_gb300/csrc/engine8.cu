@@ -35,7 +35,7 @@ struct Ctl8 {
     unsigned bar_count, bar_gen;
     int err, err_code;
     int fsize[2];
-    int pad0[2];
+    int round_active[3];  // tiles that had work in tile round p, at [p % 3]
     unsigned long long active, pos_excess, interior_dp, ref_init;
     int global_relabels, pulses, gr_levels, reach_levels;
 };
@@ -154,6 +154,8 @@ __global__ void k8_build(G8 g, const int *__restrict__ dp, const int *__restrict
 // capacities, excess and heights and a one-pixel ring of heights (corners
 // included) are staged in shared memory, up to `sweeps` push/relabel sweeps
 // run with block barriers only, and the results go back as additive deltas.
+// A tile without a pixel that has excess and a finite height is left after
+// reading its excess and heights (returns false).
 // Every tile of the image is visited concurrently in a round, so a tile's
 // ring heights are a snapshot and its neighbours change its pixels meanwhile;
 // that stays safe because every concurrent update is an addition: a pixel's
@@ -171,7 +173,7 @@ constexpr int T8W = 32, T8H = 8;
 #ifndef GCFG_N8_SWEEPS
 #define GCFG_N8_SWEEPS 8    // sweeps per tile visit
 #endif
-__device__ void tile8_visit(const G8 &g, int t, int tiles_x, int sweeps) {
+__device__ bool tile8_visit(const G8 &g, int t, int tiles_x, int sweeps) {
     __shared__ int sh[T8H + 2][T8W + 2];
     __shared__ int se[T8H][T8W];
     __shared__ int sc[ND][T8H][T8W];
@@ -179,8 +181,10 @@ __device__ void tile8_visit(const G8 &g, int t, int tiles_x, int sweeps) {
     const int x = (t % tiles_x) * T8W + lx, y = (t / tiles_x) * T8H + ly;
     const bool inb = x < g.W && y < g.H;
     const long long i = (long long)y * g.W + x;
-    int c0[ND];
     const int e0 = inb ? g.e[i] : 0;
+    int hh = inb ? g.h[i] : INF_H;
+    if (!__syncthreads_or(e0 > 0 && hh < INF_H)) return false;  // nothing to push here
+    int c0[ND];
 #pragma unroll
     for (int d = 0; d < ND; ++d) {
         c0[d] = inb ? g.cap[(long long)d * g.n + i] : 0;
@@ -190,7 +194,7 @@ __device__ void tile8_visit(const G8 &g, int t, int tiles_x, int sweeps) {
     auto hat = [&](int xx, int yy) -> int {
         return xx >= 0 && yy >= 0 && xx < g.W && yy < g.H ? g.h[(long long)yy * g.W + xx] : INF_H;
     };
-    sh[ly + 1][lx + 1] = inb ? g.h[i] : INF_H;
+    sh[ly + 1][lx + 1] = hh;
     if (ly == 0) sh[0][lx + 1] = hat(x, y - 1);
     if (ly == T8H - 1) sh[T8H + 1][lx + 1] = hat(x, y + 1);
     if (lx == 0) sh[ly + 1][0] = hat(x - 1, y);
@@ -199,8 +203,7 @@ __device__ void tile8_visit(const G8 &g, int t, int tiles_x, int sweeps) {
     if (lx == T8W - 1 && ly == 0) sh[0][T8W + 1] = hat(x + 1, y - 1);
     if (lx == 0 && ly == T8H - 1) sh[T8H + 1][0] = hat(x - 1, y + 1);
     if (lx == T8W - 1 && ly == T8H - 1) sh[T8H + 1][T8W + 1] = hat(x + 1, y + 1);
-    int hh = sh[ly + 1][lx + 1];
-    if (!__syncthreads_or(e0 > 0 && hh < INF_H)) return;  // nothing to push here
+    __syncthreads();
     for (int s = 0; s < sweeps; ++s) {
         // push half: heights fixed
         bool pushed = false;
@@ -256,6 +259,7 @@ __device__ void tile8_visit(const G8 &g, int t, int tiles_x, int sweeps) {
         }
     }
     __syncthreads();  // the shared arrays are reused by the block's next tile
+    return true;
 }
 
 __global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
@@ -263,6 +267,7 @@ __global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
     const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long nth = (long long)gridDim.x * blockDim.x;
     bool finished = false;
+    int R = 0;  // tile rounds so far in this solve (grid-uniform)
     for (int outer = 0; outer < prm.max_outer; ++outer) {
         // ---- exact global relabel ----
         for (long long i = gtid; i < g.n; i += nth) {
@@ -306,9 +311,18 @@ __global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
         const int tiles_x = (g.W + T8W - 1) / T8W;
         const int ntiles = tiles_x * ((g.H + T8H - 1) / T8H);
         for (int p = 0; p < prm.pulses; ++p) {
-            for (int t = blockIdx.x; t < ntiles; t += gridDim.x) tile8_visit(g, t, tiles_x, prm.sweeps);
+            // round_active[R % 3] counts this round's tiles with work and is read
+            // after the round's barrier; the counter of round R + 1 was last read
+            // after the barrier of round R - 2, which every block has passed
+            if (gtid == 0) c->round_active[(R + 1) % 3] = 0;
+            int worked = 0;
+            for (int t = blockIdx.x; t < ntiles; t += gridDim.x) worked += tile8_visit(g, t, tiles_x, prm.sweeps);
+            if (threadIdx.x == 0 && worked) atomicAdd(&c->round_active[R % 3], worked);
             if (gtid == 0) c->pulses++;
             if (!sync8(c, -1)) return;
+            const int done_round = *(volatile int *)&c->round_active[R % 3] == 0;
+            ++R;
+            if (done_round) break;  // nothing left to push: relabel
         }
     }
     if (!finished) {
