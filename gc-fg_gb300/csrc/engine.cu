@@ -770,13 +770,13 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
             need_bfs = false;
             continue;
         }
-        // ---- relabel phase: capacities and excess fixed ----
+        // ---- relabel phase: capacities and excess fixed (own heights as
+        // loaded for the push phase: only their owner writes them) ----
         int act = 0;
 #pragma unroll
         for (int k = 0; k < ROWS_PER_WARP; ++k) {
             const int r = warp + 8 * k;
             ev[k] = s.e[r][lane];
-            hv[k] = s.h[r + 1][lane + 1];
         }
 #pragma unroll
         for (int k = 0; k < ROWS_PER_WARP; ++k) {
