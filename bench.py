@@ -441,12 +441,19 @@ def run_n8(args, rank, world):
     stream = torch.cuda.current_stream()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     torch.cuda.synchronize()
+    solve_ms = []
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    l0 = gcfg.launch_count()
     for i in range(args.steps):
         ev[i][0].record(stream)
         gcfg.GC_SetGraph8(gw)
         r = gcfg.GC_Optimize8(gw, label)
         ev[i][1].record(stream)
+        solve_ms.append(r["ms"])
     torch.cuda.synchronize()
+    launches = gcfg.launch_count() - l0
+    clk = clocks.stop()
     ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
     gcfg.GC_End8(gw)
     hdp, hdn = dp.cpu().numpy().reshape(H, W), dn.cpu().numpy().reshape(H, W)
@@ -454,6 +461,27 @@ def run_n8(args, rank, world):
     o = O.solve8(hdp, hdn, penalty=pen)
     cpu_s = time.perf_counter() - t
     value = W * H / (ms / 1e3) / 1e6
+    # Algorithmic bytes of the solve kernel in the int32 layout (eight
+    # capacity planes): a global relabel reads caps + excess and writes the
+    # height (40 B/px), its count reads excess + height (8 B/px); a tile visit
+    # that had work reads caps + excess + height and writes them (80 B/px), a
+    # visit without work reads excess + height (8 B/px); the cut pass reads
+    # excess and writes the mark (8 B/px).
+    n = W * H
+    tiles8 = ((W + 31) // 32) * ((H + 7) // 8)
+    visits, rounds = r["push_tiles"], r["push_rounds"]
+    alg = (r["global_relabels"] * n * (40 + 8) + visits * 256 * 80 + (rounds * tiles8 - visits) * 256 * 8 + n * 8)
+    avg_solve_ms = sum(solve_ms) / len(solve_ms)
+    peak, peak_kind = load_peaks()
+    achieved = alg / (avg_solve_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "k8_solve", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak,
+                "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                else "of fallback 6.8 TB/s",
+                "traffic": ncu_traffic("solve8", "n8_640x480"),
+                "alg_bytes_per_launch": alg, "avg_launch_us": avg_solve_ms * 1e3,
+                "note": "a 640x480 graph is about 15 MB in this layout and stays in L2; the solve is bound by "
+                        "its grid barriers (one per tile or relabel round), not by HBM"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded in-repo generator; no dataset)",
@@ -461,16 +489,16 @@ def run_n8(args, rank, world):
                        "generated image, penalty 600 on all eight directions", "parallelism": f"replicas x{world}"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 4 * W * H,
                     "note": "labels to the host inside the timed step; t-links resident"},
-            "roofline": None, "gpu_launches": 2 * args.steps,
-            "solver": {"global_relabels": r["global_relabels"], "gr_levels": r["gr_sweeps"],
-                       "tile_rounds": r["push_rounds"]},
+            "roofline": roofline, "clocks": clk, "gpu_launches": launches,
+            "solver": {"global_relabels": r["global_relabels"], "gr_rounds": r["gr_sweeps"],
+                       "tile_rounds": r["push_rounds"], "tile_visits": visits, "cut_levels": r["cut_sweeps"]},
             "cpu_baseline": {"value": W * H / cpu_s / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
                              "sample": f"one solve of the same graph, oracle 8-connected push-relabel, {cpu_s:.2f} s"},
             "parity": {"flow_equal_oracle": bool(r["flow"] == o["flow"]),
                        "labels_equal_oracle": bool((label.reshape(H, W) == o["smax"]).all())}}
     # the reference's own NEIGHBORHOOD 8 build of its kernels on the same GPU and graph
     import ref_cuda
-    why = ref_cuda.unavailable(8)
+    why = ref_cuda.unavailable(8) or ("not run (--ref-cuda-budget 0)" if args.ref_cuda_budget <= 0 else None)
     if why:
         line["reference_cuda"] = {"unavailable": why}
     else:

@@ -7,8 +7,10 @@
 // capacities are eight planes, cap[d * n + i] from pixel i toward direction
 // d (0 left, 1 right, 2 up, 3 down, 4 up-left, 5 up-right, 6 down-left,
 // 7 down-right).  One cooperative launch runs the whole solve:
-//   * exact global relabel: a frontier BFS from the sink-connected pixels
-//     (excess < 0) over the reverse residual edges, level by level;
+//   * exact global relabel: the distances to the sink-connected pixels
+//     (excess < 0) over the residual edges, by Bellman-Ford rounds over
+//     32x32 tiles, each tile relaxed to its fixpoint in shared memory
+//     (gr8_tile);
 //   * count: pixels with excess that can still reach the sink; none left
 //     after an exact global relabel means the preflow is maximum (an exact
 //     termination test);
@@ -35,9 +37,10 @@ struct Ctl8 {
     unsigned bar_count, bar_gen;
     int err, err_code;
     int fsize[2];
-    int round_active[3];  // tiles that had work in tile round p, at [p % 3]
+    int round_active[3];  // tiles that had work (or changed a height) in round p, at [p % 3]
     unsigned long long active, pos_excess, interior_dp, ref_init;
-    int global_relabels, pulses, gr_levels, reach_levels;
+    unsigned long long tile_visits;  // push visits of tiles that had work
+    int global_relabels, pulses, gr_rounds, reach_levels;
 };
 
 struct G8 {
@@ -168,7 +171,7 @@ __global__ void k8_build(G8 g, const int *__restrict__ dp, const int *__restrict
 // decide termination.
 constexpr int T8W = 32, T8H = 8;
 #ifndef GCFG_N8_ROUNDS
-#define GCFG_N8_ROUNDS 32   // tile rounds between global relabels
+#define GCFG_N8_ROUNDS 12   // tile rounds between global relabels
 #endif
 #ifndef GCFG_N8_SWEEPS
 #define GCFG_N8_SWEEPS 8    // sweeps per tile visit
@@ -262,40 +265,127 @@ __device__ bool tile8_visit(const G8 &g, int t, int tiles_x, int sweeps) {
     return true;
 }
 
+// ---- exact global relabel: Bellman-Ford rounds over 32x32 tiles ----
+// Heights are 1 on the sink-connected pixels (excess < 0) and otherwise
+// 1 + the fewest residual edges to one of them (INF when there is none), as a
+// frontier BFS from those pixels would give.  A round visits every tile once:
+// the tile's heights and a ring of its neighbours' heights go to shared
+// memory, h(u) = min(h(u), 1 + min over residual u -> v of h(v)) is swept to
+// the tile's fixpoint, and the heights go back.  Every height ever written is
+// the length of a real path to the sink (or INF), so a neighbour that reads a
+// height mid-round reads a valid upper bound; a round in which no tile
+// changed a height leaves every residual edge with h(u) <= h(v) + 1, which
+// with those upper bounds makes every height exact.  A shortest path about
+// as long as a tile side crosses few tiles, so a relabel takes a few rounds
+// (grid barriers) where a level-synchronous BFS takes one per level.
+constexpr int G8W = 32, G8H = 32;
+constexpr int G8_ROWS = G8H / 8;  // rows per thread (256 threads)
+
+// first: the stored heights are stale, so every height starts from the seed
+// (1 if excess < 0, else INF) and the ring reads seeds from the excess too.
+// Returns whether a height of the tile ended below its value at the start of
+// the visit (the value a neighbour may have read).
+__device__ bool gr8_tile(const G8 &g, int t, int tiles_x, bool first) {
+    __shared__ int gh[G8H + 2][G8W + 2];
+    const int lx = threadIdx.x & 31, wy = threadIdx.x >> 5;
+    const int x0 = (t % tiles_x) * G8W, y0 = (t / tiles_x) * G8H;
+    auto outside = [&](int xx, int yy) { return xx < 0 || yy < 0 || xx >= g.W || yy >= g.H; };
+    auto height = [&](long long j) -> int {
+        return first ? (g.e[j] < 0 ? 1 : INF_H) : *(volatile const int *)&g.h[j];
+    };
+    auto ring = [&](int xx, int yy) -> int {
+        return outside(xx, yy) ? INF_H : height((long long)yy * g.W + xx);
+    };
+    unsigned rm[G8_ROWS];  // residual directions of this thread's pixels (bit d: cap toward d > 0)
+    int h0[G8_ROWS];
+#pragma unroll
+    for (int k = 0; k < G8_ROWS; ++k) {
+        const int ly = wy + 8 * k, x = x0 + lx, y = y0 + ly;
+        int hv = INF_H;
+        unsigned m = 0;
+        if (!outside(x, y)) {
+            const long long i = (long long)y * g.W + x;
+            hv = height(i);
+            if (hv != 1) {
+#pragma unroll
+                for (int d = 0; d < ND; ++d) m |= (g.cap[(long long)d * g.n + i] > 0 ? 1u : 0u) << d;
+            }
+        }
+        rm[k] = m;
+        h0[k] = hv;
+        gh[ly + 1][lx + 1] = hv;
+    }
+    if (wy == 0) gh[0][lx + 1] = ring(x0 + lx, y0 - 1);
+    if (wy == 1) gh[G8H + 1][lx + 1] = ring(x0 + lx, y0 + G8H);
+    if (wy == 2) gh[lx + 1][0] = ring(x0 - 1, y0 + lx);
+    if (wy == 3) gh[lx + 1][G8W + 1] = ring(x0 + G8W, y0 + lx);
+    if (wy == 4 && lx < 4) {
+        const int cx = lx & 1 ? G8W + 1 : 0, cy = lx & 2 ? G8H + 1 : 0;
+        gh[cy][cx] = ring(x0 - 1 + cx, y0 - 1 + cy);
+    }
+    __syncthreads();
+    // A tile's fixpoint takes at most one sweep per pixel of the tile (plus
+    // the sweep that sees no change); a visit that stops at the bound has
+    // changed heights, so another round follows.
+    for (int s = 0; s <= G8W * G8H; ++s) {
+        bool ch = false;
+#pragma unroll
+        for (int k = 0; k < G8_ROWS; ++k) {
+            if (!rm[k]) continue;
+            const int ly = wy + 8 * k;
+            int m = INF_H;
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+                if ((rm[k] >> d) & 1u) m = min(m, gh[ly + 1 + dyd(d)][lx + 1 + dxd(d)]);
+            const int nh = m >= INF_H - 1 ? INF_H : m + 1;
+            if (nh < gh[ly + 1][lx + 1]) {
+                gh[ly + 1][lx + 1] = nh;
+                ch = true;
+            }
+        }
+        if (!__syncthreads_or(ch)) break;
+    }
+    bool changed = false;
+#pragma unroll
+    for (int k = 0; k < G8_ROWS; ++k) {
+        const int ly = wy + 8 * k, x = x0 + lx, y = y0 + ly;
+        if (outside(x, y)) continue;
+        const int hv = gh[ly + 1][lx + 1];
+        if (first || hv != h0[k]) g.h[(long long)y * g.W + x] = hv;
+        changed |= hv != h0[k];
+    }
+    return __syncthreads_or(changed);  // also: gh is reused by the block's next tile
+}
+
 __global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
     Ctl8 *c = g.ctl;
     const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long nth = (long long)gridDim.x * blockDim.x;
     bool finished = false;
-    int R = 0;  // tile rounds so far in this solve (grid-uniform)
+    int R = 0;  // tile and relabel rounds so far in this solve (grid-uniform)
+    const int gtiles_x = (g.W + G8W - 1) / G8W;
+    const int gtiles = gtiles_x * ((g.H + G8H - 1) / G8H);
     for (int outer = 0; outer < prm.max_outer; ++outer) {
-        // ---- exact global relabel ----
-        for (long long i = gtid; i < g.n; i += nth) {
-            const bool s = g.e[i] < 0;
-            g.h[i] = s ? 1 : INF_H;
-            if (s) append(g, g.fr0, 0, (int)i);
-        }
-        if (gtid == 0) c->active = 0;
-        if (!sync8(c, 1)) return;
-        for (int L = 1;; ++L) {
-            const int cur = (L - 1) & 1, nxt = L & 1;
-            const int ncur = *(volatile int *)&c->fsize[cur];
-            if (ncur == 0) break;
-            const int *fc = cur ? g.fr1 : g.fr0;
-            int *fn = nxt ? g.fr1 : g.fr0;
-            for (long long k = gtid; k < ncur; k += nth) {
-                const int v = fc[k];
-                for (int d = 0; d < ND; ++d) {
-                    int u;
-                    if (!nbr(g, v, d, u)) continue;
-                    // u -> v is u's edge in the opposite direction
-                    if (g.cap[(long long)opp(d) * g.n + u] > 0 && *(volatile int *)&g.h[u] == INF_H &&
-                        atomicCAS(&g.h[u], INF_H, L + 1) == INF_H)
-                        append(g, fn, nxt, u);
-                }
+        // ---- exact global relabel (gr8_tile rounds) ----
+        // The round counters are the tile rounds' (round_active, R), with the
+        // same clearing rule.
+        for (int q = 0;; ++q) {
+            if (gtid == 0) {
+                c->round_active[(R + 1) % 3] = 0;
+                if (q == 0) c->active = 0;
             }
-            if (gtid == 0) c->gr_levels++;
-            if (!sync8(c, cur)) return;
+            int changed = 0;
+            for (int t = blockIdx.x; t < gtiles; t += gridDim.x) changed += gr8_tile(g, t, gtiles_x, q == 0);
+            if (threadIdx.x == 0 && changed) atomicAdd(&c->round_active[R % 3], changed);
+            if (gtid == 0) c->gr_rounds++;
+            if (!sync8(c, -1)) return;
+            const int more = *(volatile int *)&c->round_active[R % 3];
+            ++R;
+            if (!more) break;
+            if (q > g.n) {  // unreachable: a round makes at least one more path segment exact
+                if (gtid == 0) set_err8(c, E8_OUTER);
+                return;
+            }
         }
         if (gtid == 0) c->global_relabels++;
         // ---- count: excess that can still reach the sink ----
@@ -317,7 +407,10 @@ __global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
             if (gtid == 0) c->round_active[(R + 1) % 3] = 0;
             int worked = 0;
             for (int t = blockIdx.x; t < ntiles; t += gridDim.x) worked += tile8_visit(g, t, tiles_x, prm.sweeps);
-            if (threadIdx.x == 0 && worked) atomicAdd(&c->round_active[R % 3], worked);
+            if (threadIdx.x == 0 && worked) {
+                atomicAdd(&c->round_active[R % 3], worked);
+                atomicAdd(&c->tile_visits, (unsigned long long)worked);
+            }
             if (gtid == 0) c->pulses++;
             if (!sync8(c, -1)) return;
             const int done_round = *(volatile int *)&c->round_active[R % 3] == 0;
@@ -391,10 +484,11 @@ struct gcfg_graph8 {
     int32_t *d_label = nullptr;
     Ctl8 *ctl = nullptr, *h_ctl = nullptr;
     cudaStream_t st = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;  // solve start, solve end, extract end
     // schedule (measured on a 640x480 graph with a constant penalty of 600,
-    // 3 blocks per SM: 32 tile rounds per global relabel with 8 sweeps per
-    // visit take 3.0 ms; 16 rounds 3.7 ms, 64 rounds 4.1 ms, 8 rounds 4.2 ms)
+    // 8 sweeps per visit, solve kernel time: 12 tile rounds per global
+    // relabel take 0.96 ms at 3 blocks per SM and 1.03 ms at 2; 8 rounds
+    // 0.99 ms, 16 rounds 1.05 ms, 32 rounds 1.17 ms, 4 rounds 1.20 ms)
     int pulses = GCFG_N8_ROUNDS, max_outer = 100000, blocks_per_sm = 3, sweeps = GCFG_N8_SWEEPS;
 
     G8 g() const {
@@ -417,6 +511,7 @@ struct gcfg_graph8 {
         if (h_ctl) cudaFreeHost(h_ctl);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        if (ev2) cudaEventDestroy(ev2);
     }
 };
 
@@ -498,7 +593,8 @@ gcfg_status gcfg_init8(int w, int h, const int32_t *dp, const int32_t *dn, int32
         cudaMalloc(&g->d_label, n * sizeof(int)) != cudaSuccess || cudaMalloc(&g->ctl, sizeof(Ctl8)) != cudaSuccess ||
         cudaMallocHost(&g->h_ctl, sizeof(Ctl8)) != cudaSuccess)
         rc = GCFG_ERR_OOM;
-    if (rc == GCFG_OK && (cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess))
+    if (rc == GCFG_OK && (cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess ||
+                          cudaEventCreate(&g->ev2) != cudaSuccess))
         rc = GCFG_ERR_CUDA;
     if (rc == GCFG_OK && dp) {
         gcfg_set_dataterms8(g, dp, dn);
@@ -531,10 +627,11 @@ gcfg_status gcfg_optimize8(gcfg_graph8 *g, int32_t *host_label, gcfg_result *res
     GCFG_CK(cudaEventRecord(g->ev0, g->st));
     GCFG_CK(cudaLaunchCooperativeKernel((const void *)k8_solve, dim3((unsigned)grid), dim3(256), args, 0, g->st));
     g_launches.fetch_add(1, std::memory_order_relaxed);
+    GCFG_CK(cudaEventRecord(g->ev1, g->st));
     k8_extract<<<grid8(g->n), 256, 0, g->st>>>(gg, g->d_label, nullptr, nullptr);
     g_launches.fetch_add(1, std::memory_order_relaxed);
     GCFG_CK(cudaGetLastError());
-    GCFG_CK(cudaEventRecord(g->ev1, g->st));
+    GCFG_CK(cudaEventRecord(g->ev2, g->st));
     if (host_label)
         GCFG_CK(cudaMemcpyAsync(host_label, g->d_label, (size_t)g->n * sizeof(int32_t), cudaMemcpyDeviceToHost, g->st));
     GCFG_CK(cudaMemcpyAsync(g->h_ctl, g->ctl, sizeof(Ctl8), cudaMemcpyDeviceToHost, g->st));
@@ -549,9 +646,11 @@ gcfg_status gcfg_optimize8(gcfg_graph8 *g, int32_t *host_label, gcfg_result *res
         res->ref_energy = (int32_t)((uint32_t)c.ref_init - (uint32_t)c.pos_excess);
         res->status = st;
         res->global_relabels = c.global_relabels;
-        res->gr_sweeps = c.gr_levels;
+        res->gr_sweeps = c.gr_rounds;
         res->push_rounds = c.pulses;
         res->cut_sweeps = c.reach_levels;
+        res->push_tiles = (int64_t)c.tile_visits;
+        res->gr_tiles = (int64_t)c.gr_rounds * (((g->W + G8W - 1) / G8W) * (long long)((g->H + G8H - 1) / G8H));
         float ms = 0.f;
         cudaEventElapsedTime(&ms, g->ev0, g->ev1);
         res->ms = ms;

@@ -119,8 +119,9 @@ gcfg_status gcfg_set_schedule(gcfg_graph *g, int push_rounds_per_gr, int max_til
  * and to its left, and so on).  The diagonals of the interior pixels next to
  * the border are zeroed like the straight edges (GraphCutKernels.cu:147-151,
  * 204-208).  Capacities are limited to GCFG_MAX_CAP8 so that an excess over
- * nine edges stays inside int32.  A separate, pixel-parallel engine solves
- * these graphs (exact global relabels and termination, as for 4). */
+ * nine edges stays inside int32.  A separate engine solves these graphs
+ * (32x8 tile rounds of push/relabel, exact global relabels by tile
+ * relaxation, and the exact termination test, as for 4). */
 typedef struct gcfg_graph8 gcfg_graph8;
 #define GCFG_MAX_CAP8 ((1 << 27) - 1)
 
@@ -135,11 +136,16 @@ gcfg_status gcfg_set_edges8(gcfg_graph8 *g, const int32_t *up, const int32_t *do
                             const int32_t *downright);
 gcfg_status gcfg_set_penalty8(gcfg_graph8 *g, int32_t penalty);
 gcfg_status gcfg_set_graph8(gcfg_graph8 *g);
+/* gcfg_optimize8 fills flow, ref_energy, status, global_relabels, ms (the
+ * solve kernel), gr_sweeps (tile-relaxation rounds of the global relabels),
+ * gr_tiles (their 32x32 tile visits), push_rounds (tile rounds), push_tiles
+ * (32x8 tile visits that had work) and cut_sweeps (levels of the source-side
+ * closure); the other fields are 0. */
 gcfg_status gcfg_optimize8(gcfg_graph8 *g, int32_t *host_label, gcfg_result *res);
 gcfg_status gcfg_get_cuts8(gcfg_graph8 *g, uint8_t *d_smin, uint8_t *d_smax);
 gcfg_status gcfg_end8(gcfg_graph8 *g);
 gcfg_status gcfg_set_stream8(gcfg_graph8 *g, void *stream);
-/* Tile rounds between exact global relabels (default 32; every 32x8 tile is
+/* Tile rounds between exact global relabels (default 12; every 32x8 tile is
  * visited once per round, with up to 8 block-local push/relabel sweeps) and
  * blocks of the cooperative launch per SM (default 3; 0 = as many as fit);
  * the solver schedule only, results do not depend on it. */

@@ -150,6 +150,43 @@ def test_gpu8_640x480_vs_oracle():
     assert r["flow"] == o["flow"] and np.array_equal(smax, o["smax"]) and np.array_equal(smin, o["smin"])
 
 
+def _serpentine(H, W, period=4):
+    """A corridor that winds through the whole image: walls every `period`
+    rows with one open pixel, alternately at the right and the left end;
+    excess at the far end, sink capacity at the start.  Every residual path
+    crosses many 32x32 tiles, so each exact global relabel takes many tile
+    rounds, and the heights run to thousands."""
+    yy, xx = np.mgrid[0:H, 0:W]
+    wall = (yy % period == 0) & (yy > 0)
+    gap_x = np.where((yy // period) % 2 == 1, W - 3, 2)
+    open_ = ~wall | (xx == gap_x)
+    dxs = (-1, 1, 0, 0, -1, 1, -1, 1)
+    dys = (0, 0, -1, 1, -1, -1, 1, 1)
+    arrs = {}
+    for k, dx, dy in zip(DIRS, dxs, dys):
+        nb = np.zeros_like(open_)
+        nb[max(0, -dy):H - max(0, dy), max(0, -dx):W - max(0, dx)] = \
+            open_[max(0, dy):H - max(0, -dy), max(0, dx):W - max(0, -dx)]
+        arrs[k] = np.where(open_ & nb, 40, 0).astype(np.int32)
+    dp = np.zeros((H, W), np.int32)
+    dn = np.zeros((H, W), np.int32)
+    dn[1:3, 1:6] = 500
+    dp[H - 3:H - 1, W - 8:W - 1] = 30
+    return dp, dn, arrs
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("H,W", [(130, 150), (97, 203)])
+def test_gpu8_serpentine_vs_oracle(H, W):
+    dp, dn, arrs = _serpentine(H, W)
+    label, smin, smax, r = _gpu8(dp, dn, 0, arrs)
+    o = O.solve8(dp, dn, penalty=0, arrays=[arrs[k] for k in DIRS])
+    assert o["flow"] > 0
+    assert r["flow"] == o["flow"]
+    assert np.array_equal(smin, o["smin"]) and np.array_equal(smax, o["smax"])
+    assert r["gr_sweeps"] > 3 * r["global_relabels"]  # relabels that took many tile rounds
+
+
 @pytest.mark.gpu
 def test_gc_solve8_shim_reproduces_reference_pins(tmp_path):
     lib = gcfg.LIB_PATH
