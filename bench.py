@@ -491,7 +491,7 @@ def run_n8(args, rank, world):
                     "note": "labels to the host inside the timed step; t-links resident"},
             "roofline": roofline, "clocks": clk, "gpu_launches": launches,
             "solver": {"global_relabels": r["global_relabels"], "gr_rounds": r["gr_sweeps"],
-                       "tile_rounds": r["push_rounds"], "tile_visits": visits, "cut_levels": r["cut_sweeps"]},
+                       "tile_rounds": r["push_rounds"], "tile_visits": visits, "cut_rounds": r["cut_sweeps"]},
             "cpu_baseline": {"value": W * H / cpu_s / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
                              "sample": f"one solve of the same graph, oracle 8-connected push-relabel, {cpu_s:.2f} s"},
             "parity": {"flow_equal_oracle": bool(r["flow"] == o["flow"]),

@@ -18,7 +18,8 @@
 //     block-local push/relabel sweeps in shared memory (tile8_visit), the
 //     results added back as deltas;
 //   * cuts: S_max = pixels at height INF after the last exact global
-//     relabel, S_min = the forward closure of the pixels with excess.
+//     relabel, S_min = the forward closure of the pixels with excess, by
+//     rounds over 32x32 tiles like the global relabel (reach8_tile).
 // Every spin is bounded; a timeout or an iteration cap sets an error that
 // the host reports as GCFG_ERR_NOT_CONVERGED.
 #include <cstring>
@@ -36,11 +37,10 @@ __device__ __forceinline__ int opp(int d) { return d < 4 ? (d ^ 1) : 11 - d; }
 struct Ctl8 {
     unsigned bar_count, bar_gen;
     int err, err_code;
-    int fsize[2];
     int round_active[3];  // tiles that had work (or changed a height) in round p, at [p % 3]
     unsigned long long active, pos_excess, interior_dp, ref_init;
     unsigned long long tile_visits;  // push visits of tiles that had work
-    int global_relabels, pulses, gr_rounds, reach_levels;
+    int global_relabels, pulses, gr_rounds, reach_rounds;
 };
 
 struct G8 {
@@ -48,7 +48,6 @@ struct G8 {
     long long n;
     int *cap;  // 8 * n
     int *e, *h, *mark;
-    int *fr0, *fr1;
     Ctl8 *ctl;
 };
 
@@ -58,15 +57,14 @@ struct P8 {
     int sweeps;      // push/relabel sweeps per tile visit
 };
 
-enum { E8_BARRIER = 1, E8_OUTER = 2, E8_QUEUE = 3 };
+enum { E8_BARRIER = 1, E8_OUTER = 2 };
 
 __device__ __forceinline__ void set_err8(Ctl8 *c, int code) {
     atomicExch(&c->err, 1);
     atomicCAS(&c->err_code, 0, code);
 }
 
-// Grid barrier (bounded spin); the last block to arrive clears frontier
-// size `reset` (>= 0) before releasing the others.
+// Grid barrier (bounded spin).
 __device__ __forceinline__ unsigned atom_add_acq_rel8(unsigned *p, unsigned v) {
     unsigned old;
     asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
@@ -79,12 +77,11 @@ __device__ __forceinline__ unsigned ld_acquire8(const unsigned *p) {
     return v;
 }
 
-__device__ bool sync8(Ctl8 *c, int reset) {
+__device__ bool sync8(Ctl8 *c) {
     __syncthreads();
     if (threadIdx.x == 0) {
         const unsigned gen = ld_acquire8(&c->bar_gen);
         if (atom_add_acq_rel8(&c->bar_count, 1u) == gridDim.x - 1) {
-            if (reset >= 0) c->fsize[reset] = 0;
             c->bar_count = 0;
             atom_add_acq_rel8(&c->bar_gen, 1u);
         } else {
@@ -100,19 +97,6 @@ __device__ bool sync8(Ctl8 *c, int reset) {
     }
     // thread 0's reading of the error word decides for the whole block
     return !__syncthreads_or(threadIdx.x == 0 && *(volatile int *)&c->err != 0);
-}
-
-__device__ __forceinline__ void append(const G8 &g, int *fr, int slot, int v) {
-    const int pos = atomicAdd(&g.ctl->fsize[slot], 1);
-    if (pos < g.n) fr[pos] = v;
-    else set_err8(g.ctl, E8_QUEUE);
-}
-
-__device__ __forceinline__ bool nbr(const G8 &g, int i, int d, int &j) {
-    const int x = i % g.W + dxd(d), y = i / g.W + dyd(d);
-    if (x < 0 || y < 0 || x >= g.W || y >= g.H) return false;
-    j = y * g.W + x;
-    return true;
 }
 
 // Graph of the reference's InitGraph / InitGraphVarEdges with NEIGHBORHOOD
@@ -357,6 +341,87 @@ __device__ bool gr8_tile(const G8 &g, int t, int tiles_x, bool first) {
     return __syncthreads_or(changed);  // also: gh is reused by the block's next tile
 }
 
+// ---- the source-side closure (S_min) by rounds over 32x32 tiles ----
+// Marks start on the pixels with excess > 0; a visit stages the marks of the
+// tile and its ring, spreads them along the residual edges of the tile's
+// pixels (inside the tile and onto the ring) until nothing changes, and
+// writes the new marks back, ring pixels included (their own tile spreads
+// them in a later round).  Marks only ever go from 0 to 1, so a round in
+// which no visit wrote a mark leaves every residual edge out of a marked
+// pixel ending at a marked pixel: the marks are the closure.  Returns
+// whether the visit wrote a mark.
+__device__ bool reach8_tile(const G8 &g, int t, int tiles_x) {
+    __shared__ int gm[G8H + 2][G8W + 2];
+    const int lx = threadIdx.x & 31, wy = threadIdx.x >> 5;
+    const int x0 = (t % tiles_x) * G8W, y0 = (t / tiles_x) * G8H;
+    auto outside = [&](int xx, int yy) { return xx < 0 || yy < 0 || xx >= g.W || yy >= g.H; };
+    // a cell outside the image counts as marked, so that nothing is written there
+    auto mark_at = [&](int xx, int yy) -> int {
+        return outside(xx, yy) ? 1 : *(volatile const int *)&g.mark[(long long)yy * g.W + xx];
+    };
+    unsigned rm[G8_ROWS];
+    int m0[G8_ROWS];
+#pragma unroll
+    for (int k = 0; k < G8_ROWS; ++k) {
+        const int ly = wy + 8 * k, x = x0 + lx, y = y0 + ly;
+        const int mv = mark_at(x, y);
+        unsigned m = 0;
+        if (!outside(x, y)) {
+            const long long i = (long long)y * g.W + x;
+#pragma unroll
+            for (int d = 0; d < ND; ++d) m |= (g.cap[(long long)d * g.n + i] > 0 ? 1u : 0u) << d;
+        }
+        rm[k] = m;
+        m0[k] = mv;
+        gm[ly + 1][lx + 1] = mv;
+    }
+    // the ring: warps 0-3 one side each, warp 4 the corners; each keeps what it read
+    int rx = 0, ry = 0, r0 = 1;
+    if (wy < 4 || (wy == 4 && lx < 4)) {
+        if (wy == 0) { rx = lx + 1; ry = 0; }
+        else if (wy == 1) { rx = lx + 1; ry = G8H + 1; }
+        else if (wy == 2) { rx = 0; ry = lx + 1; }
+        else if (wy == 3) { rx = G8W + 1; ry = lx + 1; }
+        else { rx = lx & 1 ? G8W + 1 : 0; ry = lx & 2 ? G8H + 1 : 0; }
+        r0 = mark_at(x0 - 1 + rx, y0 - 1 + ry);
+        gm[ry][rx] = r0;
+    }
+    __syncthreads();
+    // each sweep that changes something marks a new cell of the tile or ring
+    for (int s = 0; s <= (G8W + 2) * (G8H + 2); ++s) {
+        bool ch = false;
+#pragma unroll
+        for (int k = 0; k < G8_ROWS; ++k) {
+            const int ly = wy + 8 * k;
+            if (!rm[k] || !gm[ly + 1][lx + 1]) continue;
+#pragma unroll
+            for (int d = 0; d < ND; ++d) {
+                if (!((rm[k] >> d) & 1u)) continue;
+                int *cell = &gm[ly + 1 + dyd(d)][lx + 1 + dxd(d)];
+                if (!*cell) {
+                    *cell = 1;
+                    ch = true;
+                }
+            }
+        }
+        if (!__syncthreads_or(ch)) break;
+    }
+    bool wrote = false;
+#pragma unroll
+    for (int k = 0; k < G8_ROWS; ++k) {
+        const int ly = wy + 8 * k, x = x0 + lx, y = y0 + ly;
+        if (!m0[k] && gm[ly + 1][lx + 1]) {  // m0 is 1 outside the image
+            g.mark[(long long)y * g.W + x] = 1;
+            wrote = true;
+        }
+    }
+    if (!r0 && gm[ry][rx]) {  // r0 is 1 for threads without a ring cell and outside the image
+        g.mark[(long long)(y0 - 1 + ry) * g.W + (x0 - 1 + rx)] = 1;
+        wrote = true;
+    }
+    return __syncthreads_or(wrote);  // also: gm is reused by the block's next tile
+}
+
 __global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
     Ctl8 *c = g.ctl;
     const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -378,7 +443,7 @@ __global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
             for (int t = blockIdx.x; t < gtiles; t += gridDim.x) changed += gr8_tile(g, t, gtiles_x, q == 0);
             if (threadIdx.x == 0 && changed) atomicAdd(&c->round_active[R % 3], changed);
             if (gtid == 0) c->gr_rounds++;
-            if (!sync8(c, -1)) return;
+            if (!sync8(c)) return;
             const int more = *(volatile int *)&c->round_active[R % 3];
             ++R;
             if (!more) break;
@@ -392,7 +457,7 @@ __global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
         unsigned long long act = 0;
         for (long long i = gtid; i < g.n; i += nth) act += g.e[i] > 0 && g.h[i] < INF_H;
         if (act) atomicAdd(&c->active, act);
-        if (!sync8(c, 0)) return;
+        if (!sync8(c)) return;
         if (*(volatile unsigned long long *)&c->active == 0) {
             finished = true;
             break;
@@ -412,7 +477,7 @@ __global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
                 atomicAdd(&c->tile_visits, (unsigned long long)worked);
             }
             if (gtid == 0) c->pulses++;
-            if (!sync8(c, -1)) return;
+            if (!sync8(c)) return;
             const int done_round = *(volatile int *)&c->round_active[R % 3] == 0;
             ++R;
             if (done_round) break;  // nothing left to push: relabel
@@ -426,29 +491,26 @@ __global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
     unsigned long long pos = 0;
     for (long long i = gtid; i < g.n; i += nth) {
         const int e = g.e[i];
-        const bool s = e > 0;
-        if (s) pos += (unsigned)e;
-        g.mark[i] = s;
-        if (s) append(g, g.fr0, 0, (int)i);
+        if (e > 0) pos += (unsigned)e;
+        g.mark[i] = e > 0;
     }
     if (pos) atomicAdd(&c->pos_excess, pos);
-    if (!sync8(c, 1)) return;
-    for (int L = 1;; ++L) {
-        const int cur = (L - 1) & 1, nxt = L & 1;
-        const int ncur = *(volatile int *)&c->fsize[cur];
-        if (ncur == 0) break;
-        const int *fc = cur ? g.fr1 : g.fr0;
-        int *fn = nxt ? g.fr1 : g.fr0;
-        for (long long k = gtid; k < ncur; k += nth) {
-            const int u = fc[k];
-            for (int d = 0; d < ND; ++d) {
-                int v;
-                if (!nbr(g, u, d, v) || g.cap[(long long)d * g.n + u] <= 0) continue;
-                if (*(volatile int *)&g.mark[v] == 0 && atomicCAS(&g.mark[v], 0, 1) == 0) append(g, fn, nxt, v);
-            }
+    if (!sync8(c)) return;
+    if (*(volatile unsigned long long *)&c->pos_excess == 0) return;  // nothing marked: S_min is empty
+    for (int q = 0;; ++q) {
+        if (gtid == 0) c->round_active[(R + 1) % 3] = 0;
+        int changed = 0;
+        for (int t = blockIdx.x; t < gtiles; t += gridDim.x) changed += reach8_tile(g, t, gtiles_x);
+        if (threadIdx.x == 0 && changed) atomicAdd(&c->round_active[R % 3], changed);
+        if (gtid == 0) c->reach_rounds++;
+        if (!sync8(c)) return;
+        const int more = *(volatile int *)&c->round_active[R % 3];
+        ++R;
+        if (!more) break;
+        if (q > g.n) {  // unreachable: every round but the last marks at least one more pixel
+            if (gtid == 0) set_err8(c, E8_OUTER);
+            return;
         }
-        if (gtid == 0) c->reach_levels++;
-        if (!sync8(c, cur)) return;
     }
 }
 
@@ -480,7 +542,7 @@ struct gcfg_graph8 {
     const int32_t *arr[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     int32_t penalty = 0;
     bool varying = false, built = false, solved = false;
-    int *cap = nullptr, *e = nullptr, *h = nullptr, *mark = nullptr, *fr0 = nullptr, *fr1 = nullptr;
+    int *cap = nullptr, *e = nullptr, *h = nullptr, *mark = nullptr;
     int32_t *d_label = nullptr;
     Ctl8 *ctl = nullptr, *h_ctl = nullptr;
     cudaStream_t st = nullptr;
@@ -500,13 +562,11 @@ struct gcfg_graph8 {
         x.e = e;
         x.h = h;
         x.mark = mark;
-        x.fr0 = fr0;
-        x.fr1 = fr1;
         x.ctl = ctl;
         return x;
     }
     void release() {
-        cudaFree(cap); cudaFree(e); cudaFree(h); cudaFree(mark); cudaFree(fr0); cudaFree(fr1);
+        cudaFree(cap); cudaFree(e); cudaFree(h); cudaFree(mark);
         cudaFree(d_label); cudaFree(ctl);
         if (h_ctl) cudaFreeHost(h_ctl);
         if (ev0) cudaEventDestroy(ev0);
@@ -589,7 +649,6 @@ gcfg_status gcfg_init8(int w, int h, const int32_t *dp, const int32_t *dn, int32
     gcfg_status rc = GCFG_OK;
     if (cudaMalloc(&g->cap, 8 * n * sizeof(int)) != cudaSuccess || cudaMalloc(&g->e, n * sizeof(int)) != cudaSuccess ||
         cudaMalloc(&g->h, n * sizeof(int)) != cudaSuccess || cudaMalloc(&g->mark, n * sizeof(int)) != cudaSuccess ||
-        cudaMalloc(&g->fr0, n * sizeof(int)) != cudaSuccess || cudaMalloc(&g->fr1, n * sizeof(int)) != cudaSuccess ||
         cudaMalloc(&g->d_label, n * sizeof(int)) != cudaSuccess || cudaMalloc(&g->ctl, sizeof(Ctl8)) != cudaSuccess ||
         cudaMallocHost(&g->h_ctl, sizeof(Ctl8)) != cudaSuccess)
         rc = GCFG_ERR_OOM;
@@ -648,7 +707,7 @@ gcfg_status gcfg_optimize8(gcfg_graph8 *g, int32_t *host_label, gcfg_result *res
         res->global_relabels = c.global_relabels;
         res->gr_sweeps = c.gr_rounds;
         res->push_rounds = c.pulses;
-        res->cut_sweeps = c.reach_levels;
+        res->cut_sweeps = c.reach_rounds;
         res->push_tiles = (int64_t)c.tile_visits;
         res->gr_tiles = (int64_t)c.gr_rounds * (((g->W + G8W - 1) / G8W) * (long long)((g->H + G8H - 1) / G8H));
         float ms = 0.f;

@@ -139,8 +139,8 @@ gcfg_status gcfg_set_graph8(gcfg_graph8 *g);
 /* gcfg_optimize8 fills flow, ref_energy, status, global_relabels, ms (the
  * solve kernel), gr_sweeps (tile-relaxation rounds of the global relabels),
  * gr_tiles (their 32x32 tile visits), push_rounds (tile rounds), push_tiles
- * (32x8 tile visits that had work) and cut_sweeps (levels of the source-side
- * closure); the other fields are 0. */
+ * (32x8 tile visits that had work) and cut_sweeps (tile rounds of the
+ * source-side closure); the other fields are 0. */
 gcfg_status gcfg_optimize8(gcfg_graph8 *g, int32_t *host_label, gcfg_result *res);
 gcfg_status gcfg_get_cuts8(gcfg_graph8 *g, uint8_t *d_smin, uint8_t *d_smax);
 gcfg_status gcfg_end8(gcfg_graph8 *g);

@@ -150,12 +150,14 @@ def test_gpu8_640x480_vs_oracle():
     assert r["flow"] == o["flow"] and np.array_equal(smax, o["smax"]) and np.array_equal(smin, o["smin"])
 
 
-def _serpentine(H, W, period=4):
+def _serpentine(H, W, period=4, source_first=False):
     """A corridor that winds through the whole image: walls every `period`
     rows with one open pixel, alternately at the right and the left end;
     excess at the far end, sink capacity at the start.  Every residual path
     crosses many 32x32 tiles, so each exact global relabel takes many tile
-    rounds, and the heights run to thousands."""
+    rounds, and the heights run to thousands.  source_first: a large excess
+    at the start and a small sink capacity at the far end instead, so that
+    S_min (the closure of the leftover excess) runs the corridor's length."""
     yy, xx = np.mgrid[0:H, 0:W]
     wall = (yy % period == 0) & (yy > 0)
     gap_x = np.where((yy // period) % 2 == 1, W - 3, 2)
@@ -170,21 +172,28 @@ def _serpentine(H, W, period=4):
         arrs[k] = np.where(open_ & nb, 40, 0).astype(np.int32)
     dp = np.zeros((H, W), np.int32)
     dn = np.zeros((H, W), np.int32)
-    dn[1:3, 1:6] = 500
-    dp[H - 3:H - 1, W - 8:W - 1] = 30
+    if source_first:
+        dp[1:3, 1:6] = 500
+        dn[H - 3:H - 1, W - 8:W - 1] = 2
+    else:
+        dn[1:3, 1:6] = 500
+        dp[H - 3:H - 1, W - 8:W - 1] = 30
     return dp, dn, arrs
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("H,W", [(130, 150), (97, 203)])
-def test_gpu8_serpentine_vs_oracle(H, W):
-    dp, dn, arrs = _serpentine(H, W)
+@pytest.mark.parametrize("H,W,source_first", [(130, 150, False), (97, 203, False), (130, 150, True),
+                                              (97, 203, True)])
+def test_gpu8_serpentine_vs_oracle(H, W, source_first):
+    dp, dn, arrs = _serpentine(H, W, source_first=source_first)
     label, smin, smax, r = _gpu8(dp, dn, 0, arrs)
     o = O.solve8(dp, dn, penalty=0, arrays=[arrs[k] for k in DIRS])
     assert o["flow"] > 0
     assert r["flow"] == o["flow"]
     assert np.array_equal(smin, o["smin"]) and np.array_equal(smax, o["smax"])
     assert r["gr_sweeps"] > 3 * r["global_relabels"]  # relabels that took many tile rounds
+    if source_first:
+        assert smin.sum() > H * W // 2 and r["cut_sweeps"] > 3  # a closure across many tiles
 
 
 @pytest.mark.gpu
