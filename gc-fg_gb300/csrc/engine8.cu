@@ -40,7 +40,7 @@ struct Ctl8 {
     int round_active[3];  // tiles that had work (or changed a height) in round p, at [p % 3]
     unsigned long long active, pos_excess, interior_dp, ref_init;
     unsigned long long tile_visits;  // push visits of tiles that had work
-    int global_relabels, pulses, gr_rounds, reach_rounds;
+    int global_relabels, tile_rounds, gr_rounds, reach_rounds;
 };
 
 struct G8 {
@@ -53,7 +53,7 @@ struct G8 {
 
 struct P8 {
     int max_outer;   // global relabels at most
-    int pulses;      // tile rounds between global relabels
+    int rounds;      // tile rounds between global relabels
     int sweeps;      // push/relabel sweeps per tile visit
 };
 
@@ -465,7 +465,7 @@ __global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
         // ---- tile rounds: every tile once per round, block-local sweeps ----
         const int tiles_x = (g.W + T8W - 1) / T8W;
         const int ntiles = tiles_x * ((g.H + T8H - 1) / T8H);
-        for (int p = 0; p < prm.pulses; ++p) {
+        for (int p = 0; p < prm.rounds; ++p) {
             // round_active[R % 3] counts this round's tiles with work and is read
             // after the round's barrier; the counter of round R + 1 was last read
             // after the barrier of round R - 2, which every block has passed
@@ -476,7 +476,7 @@ __global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
                 atomicAdd(&c->round_active[R % 3], worked);
                 atomicAdd(&c->tile_visits, (unsigned long long)worked);
             }
-            if (gtid == 0) c->pulses++;
+            if (gtid == 0) c->tile_rounds++;
             if (!sync8(c)) return;
             const int done_round = *(volatile int *)&c->round_active[R % 3] == 0;
             ++R;
@@ -551,7 +551,7 @@ struct gcfg_graph8 {
     // 8 sweeps per visit, solve kernel time: 12 tile rounds per global
     // relabel take 0.96 ms at 3 blocks per SM and 1.03 ms at 2; 8 rounds
     // 0.99 ms, 16 rounds 1.05 ms, 32 rounds 1.17 ms, 4 rounds 1.20 ms)
-    int pulses = GCFG_N8_ROUNDS, max_outer = 100000, blocks_per_sm = 3, sweeps = GCFG_N8_SWEEPS;
+    int rounds = GCFG_N8_ROUNDS, max_outer = 100000, blocks_per_sm = 3, sweeps = GCFG_N8_SWEEPS;
 
     G8 g() const {
         G8 x;
@@ -605,9 +605,9 @@ gcfg_status gcfg_set_penalty8(gcfg_graph8 *g, int32_t penalty) {
     return GCFG_OK;
 }
 
-gcfg_status gcfg_set_schedule8(gcfg_graph8 *g, int pulses_per_gr, int blocks_per_sm) {
-    if (!g || pulses_per_gr < 1 || blocks_per_sm < 0) return GCFG_ERR_INVALID;
-    g->pulses = pulses_per_gr;
+gcfg_status gcfg_set_schedule8(gcfg_graph8 *g, int rounds_per_gr, int blocks_per_sm) {
+    if (!g || rounds_per_gr < 1 || blocks_per_sm < 0) return GCFG_ERR_INVALID;
+    g->rounds = rounds_per_gr;
     g->blocks_per_sm = blocks_per_sm;
     return GCFG_OK;
 }
@@ -681,7 +681,7 @@ gcfg_status gcfg_optimize8(gcfg_graph8 *g, int32_t *host_label, gcfg_result *res
     long long grid = (long long)(per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
     if (want < grid) grid = want > 0 ? want : 1;
     G8 gg = g->g();
-    P8 prm{g->max_outer, g->pulses, g->sweeps};
+    P8 prm{g->max_outer, g->rounds, g->sweeps};
     void *args[] = {&gg, &prm};
     GCFG_CK(cudaEventRecord(g->ev0, g->st));
     GCFG_CK(cudaLaunchCooperativeKernel((const void *)k8_solve, dim3((unsigned)grid), dim3(256), args, 0, g->st));
@@ -706,7 +706,7 @@ gcfg_status gcfg_optimize8(gcfg_graph8 *g, int32_t *host_label, gcfg_result *res
         res->status = st;
         res->global_relabels = c.global_relabels;
         res->gr_sweeps = c.gr_rounds;
-        res->push_rounds = c.pulses;
+        res->push_rounds = c.tile_rounds;
         res->cut_sweeps = c.reach_rounds;
         res->push_tiles = (int64_t)c.tile_visits;
         res->gr_tiles = (int64_t)c.gr_rounds * (((g->W + G8W - 1) / G8W) * (long long)((g->H + G8H - 1) / G8H));

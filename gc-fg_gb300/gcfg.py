@@ -850,8 +850,8 @@ def GC_Optimize8(gw, label=None) -> dict:
     return res.as_dict()
 
 
-def GC_SetSchedule8(gw, pulses_per_gr, blocks_per_sm=0):
-    _check(load().gcfg_set_schedule8(gw.handle, int(pulses_per_gr), int(blocks_per_sm)), "gcfg_set_schedule8")
+def GC_SetSchedule8(gw, rounds_per_gr, blocks_per_sm=0):
+    _check(load().gcfg_set_schedule8(gw.handle, int(rounds_per_gr), int(blocks_per_sm)), "gcfg_set_schedule8")
 
 
 def GC_SetGraph8(gw):

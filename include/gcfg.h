@@ -149,7 +149,7 @@ gcfg_status gcfg_set_stream8(gcfg_graph8 *g, void *stream);
  * visited once per round, with up to 8 block-local push/relabel sweeps) and
  * blocks of the cooperative launch per SM (default 3; 0 = as many as fit);
  * the solver schedule only, results do not depend on it. */
-gcfg_status gcfg_set_schedule8(gcfg_graph8 *g, int pulses_per_gr, int blocks_per_sm);
+gcfg_status gcfg_set_schedule8(gcfg_graph8 *g, int rounds_per_gr, int blocks_per_sm);
 
 /* ---------------- data term + n-links ---------------- */
 
