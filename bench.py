@@ -6,13 +6,17 @@ graph build, exact max-flow, both canonical cuts.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--workload batch256|batch64|plain1080|plain256|plain4096|n8_640x480]
+                  [--no-single] [--no-serve] [--no-plain]
 
 Default workload (batch256): 256 images of uneven sizes (side log-uniform
 64..1024, aspect uniform 0.5..2, the 256x256 ellipse generator scaled to each
 image, per-image seeds 1000+i, lambda 50) solved as ONE batch: one data-term
 pass, one build, one persistent solver launch, one extraction.  The same
 images solved one at a time by the plain per-image path are timed beside it
-("plain_value").
+("plain_per_image"), and the single-image workloads (256x256, three
+1920x1080 images at lambda 10/50/200, 4096x4096 with 2000 blobs, and the
+8-neighbourhood 640x480 graph) are measured the same way under
+"single_image" (skipped with --no-single).
 
 value : Mpixel/s with the images already resident in HBM (CUDA events per
         step; a 256 MB buffer is written before every step to flush L2).
@@ -28,6 +32,11 @@ e2e   : the same metric through the host entry points: images and scribbles
 roofline: the kernel with the largest device time in a profiled step;
         achieved = its algorithmic bytes (work counters x bytes per pixel)
         / its CUDA-event time; peak = MEASURED_PEAKS.json hbm_gbs.
+        roofline.solve_phases: the solver's first global relabel and the push
+        rounds after it run as two separate launches (gcfg_batch_phase_split,
+        inside an NVTX range "phase_split" for ncu), each with its device
+        time, its algorithmic bytes, the bytes it really moves and the DRAM
+        traffic of its ncu capture (profiles/solve_gr_*.md, solve_push_*.md).
 cpu_baseline: the oracle's Boykov-Kolmogorov solver (oracle/, the CPU
         checker) on a bounded sample of the same images, one host thread.
 reference_cuda: the reference's own CUDA path on the same GPU (its kernels
@@ -73,6 +82,22 @@ UNIT = "Mpixel/s"
 #   build: read RGB (3 B), write 4 caps + excess (20 B)
 #   extract: read height (4 B) + reach bit, write two label bytes (2 B)
 B_GR, B_PUSH, B_REACH, B_COUNT, B_BUILD, B_EXTRACT = 24, 48, 20, 8, 23, 6
+
+# Bytes a solver phase really moves per tile visit in this build's layout
+# (what DRAM counters see when nothing is served from L2):
+#   global-relabel visit: read the tile's six residual mask planes (768 B),
+#     the neighbours' facing border-height lines (4 x 128 B) and their
+#     residual words (2 x 4 B + 2 x 128 B); write the heights (4096 B), the
+#     border lines (512 B), the reached rows (128 B) and the active count (4 B)
+#   per tile of the relabel launch besides its visits: fresh queue marks and
+#     reach rows (8 + 128 B), the pull check (own and neighbours' border
+#     lines and residual words, 512 + 512 + 264 B), the count pass (12 B)
+#   push visit: read caps, excess and heights (24 KB) and the four halo
+#     lines (512 B); write caps, excess and heights (24 KB), the mask planes
+#     (768 B), the border lines (512 B) and the excess sum (8 B)
+MOVED_GR_VISIT = 768 + 512 + 264 + 4096 + 512 + 128 + 4
+MOVED_GR_TILE = 8 + 128 + 512 + 512 + 264 + 12
+MOVED_PUSH_VISIT = 24576 + 512 + 24576 + 768 + 512 + 8
 
 
 def workload(name, rank=0):
@@ -195,23 +220,40 @@ def ncu_traffic(kind: str, workload_name: str):
     return None
 
 
-def cpu_baseline(views, lams, budget_s=10.0):
-    """Oracle BK on a bounded sample of the workload, one host thread."""
+def cpu_baseline(views, lams, budget_s=10.0, flows_gpu=None, smin_gpu=None, smax_gpu=None, offs=None):
+    """Oracle BK on a bounded sample of the workload, one host thread.  When
+    the GPU's flows and packed cuts are given, every sampled image's flow,
+    S_min and S_max are compared with the oracle's (the comparison is outside
+    the timed span).  Returns (Mpixel/s, images solved, seconds, parity)."""
     import oracle as O
     t0 = time.perf_counter()
-    px, flows, k = 0, [], 0
+    px, k, secs = 0, 0, 0.0
+    checked, eq_flow, eq_min, eq_max = set(), 0, 0, 0
     order = sorted(range(len(views)), key=lambda i: views[i][1].size)
-    while k < len(order):
+    while k < len(order) or len(views) <= 8:
         i = order[k] if len(views) > 8 else k % len(views)
         rgb, scrib = views[i]
+        t = time.perf_counter()
         r = O.segment(rgb, scrib, float(lams[i]), solver="bk")
-        flows.append((i, r["flow"]))
+        secs += time.perf_counter() - t
         px += scrib.size
         k += 1
+        if flows_gpu is not None and i not in checked:
+            checked.add(i)
+            eq_flow += int(flows_gpu[i]) == r["flow"]
+            if smin_gpu is not None:
+                o, n = int(offs[i]), scrib.size
+                eq_min += bool(np.array_equal(smin_gpu[o:o + n], r["smin"].reshape(-1)))
+                eq_max += bool(np.array_equal(smax_gpu[o:o + n], r["smax"].reshape(-1)))
         if time.perf_counter() - t0 > budget_s or (len(views) <= 8 and k >= 64):
             break
-    dt = time.perf_counter() - t0
-    return px / dt / 1e6, k, dt, flows
+    parity = None
+    if flows_gpu is not None:
+        n = len(checked)
+        parity = {"images_checked": n, "flows_equal_oracle": eq_flow == n}
+        if smin_gpu is not None:
+            parity.update(smin_equal_oracle=eq_min == n, smax_equal_oracle=eq_max == n)
+    return px / secs / 1e6, k, secs, parity
 
 
 def reference_cuda_leg(views, lams, smax_all, offs, budget_s=15.0):
@@ -263,6 +305,20 @@ def _sleep_until(now, ta):
             return
         if d > 1e-3:
             time.sleep(d - 5e-4)
+
+
+def _busy_time(results):
+    """Length of the union of the lanes' batch intervals (seconds)."""
+    iv = sorted({(r["t_start"], r["t_done"]) for r in results})
+    busy, end = 0.0, None
+    for a, b in iv:
+        if end is None or a > end:
+            busy += b - a
+            end = b
+        elif b > end:
+            busy += b - end
+            end = b
+    return busy
 
 
 def _lane_overlap(results):
@@ -347,6 +403,7 @@ def serve_bench(torch, gcfg, n_req=1200, rate=500.0, lanes=2, cap=60 << 30, seed
     res, tarr, st, dig_served = served(True)
     done = np.array([r["t_done"] for r in res])
     lat = done - tarr
+    svc = np.array([r["t_done"] - r["t_start"] for r in res])
     is_edit = np.array([q["kind"] == "edit" for q in reqs])
     res_sat, tarr_sat, st_sat, dig_sat = served(False)
     make_sat = max(r["t_done"] for r in res_sat) - tarr_sat[0]
@@ -361,7 +418,7 @@ def serve_bench(torch, gcfg, n_req=1200, rate=500.0, lanes=2, cap=60 << 30, seed
             if n_new in edited:
                 sess_scrib[n_new] = torch.from_numpy(pool_view(q["img"])[1].copy()).pin_memory().numpy()
             n_new += 1
-    p_lat, p_svc, dig_plain = [], [], []
+    p_lat, p_svc, p_done, dig_plain = [], [], [], []
     for warm in (True, False):
         n_new = 0
         t0 = now() + 0.02
@@ -384,10 +441,12 @@ def serve_bench(torch, gcfg, n_req=1200, rate=500.0, lanes=2, cap=60 << 30, seed
             if not warm:
                 p_lat.append(td - ta)
                 p_svc.append(td - ts)
+                p_done.append(td - t0)
                 dig_plain.append(out["flow"])
     seg.close()
     dig_plain = [digest(k, f) for k, f in enumerate(dig_plain)]
     p_lat = np.array(p_lat)
+    p_span = max(p_done) - reqs[0]["t"]
 
     def ms(a, p):
         return round(float(np.percentile(a, p)) * 1e3, 3)
@@ -401,29 +460,265 @@ def serve_bench(torch, gcfg, n_req=1200, rate=500.0, lanes=2, cap=60 << 30, seed
         "served": {"p50_ms": ms(lat, 50), "p99_ms": ms(lat, 99),
                    "p50_new_ms": ms(lat[~is_edit], 50), "p99_new_ms": ms(lat[~is_edit], 99),
                    "p50_edit_ms": ms(lat[is_edit], 50), "p99_edit_ms": ms(lat[is_edit], 99),
-                   "mpixel_s": total_px / (done.max() - tarr[0]) / 1e6,
+                   "mpixel_s_over_span": total_px / (done.max() - tarr[0]) / 1e6,
+                   "mpixel_s_over_busy": total_px / _busy_time(res) / 1e6,
+                   "mean_service_ms": float(np.mean(svc)) * 1e3,
                    "batches": st["batches"], "mean_batch_images": len(reqs) / max(st["batches"], 1),
                    "lane_overlap_frac": round(_lane_overlap(res), 4),
                    "resident_gb_at_end": st["bytes_in_use"] / 2 ** 30, "evicted": st["evicted"]},
         "served_saturated": {"mpixel_s": total_px / make_sat / 1e6, "makespan_ms": make_sat * 1e3,
                              "batches": st_sat["batches"]},
         "plain_cold_loop": {"p50_ms": ms(p_lat, 50), "p99_ms": ms(p_lat, 99),
-                            "mpixel_s": total_px / float(np.sum(p_svc)) / 1e6,
+                            "p50_new_ms": ms(p_lat[~is_edit], 50), "p99_new_ms": ms(p_lat[~is_edit], 99),
+                            "p50_edit_ms": ms(p_lat[is_edit], 50), "p99_edit_ms": ms(p_lat[is_edit], 99),
+                            "mpixel_s_over_span": total_px / p_span / 1e6,
+                            "mpixel_s_over_busy": total_px / float(np.sum(p_svc)) / 1e6,
                             "mean_service_ms": float(np.mean(p_svc)) * 1e3},
+        "throughput_note": "mpixel_s_over_span = all pixels / (last completion - first arrival): at 500 req/s the "
+                           "arrival rate bounds it for both; mpixel_s_over_busy = all pixels / the time the GPU "
+                           "side was busy (union of the lanes' batch intervals; the plain loop's summed service "
+                           "times); served_saturated submits the whole trace at once",
         "p99_target_ms": P99_TARGET_MS, "p99_met": bool(ms(lat, 99) <= P99_TARGET_MS),
         "results_equal": bool(dig_served == dig_plain and dig_sat == dig_plain),
     }
 
 
-def run_n8(args, rank, world):
+def nvtx_range(name):
+    """NVTX push/pop around a block (ncu --nvtx-include filters on it); a
+    no-op where NVTX is unavailable."""
+    import contextlib
+
+    @contextlib.contextmanager
+    def cm():
+        import torch
+        pushed = False
+        try:
+            torch.cuda.nvtx.range_push(name)
+            pushed = True
+        except Exception:
+            pass
+        try:
+            yield
+        finally:
+            if pushed:
+                torch.cuda.nvtx.range_pop()
+    return cm()
+
+
+def tiles_of(Ws, Hs):
+    return int(sum(((int(w) + 31) // 32) * ((int(h) + 31) // 32) for w, h in zip(Ws, Hs)))
+
+
+def peak_source(peak_kind):
+    return ("of measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "of fallback 6.8 TB/s")
+
+
+def phase_record(ms, alg, moved, traffic, peak, **extra):
+    """Device time of a phase with three byte counts over it: algorithmic
+    (int32 accounting), moved (what the phase reads and writes in this
+    layout) and, when an ncu capture exists, DRAM traffic."""
+    r = {"ms": round(ms, 4), "alg_bytes": int(alg), "moved_bytes": int(moved)}
+    if ms > 0:
+        a, m = alg / (ms / 1e3) / 1e9, moved / (ms / 1e3) / 1e9
+        r.update(achieved_alg_gbs=round(a, 1), frac_alg=round(a / peak, 4),
+                 achieved_moved_gbs=round(m, 1), frac_moved=round(m / peak, 4))
+    r["traffic"] = traffic
+    if traffic and ms > 0:
+        t = traffic / (ms / 1e3) / 1e9
+        r.update(achieved_dram_gbs=round(t, 1), frac_dram=round(t / peak, 4))
+    r.update(extra)
+    return r
+
+
+def ncu_phase_traffic(kind, workload_name):
+    """DRAM bytes of one phase over one pass of the workload, from a committed
+    ncu summary (profiles/solve_<kind>_<workload>.md, line traffic_bytes:)."""
+    p = os.path.join(ROOT, "profiles", f"solve_{kind}_{workload_name}.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+def solve_phases(gcfg, stream, Ws, Hs, lams, d_rgb, d_scrib, offs, peak, workload_name, batched, bs=None):
+    """The solver's first exact global relabel and the push rounds after it,
+    each as a launch of its own (gcfg_batch_phase_split), inside the NVTX
+    range "phase_split".  A batch is split as one batch; the images of a
+    per-image workload one at a time, as the plain solver runs them."""
+    own = bs is None
+    if own:
+        bs = gcfg.BatchSolver(len(Ws) if batched else 1,
+                              int(max(int(w) * int(h) for w, h in zip(Ws, Hs))) if not batched else
+                              int(sum(int(w) * int(h) for w, h in zip(Ws, Hs))))
+        bs.set_stream(stream)
+    groups = [list(range(len(Ws)))] if batched else [[i] for i in range(len(Ws))]
+    tot = {"ms_relabel": 0.0, "ms_push": 0.0, "relabel_tiles": 0, "push_tiles": 0, "push_sweeps": 0,
+           "push_local_relabels": 0, "relabel_rounds": 0, "push_phases": 0, "active_pixels": 0, "tiles": 0}
+    grid = []
+    for g in groups:
+        w, h, lam = Ws[g], Hs[g], lams[g]
+        if batched:
+            rgb, scr = d_rgb, d_scrib
+        else:
+            i = g[0]
+            o, n = int(offs[i]), int(Ws[i]) * int(Hs[i])
+            rgb, scr = d_rgb[3 * o:3 * (o + n)], d_scrib[o:o + n]
+        with nvtx_range("phase_split"):
+            ps = bs.phase_split(w, h, lam, rgb, scr)
+        for k in tot:
+            if k != "tiles":
+                tot[k] += ps[k]
+        tot["tiles"] += tiles_of(w, h)
+        grid.append(ps["grid_blocks"])
+    if own:
+        bs.close()
+    nt = tot["tiles"]
+    gr = phase_record(tot["ms_relabel"],
+                      1024 * (B_GR * min(tot["relabel_tiles"], nt) + B_COUNT * nt),
+                      MOVED_GR_VISIT * tot["relabel_tiles"] + MOVED_GR_TILE * nt,
+                      ncu_phase_traffic("gr", workload_name), peak,
+                      launches=len(groups), tile_visits=tot["relabel_tiles"], frontier_rounds=tot["relabel_rounds"],
+                      tiles=nt)
+    push = phase_record(tot["ms_push"], 1024 * B_PUSH * tot["push_tiles"], MOVED_PUSH_VISIT * tot["push_tiles"],
+                        ncu_phase_traffic("push", workload_name), peak,
+                        launches=len(groups), tile_visits=tot["push_tiles"], sweeps=tot["push_sweeps"],
+                        local_relabels=tot["push_local_relabels"], colour_phases=tot["push_phases"])
+    return {"global_relabel": gr, "push": push, "grid_blocks": max(grid),
+            "how": "gcfg_batch_phase_split: launch 1 = initialisation + the first exact global relabel + its count "
+                   "pass, launch 2 = the push rounds that follow (until the next global relabel), CUDA events "
+                   "per launch; alg = int32 accounting (global relabel 24 B/px once + count 8 B/px; push 48 B/px "
+                   "per visited pixel); moved = what the phase reads and writes in this layout (relabel: mask "
+                   "planes, halo lines, heights, border lines; push: the 24 KB tile in and out, halos, masks); "
+                   "traffic = ncu dram__bytes_read.sum + dram__bytes_write.sum of the same launches"}
+
+
+def profiled_roofline(gcfg, flush, run_once, Ws, Hs, batched, px, peak, peak_kind, workload_name):
+    """One profiled pass (per-kernel CUDA events on the launching stream):
+    the kernel with the largest device time and its algorithmic bytes."""
+    gcfg.profile_enable(True)
+    gcfg.profile_read()
+    flush.fill_(7)
+    recs = run_once()
+    prof = gcfg.profile_read()
+    gcfg.profile_enable(False)
+    dom = max(prof, key=lambda k: prof[k]["ms"])
+    tiles_total = tiles_of(Ws, Hs)
+    solve_bytes = 0
+    for j, r in enumerate(recs[:1] if batched else recs):
+        nt = tiles_total if batched else tiles_of(Ws[j:j + 1], Hs[j:j + 1])
+        solve_bytes += 1024 * (B_GR * min(r["gr_tiles"], nt * r["global_relabels"]) + B_PUSH * r["push_tiles"] +
+                               B_REACH * min(r["reach_tiles"], nt) + B_COUNT * nt * r["global_relabels"] +
+                               B_REACH * nt * r.get("closure_checks", 0))
+    alg = {"solve": solve_bytes, "build": B_BUILD * 1024 * tiles_total, "extract": B_EXTRACT * px,
+           "hist": 4 * px, "sigma": 3 * px}
+    launches_dom = max(prof[dom]["launches"], 1)
+    alg_bytes = alg.get(dom, 0)
+    achieved = alg_bytes / (prof[dom]["ms"] / 1e3) / 1e9 if prof[dom]["ms"] > 0 else 0.0
+    step_prof_ms = sum(v["ms"] for v in prof.values())
+    return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_source(peak_kind),
+            "traffic": ncu_traffic(dom, workload_name),
+            "alg_bytes_per_launch": alg_bytes / launches_dom,
+            "avg_launch_us": prof[dom]["ms"] / launches_dom * 1e3,
+            "share_of_step": prof[dom]["ms"] / step_prof_ms if step_prof_ms else None,
+            "kernels_ms": {k: round(v["ms"], 4) for k, v in prof.items() if v["launches"]}}, recs
+
+
+def plain_leg(torch, gcfg, name, steps, warmup, flush, stream, peak, peak_kind, cpu_budget=10.0, ref_budget=5.0):
+    """One single-image workload through the plain per-image solver
+    (gcfg_seg_run): images resident in HBM (value), the same through
+    gcfg_seg_run_host with pinned host buffers (e2e), the profiled roofline,
+    the two solver phases as separate launches, the oracle on one host thread
+    (cpu_baseline, with flow / S_min / S_max parity on every image) and the
+    reference's CUDA path on the same images."""
+    spec = workload(name)
+    rgb, scrib, offs, Ws, Hs, lams = make_inputs(spec)
+    views = image_views(rgb, scrib, offs, Ws, Hs)
+    n_img, px = len(Ws), int(scrib.size)
+    offs_l = [int(o) for o in offs]
+    d_rgb, d_scrib = torch.from_numpy(rgb).cuda(), torch.from_numpy(scrib).cuda()
+    d_smin = torch.empty(px, dtype=torch.uint8, device="cuda")
+    d_smax = torch.empty(px, dtype=torch.uint8, device="cuda")
+    h_rgb = torch.from_numpy(rgb).pin_memory().numpy()
+    h_scrib = torch.from_numpy(scrib).pin_memory().numpy()
+    h_smin = torch.empty(px, dtype=torch.uint8).pin_memory().numpy()
+    h_smax = torch.empty(px, dtype=torch.uint8).pin_memory().numpy()
+    seg = gcfg.Segmenter(int(Ws.max()), int(Hs.max()))
+    seg.set_stream(stream)
+
+    def step():
+        out = []
+        for i in range(n_img):
+            o, n = offs_l[i], int(Ws[i]) * int(Hs[i])
+            out.append(seg.run(d_rgb[3 * o:3 * (o + n)], d_scrib[o:o + n], int(Ws[i]), int(Hs[i]),
+                               float(lams[i]), d_smin[o:o + n], d_smax[o:o + n]))
+        return out
+
+    def step_host():
+        out = []
+        for i in range(n_img):
+            o, n = offs_l[i], int(Ws[i]) * int(Hs[i])
+            out.append(seg.run_host(h_rgb[3 * o:3 * (o + n)], h_scrib[o:o + n], int(Ws[i]), int(Hs[i]),
+                                    float(lams[i]), h_smin[o:o + n], h_smax[o:o + n]))
+        return out
+
+    for _ in range(warmup):
+        step()
+        step_host()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    res = None
+    for i in range(steps):
+        flush.fill_(i & 0xFF)
+        ev[i][0].record(stream)
+        res = step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    flows = np.array([r["flow"] for r in res], np.int64)
+    e2e_ms, res_h = [], None
+    for i in range(steps):
+        flush.fill_(i & 0xFF)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        res_h = step_host()
+        e2e_ms.append((time.perf_counter() - t) * 1e3)
+    e2e = float(np.mean(e2e_ms))
+    host_equal = bool(np.array_equal(flows, [r["flow"] for r in res_h]) and np.array_equal(h_smin, d_smin.cpu().numpy())
+                      and np.array_equal(h_smax, d_smax.cpu().numpy()))
+    roof, _ = profiled_roofline(gcfg, flush, step, Ws, Hs, False, px, peak, peak_kind, name)
+    roof["solve_phases"] = solve_phases(gcfg, stream, Ws, Hs, lams, d_rgb, d_scrib, offs, peak, name, False)
+    smin_all, smax_all = d_smin.cpu().numpy(), d_smax.cpu().numpy()
+    seg.close()
+    cpu_v, n_chk, secs, parity = cpu_baseline(views, lams, budget_s=cpu_budget, flows_gpu=flows,
+                                              smin_gpu=smin_all, smax_gpu=smax_all, offs=offs)
+    leg = {"desc": spec["desc"], "images": n_img, "pixels": px, "value": px / (ms / 1e3) / 1e6, "unit": UNIT,
+           "ms_per_step": ms, "steps": steps,
+           "e2e": {"value": px / (e2e / 1e3) / 1e6, "unit": UNIT, "ms_per_step": e2e,
+                   "h2d_bytes_per_step": 4 * px, "d2h_bytes_per_step": 2 * px,
+                   "api": "gcfg_seg_run_host per image, pinned host buffers, wall clock per step",
+                   "results_equal_device": host_equal},
+           "roofline": roof,
+           "solver": {k: res[0][k] for k in ("global_relabels", "closure_checks", "push_tiles", "gr_tiles",
+                                             "push_sweeps", "push_local_relabels")},
+           "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": 1, "kind": "port",
+                            "sample": f"{n_chk} solve(s) of the workload's images in {secs:.1f} s, oracle "
+                                      "Boykov-Kolmogorov, 1 thread"},
+           "parity": parity}
+    if ref_budget > 0:
+        leg["reference_cuda"] = reference_cuda_leg(views, lams, smax_all, offs, budget_s=ref_budget)
+    return leg
+
+
+def n8_leg(torch, gcfg, steps, warmup, peak, peak_kind, ref_budget=5.0):
     """8-neighbourhood graph (the reference's NEIGHBORHOOD == 8 build) at
     640x480: histogram t-links of a generated image, constant penalty 600 on
     all eight directions.  A step is GC_SetGraph8 + GC_Optimize8 (labels to
     the host) on device-resident t-links."""
-    import torch
-    import __graft_entry__ as ge
-    ge.build()
-    import gcfg
     import oracle as O
     import synth
     W, H, pen = 640, 480, 600
@@ -435,17 +730,16 @@ def run_n8(args, rank, world):
     gcfg.tlinks(d_rgb, d_scrib, dp, dn)
     gw = gcfg.GC_Init8(W, H, dp, dn, pen)
     label = torch.empty(W * H, dtype=torch.int32).pin_memory().numpy()
-    for _ in range(args.warmup):
+    d_smin = torch.empty(W * H, dtype=torch.uint8, device="cuda")
+    for _ in range(warmup):
         gcfg.GC_SetGraph8(gw)
         gcfg.GC_Optimize8(gw, label)
     stream = torch.cuda.current_stream()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     torch.cuda.synchronize()
     solve_ms = []
-    clocks = ClockSampler(torch.cuda.current_device())
-    clocks.start()
     l0 = gcfg.launch_count()
-    for i in range(args.steps):
+    for i in range(steps):
         ev[i][0].record(stream)
         gcfg.GC_SetGraph8(gw)
         r = gcfg.GC_Optimize8(gw, label)
@@ -453,8 +747,9 @@ def run_n8(args, rank, world):
         solve_ms.append(r["ms"])
     torch.cuda.synchronize()
     launches = gcfg.launch_count() - l0
-    clk = clocks.stop()
-    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    gcfg.GC_GetCuts8(gw, d_smin, None)
+    smin = d_smin.cpu().numpy().reshape(H, W)
     gcfg.GC_End8(gw)
     hdp, hdn = dp.cpu().numpy().reshape(H, W), dn.cpu().numpy().reshape(H, W)
     t = time.perf_counter()
@@ -472,44 +767,75 @@ def run_n8(args, rank, world):
     visits, rounds = r["push_tiles"], r["push_rounds"]
     alg = (r["global_relabels"] * n * (40 + 8) + visits * 256 * 80 + (rounds * tiles8 - visits) * 256 * 8 + n * 8)
     avg_solve_ms = sum(solve_ms) / len(solve_ms)
-    peak, peak_kind = load_peaks()
     achieved = alg / (avg_solve_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": "k8_solve", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak,
-                "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
-                else "of fallback 6.8 TB/s",
+                "frac": achieved / peak, "peak_source": peak_source(peak_kind),
                 "traffic": ncu_traffic("solve8", "n8_640x480"),
                 "alg_bytes_per_launch": alg, "avg_launch_us": avg_solve_ms * 1e3,
                 "note": "a 640x480 graph is about 15 MB in this layout and stays in L2; the solve is bound by "
                         "its grid barriers (one per tile or relabel round), not by HBM"}
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded in-repo generator; no dataset)",
-            "config": {"workload": "n8_640x480", "desc": "8-neighbourhood graph, 640x480, histogram t-links of a "
-                       "generated image, penalty 600 on all eight directions", "parallelism": f"replicas x{world}"},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 4 * W * H,
-                    "note": "labels to the host inside the timed step; t-links resident"},
-            "roofline": roofline, "clocks": clk, "gpu_launches": launches,
-            "solver": {"global_relabels": r["global_relabels"], "gr_rounds": r["gr_sweeps"],
-                       "tile_rounds": r["push_rounds"], "tile_visits": visits, "cut_rounds": r["cut_sweeps"]},
-            "cpu_baseline": {"value": W * H / cpu_s / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
-                             "sample": f"one solve of the same graph, oracle 8-connected push-relabel, {cpu_s:.2f} s"},
-            "parity": {"flow_equal_oracle": bool(r["flow"] == o["flow"]),
-                       "labels_equal_oracle": bool((label.reshape(H, W) == o["smax"]).all())}}
+    leg = {"desc": "8-neighbourhood graph, 640x480, histogram t-links of a generated image, penalty 600 on all "
+                   "eight directions", "pixels": n, "value": value, "unit": UNIT, "ms_per_step": ms, "steps": steps,
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 4 * W * H,
+                   "note": "labels to the host inside the timed step (GC_Optimize8); t-links resident"},
+           "roofline": roofline, "gpu_launches": launches,
+           "solver": {"global_relabels": r["global_relabels"], "gr_rounds": r["gr_sweeps"],
+                      "tile_rounds": r["push_rounds"], "tile_visits": visits, "cut_rounds": r["cut_sweeps"]},
+           "cpu_baseline": {"value": W * H / cpu_s / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
+                            "sample": f"one solve of the same graph, oracle 8-connected push-relabel, "
+                                      f"{cpu_s:.2f} s"},
+           "parity": {"flow_equal_oracle": bool(r["flow"] == o["flow"]),
+                      "smax_equal_oracle": bool((label.reshape(H, W) == o["smax"]).all()),
+                      "smin_equal_oracle": bool(np.array_equal(smin, o["smin"]))}}
     # the reference's own NEIGHBORHOOD 8 build of its kernels on the same GPU and graph
     import ref_cuda
-    why = ref_cuda.unavailable(8) or ("not run (--ref-cuda-budget 0)" if args.ref_cuda_budget <= 0 else None)
+    why = ref_cuda.unavailable(8) or ("not run (reference budget 0)" if ref_budget <= 0 else None)
     if why:
-        line["reference_cuda"] = {"unavailable": why}
+        leg["reference_cuda"] = {"unavailable": why}
     else:
         rr = [ref_cuda.solve8(hdp, hdn, penalty=pen, max_seconds=30.0) for _ in range(3)]
         best = min(x["ms_solve"] for x in rr)
-        line["reference_cuda"] = {
+        leg["reference_cuda"] = {
             "value": W * H / (best / 1e3) / 1e6, "unit": UNIT, "ms_per_image": best,
             "status": rr[-1]["status"], "iterations": rr[-1]["iterations"],
             "labels_equal": bool(np.array_equal(rr[-1]["label"], label.reshape(H, W))),
             "how": "the reference's kernels built with NEIGHBORHOOD 8 (GraphCutKernels.cu, sm_103a), launched in "
                    "GC_Optimize's order; best of 3 solves, wall clock of GC_SetGraph + GC_Optimize"}
+    return leg
+
+
+SINGLE_WORKLOADS = ("plain256", "plain1080", "plain4096")
+
+
+def workload_config(name, spec, world):
+    """The `config` object of a workload; both arms print the same one."""
+    if name == "n8_640x480":
+        return {"workload": name, "desc": "8-neighbourhood graph, 640x480, histogram t-links of a generated image, "
+                "penalty 600 on all eight directions", "parallelism": f"replicas x{world}"}
+    batched = spec["kind"] == "batch"
+    px = int(sum(W * H for (_, W, H, _, _) in spec["images"]))
+    return {"workload": name, "desc": spec["desc"], "images_per_step": len(spec["images"]),
+            "pixels_per_step": px, "mode": "batched" if batched else "per-image",
+            "l2": "GPU arm: flushed (256 MB write) before every step",
+            "parallelism": (f"shard by image x{world}" if batched else f"replicas x{world}")}
+
+
+def run_n8(args, rank, world):
+    import torch
+    import __graft_entry__ as ge
+    ge.build()
+    import gcfg
+    peak, peak_kind = load_peaks()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    leg = n8_leg(torch, gcfg, args.steps, args.warmup, peak, peak_kind,
+                 ref_budget=args.ref_cuda_budget)
+    clk = clocks.stop()
+    line = {"metric": METRIC, "value": leg["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": leg["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded in-repo generator; no dataset)",
+            "config": workload_config("n8_640x480", None, world), "clocks": clk}
+    line.update({k: v for k, v in leg.items() if k not in ("desc", "value", "unit", "ms_per_step", "steps")})
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
@@ -520,29 +846,42 @@ def run_reference_arm(args, spec, rank, world):
     if rank != 0:
         return 0
     import oracle as O
-    rgb, scrib, offs, Ws, Hs, lams = make_inputs(spec)
-    views = image_views(rgb, scrib, offs, Ws, Hs)
-    nthreads = os.cpu_count() or 1
-    reps = max(1, nthreads // len(views))
-    per_step = []
-    total_px = int(sum(s.size for _, s in views)) * reps
-    for i in range(args.warmup + args.steps):
-        t = time.perf_counter()
-        O.segment_batch(views * reps, list(lams) * reps, nthreads)
-        dt = time.perf_counter() - t
-        if i >= args.warmup:
-            per_step.append(dt)
-    secs = sum(per_step)
-    value = total_px * len(per_step) / secs / 1e6
+    if args.workload == "n8_640x480":
+        import synth
+        W, H, pen = 640, 480, 600
+        rgb, scrib = synth.generate(1, W, H, 7)
+        dp, dn = O.tlinks(rgb, scrib)
+        per_step = []
+        for i in range(args.warmup + args.steps):
+            t = time.perf_counter()
+            O.solve8(dp, dn, penalty=pen)
+            if i >= args.warmup:
+                per_step.append(time.perf_counter() - t)
+        value = W * H * len(per_step) / sum(per_step) / 1e6
+        cores, sample, total_px = 1, "one 640x480 8-connected solve per step, oracle push-relabel, 1 thread", W * H
+    else:
+        rgb, scrib, offs, Ws, Hs, lams = make_inputs(spec)
+        views = image_views(rgb, scrib, offs, Ws, Hs)
+        cores = os.cpu_count() or 1
+        reps = max(1, cores // len(views))
+        per_step = []
+        total_px = int(sum(s.size for _, s in views)) * reps
+        for i in range(args.warmup + args.steps):
+            t = time.perf_counter()
+            O.segment_batch(views * reps, list(lams) * reps, cores)
+            dt = time.perf_counter() - t
+            if i >= args.warmup:
+                per_step.append(dt)
+        value = total_px * len(per_step) / sum(per_step) / 1e6
+        sample = (f"{len(views)} image(s) x {reps} per step, oracle Boykov-Kolmogorov, one image per host thread; "
+                  "the reference has no CPU solver (its CUDA path is timed in the reference_cuda leg of the "
+                  "default arm)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / len(per_step) * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(per_step) / len(per_step) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-            "data": "synthetic (seeded in-repo generator)",
-            "config": {"workload": args.workload, "desc": spec["desc"]},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                             "sample": f"{len(views)} image(s) x {reps} per step, oracle Boykov-Kolmogorov, "
-                                       "one image per host thread; the reference has no CPU solver (its CUDA "
-                                       "path is timed in the reference_cuda leg of the default arm)"},
+            "data": "synthetic (seeded in-repo generator; no dataset)",
+            "config": workload_config(args.workload, spec, world),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -558,6 +897,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-plain", action="store_true", help="skip the per-image comparison leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--no-single", action="store_true", help="skip the single-image legs")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default solver settings)")
     ap.add_argument("--no-graph", action="store_true", help="run the batch without CUDA graph replay")
     ap.add_argument("--solver-params", default=None,
@@ -569,13 +909,13 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_info()
-    if args.workload == "n8_640x480" and args.impl == "ours":
+    spec = None if args.workload == "n8_640x480" else workload(args.workload, rank)
+    if args.impl == "reference":
+        return run_reference_arm(args, spec, rank, world)
+    if args.workload == "n8_640x480":
         import torch
         torch.cuda.set_device(local)
         return run_n8(args, rank, world)
-    spec = workload(args.workload, rank)
-    if args.impl == "reference":
-        return run_reference_arm(args, spec, rank, world)
 
     import torch
     import __graft_entry__ as ge
@@ -607,6 +947,7 @@ def main():
     h_smin = torch.empty(px_per_step, dtype=torch.uint8).pin_memory().numpy()
     h_smax = torch.empty(px_per_step, dtype=torch.uint8).pin_memory().numpy()
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    peak, peak_kind = load_peaks()
 
     batched = spec["kind"] == "batch"
     bs = gcfg.BatchSolver(n_img, px_per_step)
@@ -706,6 +1047,7 @@ def main():
     barrier()
     launches = gcfg.launch_count() - l0
     clk = clocks.stop()
+    smin_dev, smax_dev = d_smin.cpu().numpy(), d_smax.cpu().numpy()
 
     # ---- e2e through the host entry point ----
     barrier()
@@ -724,6 +1066,8 @@ def main():
         barrier()
         e2e_total, flows_p = host_pipelined(args.steps)
         barrier()
+    cuts_host_equal = bool(np.array_equal(h_out[(args.steps - 1) % 2][0] if batched else h_smin, smin_dev) and
+                           np.array_equal(h_out[(args.steps - 1) % 2][1] if batched else h_smax, smax_dev))
 
     # ---- the same images, plain per-image path (batched workload only) ----
     plain = None
@@ -732,7 +1076,9 @@ def main():
         plain_ms, (pflows, _) = timed(step_plain, psteps)
         plain = {"value": px_per_step * psteps / (plain_ms / 1e3) / 1e6, "unit": UNIT,
                  "ms_per_step": plain_ms / psteps, "steps": psteps,
-                 "flows_equal_batched": bool(np.array_equal(pflows, flows))}
+                 "flows_equal_batched": bool(np.array_equal(pflows, flows)),
+                 "cuts_equal_batched": bool(np.array_equal(d_smin.cpu().numpy(), smin_dev) and
+                                            np.array_equal(d_smax.cpu().numpy(), smax_dev))}
 
     import shard
     total_ms = shard.max_over_ranks(total_ms, device="cuda")
@@ -741,67 +1087,40 @@ def main():
     value = world * px_per_step * args.steps / (total_ms / 1e3) / 1e6
     e2e_value = world * px_per_step * args.steps / (e2e_total / 1e3) / 1e6
 
-    # ---- roofline: one profiled step ----
-    gcfg.profile_enable(True)
-    gcfg.profile_read()
-    flush.fill_(7)
-    if batched:
-        pflows2, pres = bs.run(Ws, Hs, lams, d_rgb, d_scrib, d_smin, d_smax, results=True)
-    else:
-        pflows2, pres = step()
-    prof = gcfg.profile_read()
-    gcfg.profile_enable(False)
-    dom = max(prof, key=lambda k: prof[k]["ms"])
-    peak, peak_kind = load_peaks()
-    tiles_total = int(sum(((int(w) + 31) // 32) * ((int(h) + 31) // 32) for w, h in zip(Ws, Hs)))
-    recs = pres if isinstance(pres, list) else [pres]
-    solve_bytes = 0
-    for j, r in enumerate(recs[:1] if batched else recs):
-        nt = tiles_total if batched else ((int(Ws[j]) + 31) // 32) * ((int(Hs[j]) + 31) // 32)
-        solve_bytes += 1024 * (B_GR * min(r["gr_tiles"], nt * r["global_relabels"]) + B_PUSH * r["push_tiles"] +
-                               B_REACH * min(r["reach_tiles"], nt) + B_COUNT * nt * r["global_relabels"] +
-                               B_REACH * nt * r.get("closure_checks", 0))
-    alg = {"solve": solve_bytes, "build": B_BUILD * 1024 * tiles_total, "extract": B_EXTRACT * px_per_step,
-           "hist": 4 * px_per_step, "sigma": 3 * px_per_step}
-    launches_dom = max(prof[dom]["launches"], 1)
-    alg_bytes = alg.get(dom, 0)
-    achieved = alg_bytes / (prof[dom]["ms"] / 1e3) / 1e9 if prof[dom]["ms"] > 0 else 0.0
-    step_prof_ms = sum(v["ms"] for v in prof.values())
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak,
-                "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
-                else "of fallback 6.8 TB/s",
-                "traffic": ncu_traffic(dom, args.workload),
-                "alg_bytes_per_launch": alg_bytes / launches_dom,
-                "avg_launch_us": prof[dom]["ms"] / launches_dom * 1e3,
-                "share_of_step": prof[dom]["ms"] / step_prof_ms if step_prof_ms else None,
-                "kernels_ms": {k: round(v["ms"], 4) for k, v in prof.items() if v["launches"]}}
-    # the solver's two main phases on their own (device timers of the phases; same byte accounting)
+    # ---- roofline: one profiled step, then the two solver phases as separate launches ----
+    def run_once():
+        if batched:
+            return bs.run(Ws, Hs, lams, d_rgb, d_scrib, d_smin, d_smax, results=True)[1]
+        return step_plain()[1]
+
+    roofline, recs = profiled_roofline(gcfg, flush, run_once, Ws, Hs, batched, px_per_step, peak, peak_kind,
+                                       args.workload)
+    roofline["solve_phases"] = solve_phases(gcfg, stream, Ws, Hs, lams, d_rgb, d_scrib, offs, peak, args.workload,
+                                            batched, bs=bs if batched else None)
+    # in-solve phase timers of the profiled full solve (the same byte accounting)
     r_ph = recs[0]
-    nt0 = tiles_total if batched else ((int(Ws[0]) + 31) // 32) * ((int(Hs[0]) + 31) // 32)
-    ph = {}
+    nt0 = tiles_of(Ws, Hs) if batched else tiles_of(Ws[:1], Hs[:1])
+    inside = {}
     for name, nbytes, ms in (("global_relabel", 1024 * (B_GR * min(r_ph["gr_tiles"], nt0 * r_ph["global_relabels"]) +
                                                      B_REACH * nt0 * r_ph.get("closure_checks", 0)),
                               r_ph["t_global_relabel_ms"]),
                              ("push", 1024 * B_PUSH * r_ph["push_tiles"], r_ph["t_push_ms"])):
         if ms > 0:
             gbs = nbytes / (ms / 1e3) / 1e9
-            ph[name] = {"achieved": round(gbs, 1), "frac": round(gbs / peak, 4), "ms": ms, "bytes": nbytes}
-    ph["note"] = ("int32-layout bytes per unit as for the whole kernel; the global relabel and the termination "
-                  "check read 1-bit residual planes (0.75 B/px) instead of the int32 capacities and write 4-byte "
-                  "heights, so their figure can pass the HBM peak")
-    roofline["solve_phases"] = ph
+            inside[name] = {"achieved_alg_gbs": round(gbs, 1), "frac_alg": round(gbs / peak, 4), "ms": ms,
+                            "alg_bytes": nbytes}
+    inside["note"] = ("phase timers inside the whole solve (every global relabel and termination check, every push "
+                      "round), int32-layout bytes")
+    roofline["solve_phases"]["inside_full_solve"] = inside
 
     r0 = recs[0]
+    config = workload_config(args.workload, spec, world)
+    config.update(tuning=tuning, cuda_graph=bs.graph_info() if batched else None)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded in-repo generator; no dataset)",
-            "config": {"workload": args.workload, "desc": spec["desc"], "images_per_step": n_img,
-                       "pixels_per_step": px_per_step, "mode": "batched" if batched else "per-image",
-                       "l2": "flushed (256 MB write) before every step",
-                       "parallelism": (f"shard by image x{world}" if batched else f"replicas x{world}"),
-                       "tuning": tuning, "cuda_graph": bs.graph_info() if batched else None},
+            "config": config,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 4 * px_per_step,
                     "d2h_bytes_per_step": 2 * px_per_step, "ms_per_step": e2e_total / args.steps,
                     "api": ("gcfg_batch_submit_host/gcfg_batch_wait, 2 batches in flight, wall clock over "
@@ -825,16 +1144,31 @@ def main():
     line["flows_host_equal_device"] = bool(np.array_equal(np.asarray(flows_h), np.asarray(flows)) and
                                            (flows_p is None or np.array_equal(np.asarray(flows_p),
                                                                               np.asarray(flows))))
+    line["cuts_host_equal_device"] = cuts_host_equal
+    bs.close()
+    seg.close()
     if rank == 0:
-        cpu_v, n_chk, secs, cflows = cpu_baseline(views, lams, budget_s=args.cpu_budget)
-        ok = all(int(flows[i]) == f for i, f in cflows)
+        cpu_v, n_chk, secs, parity = cpu_baseline(views, lams, budget_s=args.cpu_budget, flows_gpu=flows,
+                                                  smin_gpu=smin_dev, smax_gpu=smax_dev, offs=offs)
         line["cpu_baseline"] = {"value": cpu_v, "unit": UNIT, "cores": 1, "kind": "port",
                                 "sample": f"{n_chk} image(s) of the workload in {secs:.1f} s, oracle "
                                           "Boykov-Kolmogorov, 1 thread"}
-        line["parity"] = {"flows_equal_oracle": ok, "images_checked": len(set(i for i, _ in cflows))}
+        line["parity"] = parity
         if args.ref_cuda_budget > 0:
-            line["reference_cuda"] = reference_cuda_leg(views, lams, d_smax.cpu().numpy(), offs,
+            line["reference_cuda"] = reference_cuda_leg(views, lams, smax_dev, offs,
                                                         budget_s=args.ref_cuda_budget)
+        if batched and not args.no_single:
+            legs = {}
+            sclk = ClockSampler(local)
+            sclk.start()
+            for name in SINGLE_WORKLOADS:
+                legs[name] = plain_leg(torch, gcfg, name, max(3, min(args.steps, 10)), args.warmup, flush, stream,
+                                       peak, peak_kind, cpu_budget=min(args.cpu_budget, 5.0),
+                                       ref_budget=min(args.ref_cuda_budget, 3.0))
+            legs["n8_640x480"] = n8_leg(torch, gcfg, max(3, min(args.steps, 10)), args.warmup, peak, peak_kind,
+                                        ref_budget=min(args.ref_cuda_budget, 3.0))
+            legs["clocks"] = sclk.stop()
+            line["single_image"] = legs
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -43,9 +43,9 @@ __global__ void k_sel_square(uint8_t *map, int W, int H, int x0, int y0, int siz
     map[(long long)y * W + x] = (uint8_t)cls;
 }
 
-// drawSelection: class-1 pixels become (0, 0, 255) as in K_DrawMap
-// (DataTermKernels.cu:96-113); class-2 pixels (no counterpart) become
-// (255, 0, 0).
+// drawSelection: the pixels whose selection-map entry is 1 become
+// (0, 0, 255), every other pixel keeps its colour, as K_DrawMap does
+// (DataTermKernels.cu:96-113; a map set from labels marks label 1).
 __global__ void k_draw_sel(const uint8_t *__restrict__ map, const uint8_t *__restrict__ img,
                            uint8_t *__restrict__ out, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -55,10 +55,6 @@ __global__ void k_draw_sel(const uint8_t *__restrict__ map, const uint8_t *__res
             c0 = 0;
             c1 = 0;
             c2 = 255;
-        } else if (m == 2) {
-            c0 = 255;
-            c1 = 0;
-            c2 = 0;
         }
         out[3 * i + 0] = c0;
         out[3 * i + 1] = c1;

@@ -26,6 +26,7 @@
 //   * Everything above runs in one cooperative persistent kernel; phases are
 //     separated by a grid barrier whose spin is bounded (on timeout the
 //     kernel records an error and returns).
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -987,23 +988,32 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
 
     if (threadIdx.x < ST_N) st[threadIdx.x] = 0;
     __syncthreads();
+    // the block's statistics reach the control block once, when it leaves
+    auto flush_stats = [&]() {
+        __syncthreads();
+        if (threadIdx.x < ST_N && st[threadIdx.x]) atomicAdd(ctl_stat(ctl, threadIdx.x), st[threadIdx.x]);
+    };
     PhaseClock clk;
     clk.start();
-    // fresh de-duplication marks and reach bits for this solve
     const int nt = batch_ntiles(b);
-    for (int k = gtid; k < nt; k += nthreads) {
-        const int t = batch_tile(b, k);
-        b.mark_push[t] = -1;
-        b.mark_gr[t] = -1;
+    if (prm.phase != 2) {
+        // fresh de-duplication marks and reach bits for this solve
+        for (int k = gtid; k < nt; k += nthreads) {
+            const int t = batch_tile(b, k);
+            b.mark_push[t] = -1;
+            b.mark_gr[t] = -1;
+        }
+        for (size_t i = gtid; i < (size_t)nt * 32; i += nthreads)
+            b.reach[(size_t)batch_tile(b, (int)(i >> 5)) * 32 + (i & 31)] = 0;
+        if (!grid_sync(b, 0)) return;
+        clk.charge(&ctl->t_init);
     }
-    for (size_t i = gtid; i < (size_t)nt * 32; i += nthreads) b.reach[(size_t)batch_tile(b, (int)(i >> 5)) * 32 + (i & 31)] = 0;
-    if (!grid_sync(b, 0)) return;
-    clk.charge(&ctl->t_init);
 
     int P = 0;  // push phase counter (even at the start of every outer iteration)
     int G = 0;  // global relabel round counter (tags of the tile frontier)
     bool finished = false;
     for (int outer = 0; outer < prm.max_outer; ++outer) {
+        if (prm.phase == 2) goto push_rounds;  // the phase-1 launch did the relabel and the count
         if (outer > 0) {
             const int rc = closure_check(b, prm, G);
             if (rc < 0) return;
@@ -1116,16 +1126,23 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
             ctl->global_relabels++;
             ctl->outer_iters = outer + 1;
         }
-        const unsigned long long total = *(volatile unsigned long long *)&ctl->total_active;
-        for (int k = gtid; k < batch_nimg(b); k += nthreads) {
-            const int i = batch_img(b, k);
-            if (!b.ist[i].done && *(volatile unsigned long long *)&b.ist[i].active == 0) b.ist[i].done = 1;
+        if (prm.phase == 1) {
+            flush_stats();
+            return;
         }
-        if (total == 0) {
-            finished = true;
-            break;
+        {
+            const unsigned long long total = *(volatile unsigned long long *)&ctl->total_active;
+            for (int k = gtid; k < batch_nimg(b); k += nthreads) {
+                const int i = batch_img(b, k);
+                if (!b.ist[i].done && *(volatile unsigned long long *)&b.ist[i].active == 0) b.ist[i].done = 1;
+            }
+            if (total == 0) {
+                finished = true;
+                break;
+            }
         }
         // ------------------------ checkerboard push rounds ------------------------
+    push_rounds:
         int last = P;
         for (int r = 0; r < prm.push_rounds; ++r) {
             bool more = true;
@@ -1160,6 +1177,10 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
         }
         P = (last + 3) & ~1;
         clk.charge(&ctl->t_push);
+        if (prm.phase == 2) {
+            flush_stats();
+            return;
+        }
     }
     if (!finished) {
         if (gtid == 0) set_error(b, ERRC_OUTER);
@@ -1186,8 +1207,7 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
         if (gtid == 0) ctl->reach_rounds++;
     }
     clk.charge(&ctl->t_reach);
-    __syncthreads();
-    if (threadIdx.x < ST_N && st[threadIdx.x]) atomicAdd(ctl_stat(ctl, threadIdx.x), st[threadIdx.x]);
+    flush_stats();
 }
 
 // ---------------------------------------------------------------------------
@@ -1280,17 +1300,25 @@ __global__ void __launch_bounds__(TILE_THREADS) k_extract(Batch b, uint8_t *smin
 namespace gcfg {
 
 int solve_grid_blocks(int n_tiles, int max_grid) {
-    static int cached = 0;
-    if (!cached) {
-        int dev = 0, sms = 0, per_sm = 0;
-        cudaGetDevice(&dev);
+    // co-resident blocks of k_solve on the current device, computed once per
+    // device ordinal; several host threads (the server's lanes) may race to
+    // fill an entry, and they all store the same value
+    constexpr int MAX_DEV = 64;
+    static std::atomic<int> cached[MAX_DEV];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const bool slot = dev >= 0 && dev < MAX_DEV;
+    int full = slot ? cached[dev].load(std::memory_order_relaxed) : 0;
+    if (!full) {
+        int sms = 0, per_sm = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve, TILE_THREADS, 0);
-        cached = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+        full = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+        if (slot) cached[dev].store(full, std::memory_order_relaxed);
     }
     // half the tiles run in a push phase; more blocks than that only make
     // the grid barrier slower
-    int cap = cached;
+    int cap = full;
     if (max_grid > 0 && max_grid < cap) cap = max_grid;
     const int want = (n_tiles + 1) / 2;
     return want < 1 ? 1 : (want < cap ? want : cap);

@@ -112,6 +112,14 @@ struct SolveParams {
     int bfs_first;     // exact local relabel at the start of every tile visit
     int max_rounds;    // cap on BFS rounds of one global relabel / reach pass
     int push_only;     // 1: sweeps only push; heights change only by exact local relabels
+    // Diagnostic split of one solve into two launches, so that a profiler
+    // sees the two main phases as separate kernels.  0: the whole solve.
+    // 1: initialisation, the first exact global relabel and its count pass,
+    // then return (the work queues of the first push round stay in the
+    // control block).  2: continue from the state a phase-1 launch left (the
+    // control block not cleared in between): the push rounds of the first
+    // outer iteration, then return.  A split leaves the solve unfinished.
+    int phase;
 };
 
 // Default solver settings of every entry point (before any tuning): 2 push
@@ -120,7 +128,7 @@ struct SolveParams {
 // the 256-image batch, these are at or near the fastest of the settings tried
 // for every case (4 rounds with 64 sweeps and a local relabel every 16 sweeps
 // took up to 2.9x longer on the 1920x1080 image with lambda 200).
-constexpr SolveParams kDefaultSolveParams{64, 2, 24, 4, 0, 1 << 20, 0};
+constexpr SolveParams kDefaultSolveParams{64, 2, 24, 4, 0, 1 << 20, 0, 0};
 
 __host__ __device__ __forceinline__ int batch_ntiles(const Batch &b) { return b.tlist ? b.n_tlist : b.n_tiles; }
 __device__ __forceinline__ int batch_tile(const Batch &b, int k) { return b.tlist ? __ldg(b.tlist + k) : k; }

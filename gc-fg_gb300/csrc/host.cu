@@ -1341,6 +1341,53 @@ gcfg_status gcfg_batch_wait(gcfg_batch *b, int64_t ticket, int64_t *h_flows, gcf
     return batch_wait(b->e, ticket, h_flows, h_res);
 }
 
+gcfg_status gcfg_batch_phase_split(gcfg_batch *b, int n, const int *widths, const int *heights,
+                                   const double *lambdas, const uint8_t *d_rgb, const uint8_t *d_scrib,
+                                   gcfg_phase_split *out) {
+    if (!b || n < 1 || !widths || !heights || !lambdas || !d_rgb || !d_scrib || !out) return GCFG_ERR_INVALID;
+    Engine &e = b->e;
+    if (e.in_flight()) return GCFG_ERR_STATE;
+    memset(out, 0, sizeof(*out));
+    GCFG_TRY(e.layout(n, widths, heights, lambdas, true, false));
+    GCFG_TRY(e.build_images(d_rgb, d_scrib));
+    cudaEvent_t ev[4] = {};
+    for (auto &x : ev) GCFG_CK(cudaEventCreate(&x));
+    gcfg_status rc = GCFG_OK;
+    Ctl c1;
+    SolveParams p = e.prm;
+    do {
+        if (cudaMemsetAsync(e.d_ctl, 0, sizeof(Ctl), e.st) != cudaSuccess) { rc = GCFG_ERR_CUDA; break; }
+        p.phase = 1;
+        cudaEventRecord(ev[0], e.st);
+        if ((rc = launch_solve(e.batch(), p, e.n_tiles, e.st, e.max_grid)) != GCFG_OK) break;
+        cudaEventRecord(ev[1], e.st);
+        if ((rc = e.fetch()) != GCFG_OK) break;
+        c1 = *e.h_ctl;
+        if (c1.err) { rc = GCFG_ERR_NOT_CONVERGED; break; }
+        out->grid_blocks = solve_grid_blocks(e.n_tiles, e.max_grid);
+        out->relabel_tiles = (int64_t)c1.gr_tiles;
+        out->relabel_rounds = c1.gr_rounds;
+        out->active_pixels = (int64_t)c1.total_active;
+        out->push_queue = c1.size[L_PUSH0] + c1.size[L_PUSH1];
+        cudaEventElapsedTime(&out->ms_relabel, ev[0], ev[1]);
+        if (c1.total_active == 0) break;  // nothing to push: the solve is over after the relabel
+        p.phase = 2;  // the control block keeps the first push round's queues
+        cudaEventRecord(ev[2], e.st);
+        if ((rc = launch_solve(e.batch(), p, e.n_tiles, e.st, e.max_grid)) != GCFG_OK) break;
+        cudaEventRecord(ev[3], e.st);
+        if ((rc = e.fetch()) != GCFG_OK) break;
+        const Ctl &c2 = *e.h_ctl;
+        if (c2.err) { rc = GCFG_ERR_NOT_CONVERGED; break; }
+        out->push_tiles = (int64_t)(c2.push_tiles - c1.push_tiles);
+        out->push_sweeps = (int64_t)(c2.push_sweeps - c1.push_sweeps);
+        out->push_local_relabels = (int64_t)(c2.push_bfs - c1.push_bfs);
+        out->push_phases = c2.push_phases - c1.push_phases;
+        cudaEventElapsedTime(&out->ms_push, ev[2], ev[3]);
+    } while (false);
+    for (auto &x : ev) cudaEventDestroy(x);
+    return rc;
+}
+
 gcfg_status gcfg_batch_destroy(gcfg_batch *b) {
     if (!b) return GCFG_ERR_INVALID;
     delete b;

@@ -19,11 +19,12 @@
 //     that must start from zero are cleared by each call;
 //   * two calls whose GPU work overlaps (e.g. on two streams) race on the
 //     array: serialise them;
-//   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture begins.
-#include <mutex>
-
+//   * every call looks up the array's device address on the current device
+//     (cudaGetSymbolAddress, which allocates nothing), so a context that was
+//     reset or recreated since the last call never receives a stale address;
+//   * the call synchronises its stream twice (it reads back the capacity
+//     check after the build and the flow after the solve) and returns after
+//     the solve has finished.
 #include "engine.cuh"
 
 namespace gcfg {
@@ -58,22 +59,14 @@ static_assert(NEEDED <= GCFG_NOALLOC_SCRATCH_BYTES, "scratch array too small for
 // cudaGetSymbolAddress, never an address the GPU can use.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[GCFG_NOALLOC_SCRATCH_BYTES];
 
-constexpr int MAX_DEVICES = 64;
-std::mutex g_mu;
-unsigned char *g_dev_addr[MAX_DEVICES] = {};
-
-// Device address of the array on the current device (looked up once).
+// Device address of the array in the current device's context.  Looked up
+// on every call, not cached: after cudaDeviceReset or a recreated primary
+// context the module is loaded again and the array may move.
 gcfg_status scratch_address(unsigned char **out) {
-    int dev = 0;
-    GCFG_CK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= MAX_DEVICES) return GCFG_ERR_CUDA;
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_dev_addr[dev]) {
-        void *p = nullptr;
-        GCFG_CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        g_dev_addr[dev] = static_cast<unsigned char *>(p);
-    }
-    *out = g_dev_addr[dev];
+    void *p = nullptr;
+    GCFG_CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    if (!p) return GCFG_ERR_CUDA;
+    *out = static_cast<unsigned char *>(p);
     return GCFG_OK;
 }
 

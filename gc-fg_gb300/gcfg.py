@@ -40,7 +40,7 @@ EXPORTS = [
     "gcfg_batch_set_params", "gcfg_batch_run", "gcfg_batch_run_host", "gcfg_batch_submit_host",
     "gcfg_batch_wait", "gcfg_batch_destroy",
     "gcfg_solve_noalloc", "gcfg_batch_set_graph", "gcfg_batch_graph_info", "gcfg_batch_autotune",
-    "gcfg_batch_set_solver",
+    "gcfg_batch_set_solver", "gcfg_batch_phase_split",
     "gcfg_init8", "gcfg_set_dataterms8", "gcfg_set_edges8", "gcfg_set_penalty8", "gcfg_set_graph8",
     "gcfg_optimize8", "gcfg_get_cuts8", "gcfg_end8", "gcfg_set_stream8", "gcfg_set_schedule8",
 ]
@@ -80,6 +80,16 @@ class Tuning(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+
+
+class PhaseSplit(C.Structure):
+    _fields_ = [("ms_relabel", C.c_float), ("ms_push", C.c_float), ("relabel_tiles", C.c_int64),
+                ("active_pixels", C.c_int64), ("push_tiles", C.c_int64), ("push_sweeps", C.c_int64),
+                ("push_local_relabels", C.c_int64), ("relabel_rounds", C.c_int32), ("push_phases", C.c_int32),
+                ("push_queue", C.c_int32), ("grid_blocks", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class ProfEntry(C.Structure):
@@ -134,6 +144,7 @@ def load(path: str = LIB_PATH):
                                       C.POINTER(C.c_int64)]),
         "gcfg_batch_autotune": (S, [P, I, P, P, P, P, P, I, C.POINTER(Tuning)]),
         "gcfg_batch_set_solver": (S, [P, C.POINTER(Tuning)]),
+        "gcfg_batch_phase_split": (S, [P, I, P, P, P, P, P, C.POINTER(PhaseSplit)]),
         "gcfg_init8": (S, [I, I, P, P, C.c_int32, P, P, P, P, P, P, P, P, C.POINTER(P)]),
         "gcfg_set_dataterms8": (S, [P, P, P]),
         "gcfg_set_edges8": (S, [P, P, P, P, P, P, P, P, P]),
@@ -396,6 +407,16 @@ class BatchSolver:
         _check(load().gcfg_batch_autotune(self.handle, len(w), _ptr(w), _ptr(h), _ptr(lam), _ptr(d_rgb),
                                           _ptr(d_scrib), int(reps), C.byref(t)), "gcfg_batch_autotune")
         return t.as_dict()
+
+    def phase_split(self, widths, heights, lambdas, d_rgb, d_scrib) -> dict:
+        """Diagnostic (gcfg_batch_phase_split): the first global relabel and the
+        push rounds after it as two separate solver launches, with their device
+        times and work counters.  Leaves the solve unfinished."""
+        w, h, lam = self._arrays(widths, heights, lambdas)
+        out = PhaseSplit()
+        _check(load().gcfg_batch_phase_split(self.handle, len(w), _ptr(w), _ptr(h), _ptr(lam), _ptr(d_rgb),
+                                             _ptr(d_scrib), C.byref(out)), "gcfg_batch_phase_split")
+        return out.as_dict()
 
     @staticmethod
     def _arrays(widths, heights, lambdas):

@@ -223,8 +223,9 @@ int32_t *gcfg_dt_neg(gcfg_dataterm *dt);
 uint8_t *gcfg_dt_image(gcfg_dataterm *dt);
 uint8_t *gcfg_dt_selection(gcfg_dataterm *dt);
 /* drawSelection (DataTerm.cpp:155): h_in becomes the current image; h_out
- * receives it with class-1 pixels set to (0, 0, 255) as in the reference and
- * class-2 pixels set to (255, 0, 0). */
+ * receives it with the pixels whose selection-map entry is 1 set to
+ * (0, 0, 255), every other pixel unchanged, as K_DrawMap does
+ * (DataTermKernels.cu:96-113). */
 gcfg_status gcfg_dt_draw_selection(gcfg_dataterm *dt, const uint8_t *h_in, uint8_t *h_out);
 /* Choose the colour model.  GCFG_DT_KDE is the reference's own data term: a
  * kernel density over the 256^3 colour cube (64 MB, allocated on first use)
@@ -349,6 +350,32 @@ gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const i
                                 const double *lambdas, const uint8_t *d_rgb, const uint8_t *d_scrib,
                                 int reps, gcfg_tuning *out);
 
+/* Diagnostic: the batch's data term and build, then the solver's two main
+ * phases as two separate launches of the persistent solver kernel, so that a
+ * profiler (or the events below) sees each on its own: launch 1 = the first
+ * exact global relabel with its count pass (the reference's InitGlobalRelabel
+ * + GlobalRelabel, GraphCutKernels.cu:757-875), launch 2 = the push rounds
+ * that follow it (WavePush + Relabel, GraphCutKernels.cu:433-724).  The solve
+ * is left unfinished (no cut); run the batch again for results.  Current
+ * solver settings of the handle apply. */
+typedef struct {
+    float ms_relabel;             /* device time of launch 1 */
+    float ms_push;                /* device time of launch 2 (0 when nothing was active) */
+    int64_t relabel_tiles;        /* global-relabel tile visits of launch 1 */
+    int64_t active_pixels;        /* pixels with excess and finite height after the relabel */
+    int64_t push_tiles;           /* push tile visits of launch 2 */
+    int64_t push_sweeps;          /* push/relabel sweeps of those visits */
+    int64_t push_local_relabels;  /* exact local relabels of those visits */
+    int32_t relabel_rounds;       /* tile-frontier rounds of the relabel after its first */
+    int32_t push_phases;          /* checkerboard colour phases of launch 2 */
+    int32_t push_queue;           /* tiles queued for the first two colour phases */
+    int32_t grid_blocks;          /* blocks of each launch */
+} gcfg_phase_split;
+
+gcfg_status gcfg_batch_phase_split(gcfg_batch *b, int n, const int *widths, const int *heights,
+                                   const double *lambdas, const uint8_t *d_rgb, const uint8_t *d_scrib,
+                                   gcfg_phase_split *out);
+
 /* ---------------- serving (continuous batching, resident images) ---------------- */
 
 /* A server keeps every admitted image resident on the device (pixels,
@@ -442,11 +469,13 @@ double gcfg_serve_now(void);
  * 800x800 pixels), else GCFG_ERR_TOO_LARGE before any GPU work.
  * All calls share the array and it keeps the last call's contents (each call
  * clears what must start at zero); calls whose GPU work overlaps, e.g. on two
- * streams, race on it and must be serialised.  The first call on a device
- * looks up the array's device address with that device current
- * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * streams, race on it and must be serialised.  Every call looks up the
+ * array's device address on the current device (cudaGetSymbolAddress, which
+ * allocates nothing).
  * stream: cudaStream_t as void* (NULL = legacy default stream).  The call
- * returns after the solve has finished. */
+ * synchronises that stream twice (after the build, to read the capacity
+ * check, and after the solve, to read the flow) and returns after the solve
+ * has finished. */
 gcfg_status gcfg_solve_noalloc(int w, int h, const int32_t *d_dp, const int32_t *d_dn, int32_t penalty,
                                const int32_t *d_up, const int32_t *d_down, const int32_t *d_left,
                                const int32_t *d_right, int32_t *d_label, int64_t *h_flow,

@@ -21,6 +21,7 @@ SRC = os.path.join(HERE, "refgpu", "ref_gpu.cpp")
 LIB_PATH = os.path.join(HERE, "librefgpu.so")
 CUBIN = os.path.join(HERE, "_ref", "gc_ref_kernels.cubin")
 CUBIN8 = os.path.join(HERE, "_ref", "gc_ref_kernels8.cubin")  # the NEIGHBORHOOD 8 build
+CUBIN_DT = os.path.join(HERE, "_ref", "gc_ref_dt_kernels.cubin")  # the data-term kernels
 
 STATUS = {0: "ok", 1: "invalid", 2: "cuda error", 3: "iteration or time cap reached", 4: "kernels not loaded"}
 
@@ -46,8 +47,9 @@ def build(force: bool = False) -> str:
 
 
 def unavailable(neighborhood: int = 4) -> str | None:
-    """None when the reference's CUDA path can run here, else why not."""
-    path = CUBIN8 if neighborhood == 8 else CUBIN
+    """None when the reference's CUDA path can run here, else why not
+    (neighborhood 4 or 8: the solver's kernels; 0: the data-term kernels)."""
+    path = CUBIN8 if neighborhood == 8 else CUBIN_DT if neighborhood == 0 else CUBIN
     if not os.path.exists(path):
         return (f"the reference's kernels were not compiled (oracle/_ref/{os.path.basename(path)} is built "
                 "from the reference checkout)")
@@ -73,9 +75,13 @@ def lib(neighborhood: int = 4):
                                    C.POINTER(Stats)]
         L.refgpu_solve8.argtypes = [C.c_int, C.c_int, P, P, C.c_int, P, P, C.c_longlong, C.c_double,
                                     C.POINTER(Stats)]
+        L.refgpu_load_dt.argtypes = [C.c_char_p]
+        L.refgpu_kde.argtypes = [C.c_int, C.c_int, P, C.c_int, C.c_int, P, P, P, P, P]
+        L.refgpu_draw.argtypes = [C.c_int, C.c_int, P, P, P]
         _lib = L
     if neighborhood not in _loaded:
-        rc = (_lib.refgpu_load8(CUBIN8.encode()) if neighborhood == 8 else _lib.refgpu_load(CUBIN.encode()))
+        rc = (_lib.refgpu_load8(CUBIN8.encode()) if neighborhood == 8 else
+              _lib.refgpu_load_dt(CUBIN_DT.encode()) if neighborhood == 0 else _lib.refgpu_load(CUBIN.encode()))
         if rc:
             raise RuntimeError(f"loading the reference's kernels failed: {STATUS.get(rc, rc)}")
         _loaded.add(neighborhood)
@@ -126,3 +132,36 @@ def solve8(dp, dn, penalty=0, arrays=None, max_iters=5_000_000, max_seconds=60.0
     rc = lib(8).refgpu_solve8(W, H, _p(dp), _p(dn), int(penalty), ptrs, _p(label), int(max_iters),
                               float(max_seconds), C.byref(st))
     return _result(st, rc, label)
+
+
+def kde(img, points, sigma=0):
+    """The reference's kernel-density data term on the GPU (DataTermKernels.cu
+    driven as DataTerm.cpp does: init_data_term, setImage, setSigmaGaussian
+    when sigma > 0, selectOnMap per point, getDataTermsMixture).  img: (H, W, 3)
+    uint8 with H and W multiples of 16; points: (x, y) pairs whose 5x5 squares
+    lie inside the image.  Returns dict(pos, neg (H, W) int32, gauss (101,)
+    float32, map (H, W) uint8)."""
+    img = np.ascontiguousarray(img, np.uint8)
+    H, W = img.shape[:2]
+    pts = np.ascontiguousarray(np.asarray(points, np.int32).reshape(-1, 2))
+    pos = np.zeros((H, W), np.int32)
+    neg = np.zeros((H, W), np.int32)
+    gauss = np.zeros(101, np.float32)
+    sel = np.zeros((H, W), np.uint8)
+    rc = lib(0).refgpu_kde(W, H, _p(img), int(sigma), len(pts), _p(pts), _p(pos), _p(neg), _p(gauss), _p(sel))
+    if rc:
+        raise RuntimeError(f"refgpu_kde: {STATUS.get(rc, rc)}")
+    return dict(pos=pos, neg=neg, gauss=gauss, map=sel)
+
+
+def draw(sel_map, img):
+    """The reference's drawSelection (K_DrawMap) on the GPU: the pixels whose
+    map entry is 1 painted (0, 0, 255).  H and W multiples of 16."""
+    img = np.ascontiguousarray(img, np.uint8)
+    H, W = img.shape[:2]
+    m = np.ascontiguousarray(sel_map, np.uint8)
+    out = np.empty_like(img)
+    rc = lib(0).refgpu_draw(W, H, _p(m), _p(img), _p(out))
+    if rc:
+        raise RuntimeError(f"refgpu_draw: {STATUS.get(rc, rc)}")
+    return out

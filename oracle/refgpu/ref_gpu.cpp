@@ -12,6 +12,11 @@
  *                   allocations) + GC_SetGraph (:301-319) + GC_Optimize
  *                   (:385-534) + GC_End (:542-568)
  *   get_energy    = getEnergy (GraphCut.cu:359-376)
+ *   refgpu_kde    = DataTerm::init_data_term + setImage + setSigmaGaussian +
+ *                   selectOnMap (per point) + getDataTermsMixture
+ *                   (DataTerm.cpp:28-137) over the data-term kernels
+ *                   (DataTermKernels.cu, gc_ref_dt_kernels.cubin)
+ *   refgpu_draw   = DataTerm::drawSelection (DataTerm.cpp:155-165)
  *
  * Differences, all outside the timed arithmetic: every loop is bounded (an
  * iteration cap and a wall-clock cap, reported through the status instead of
@@ -373,6 +378,148 @@ int refgpu_solve(int w, int h, const int *dp, const int *dn, int penalty, const 
 int refgpu_solve8(int w, int h, const int *dp, const int *dn, int penalty, const int *const *edges8, int *label,
                   long long max_iters, double max_seconds, refgpu_stats *st) {
     return solve<8>(g_k8, w, h, dp, dn, penalty, edges8, label, max_iters, max_seconds, st);
+}
+
+}  // extern "C"
+
+namespace {
+
+// The data-term kernels (DataTermKernels.cu) and the launch shapes
+// DataTerm::init_data_term sets up (DataTerm.cpp:34-50).
+struct DtKernels {
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t gauss, init_map, init_cs, select, calc, draw;
+};
+DtKernels g_dt;
+constexpr int DT_N_PDF = 256;
+
+int dt_ready() { return g_dt.lib ? OK : ERR_NOT_LOADED; }
+
+}  // namespace
+
+extern "C" {
+
+/* Loads the reference's data-term kernels from their cubin. */
+int refgpu_load_dt(const char *cubin_path) {
+    if (g_dt.lib) return OK;
+    if (!cubin_path) return ERR_INVALID;
+    cudaLibrary_t lib;
+    if (cudaLibraryLoadFromFile(&lib, cubin_path, nullptr, nullptr, 0, nullptr, nullptr, 0) != cudaSuccess)
+        return ERR_CUDA;
+    bool ok = cudaLibraryGetKernel(&g_dt.gauss, lib, "_Z14K_InitGaussianfPf") == cudaSuccess;
+    ok = ok && cudaLibraryGetKernel(&g_dt.init_map, lib, "_Z18K_InitSelectionMapPhi") == cudaSuccess;
+    ok = ok && cudaLibraryGetKernel(&g_dt.init_cs, lib, "_Z16K_InitColorSpacePfi") == cudaSuccess;
+    ok = ok && cudaLibraryGetKernel(&g_dt.select, lib, "_Z16K_SelectAndGaussPhS_PfS0_iiii") == cudaSuccess;
+    ok = ok && cudaLibraryGetKernel(&g_dt.calc, lib, "_Z11K_CalcTermsPhPfPiS1_i") == cudaSuccess;
+    ok = ok && cudaLibraryGetKernel(&g_dt.draw, lib, "_Z9K_DrawMapPhS_i") == cudaSuccess;
+    if (!ok) {
+        cudaLibraryUnload(lib);
+        return ERR_CUDA;
+    }
+    g_dt.lib = lib;
+    return OK;
+}
+
+/* The reference's kernel-density data term on the GPU, driven as
+ * DataTerm.cpp does: init_data_term (K_InitGaussian with the default sigma 5,
+ * reset = K_InitSelectionMap + K_InitColorSpace), setImage, then
+ * setSigmaGaussian(sigma) when sigma > 0, selectOnMap for every point
+ * (25 K_SelectAndGauss launches over the 256^3 colour cube, one per pixel of
+ * the 5x5 square at (x, y)), getDataTermsMixture (K_CalcTerms).  Host
+ * buffers: img (h*w*3 bytes, the reference's channel order), pts (npts (x, y)
+ * pairs); outputs pos, neg (w*h int32), gauss (the 101 table entries) and map
+ * (w*h bytes, the selection map).
+ * The reference's kernels cover floor(w/16)*16 x floor(h/16)*16 pixels and
+ * selectOnMap writes past the image when the square does not fit, so w and
+ * h must be multiples of 16 and every square must lie inside the image
+ * (else 1, before any GPU work). */
+int refgpu_kde(int w, int h, const unsigned char *img, int sigma, int npts, const int *pts, int *pos, int *neg,
+               float *gauss, unsigned char *map) {
+    if (dt_ready() != OK) return ERR_NOT_LOADED;
+    if (w < 16 || h < 16 || w % 16 || h % 16 || !img || npts < 0 || (npts && !pts) || !pos || !neg) return ERR_INVALID;
+    for (int k = 0; k < npts; ++k)
+        if (pts[2 * k] < 0 || pts[2 * k + 1] < 0 || pts[2 * k] + 5 > w || pts[2 * k + 1] + 5 > h) return ERR_INVALID;
+    const size_t n = (size_t)w * h;
+    unsigned char *d_img = nullptr, *d_map = nullptr;
+    float *d_gauss = nullptr, *d_pdf = nullptr;
+    int *d_pos = nullptr, *d_neg = nullptr;
+    int rc = OK;
+    const dim3 t3(8, 8, 8), b3(DT_N_PDF / 8, DT_N_PDF / 8, DT_N_PDF / 8);  // DataTerm.cpp:34-40
+    const dim3 t2(16, 16, 1), b2(w / 16, h / 16, 1);                       // :42-49
+    const dim3 blin(256 * 3 / 16, 1, 1);                                    // :51-52
+    TRY(cudaMalloc(&d_img, 3 * n));
+    TRY(cudaMalloc(&d_gauss, sizeof(float) * DT_N_PDF));
+    TRY(cudaMalloc(&d_pdf, sizeof(float) * DT_N_PDF * DT_N_PDF * DT_N_PDF));
+    TRY(cudaMalloc(&d_map, n));
+    TRY(cudaMalloc(&d_pos, sizeof(int) * n));
+    TRY(cudaMalloc(&d_neg, sizeof(int) * n));
+    {
+        float s0 = 5.0f;  // DEFAULT_SIGMA (DataTerm.cpp:6)
+        int npdf = DT_N_PDF, width = w;
+        void *ag[] = {&s0, &d_gauss};
+        TRY(cudaLaunchKernel((const void *)g_dt.gauss, blin, t2, ag, 0, 0));
+        void *am[] = {&d_map, &width};
+        TRY(cudaLaunchKernel((const void *)g_dt.init_map, b2, t2, am, 0, 0));
+        void *ac[] = {&d_pdf, &npdf};
+        TRY(cudaLaunchKernel((const void *)g_dt.init_cs, b3, t3, ac, 0, 0));
+        TRY(cudaMemcpy(d_img, img, 3 * n, cudaMemcpyHostToDevice));
+        if (sigma > 0) {
+            float sg = (float)sigma;
+            void *as[] = {&sg, &d_gauss};
+            TRY(cudaLaunchKernel((const void *)g_dt.gauss, blin, t2, as, 0, 0));
+        }
+        int rect = 8;
+        for (int k = 0; k < npts; ++k)
+            for (int i = 0; i < 5; ++i)
+                for (int j = 0; j < 5; ++j) {
+                    int x1 = pts[2 * k] + i, y1 = pts[2 * k + 1] + j;
+                    void *a[] = {&d_map, &d_img, &d_pdf, &d_gauss, &x1, &y1, &rect, &width};
+                    TRY(cudaLaunchKernel((const void *)g_dt.select, b3, t3, a, 0, 0));
+                }
+        void *at[] = {&d_img, &d_pdf, &d_pos, &d_neg, &width};
+        TRY(cudaLaunchKernel((const void *)g_dt.calc, b2, t2, at, 0, 0));
+        TRY(cudaMemcpy(pos, d_pos, sizeof(int) * n, cudaMemcpyDeviceToHost));
+        TRY(cudaMemcpy(neg, d_neg, sizeof(int) * n, cudaMemcpyDeviceToHost));
+        if (gauss) TRY(cudaMemcpy(gauss, d_gauss, sizeof(float) * 101, cudaMemcpyDeviceToHost));
+        if (map) TRY(cudaMemcpy(map, d_map, n, cudaMemcpyDeviceToHost));
+    }
+done:
+    cudaFree(d_img);
+    cudaFree(d_gauss);
+    cudaFree(d_pdf);
+    cudaFree(d_map);
+    cudaFree(d_pos);
+    cudaFree(d_neg);
+    if (rc == OK && cudaGetLastError() != cudaSuccess) rc = ERR_CUDA;
+    return rc;
+}
+
+/* DataTerm::drawSelection (DataTerm.cpp:155-165): the input image is copied
+ * to the device, K_DrawMap paints the pixels whose selection-map entry is 1,
+ * and the result comes back.  map: w*h bytes (host), in, out: h*w*3 bytes;
+ * w and h multiples of 16 as for refgpu_kde. */
+int refgpu_draw(int w, int h, const unsigned char *map, const unsigned char *in, unsigned char *out) {
+    if (dt_ready() != OK) return ERR_NOT_LOADED;
+    if (w < 16 || h < 16 || w % 16 || h % 16 || !map || !in || !out) return ERR_INVALID;
+    const size_t n = (size_t)w * h;
+    unsigned char *d_img = nullptr, *d_map = nullptr;
+    int rc = OK;
+    int width = w;
+    const dim3 t2(16, 16, 1), b2(w / 16, h / 16, 1);
+    TRY(cudaMalloc(&d_img, 3 * n));
+    TRY(cudaMalloc(&d_map, n));
+    TRY(cudaMemcpy(d_map, map, n, cudaMemcpyHostToDevice));
+    TRY(cudaMemcpy(d_img, in, 3 * n, cudaMemcpyHostToDevice));
+    {
+        void *a[] = {&d_map, &d_img, &width};
+        TRY(cudaLaunchKernel((const void *)g_dt.draw, b2, t2, a, 0, 0));
+    }
+    TRY(cudaMemcpy(out, d_img, 3 * n, cudaMemcpyDeviceToHost));
+done:
+    cudaFree(d_img);
+    cudaFree(d_map);
+    if (rc == OK && cudaGetLastError() != cudaSuccess) rc = ERR_CUDA;
+    return rc;
 }
 
 }  // extern "C"

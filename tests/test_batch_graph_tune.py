@@ -114,3 +114,26 @@ def test_solver_settings_do_not_change_results(settings):
     for a, b in zip(ref, got):
         assert np.array_equal(a, b)
     bs.close()
+
+
+def test_phase_split_runs_both_phases_and_changes_no_result():
+    """gcfg_batch_phase_split runs the first global relabel and the push rounds
+    after it as two launches of the solver; the counters it reports are
+    consistent, and the handle's next run still gives the full solve's
+    results."""
+    Ws, Hs, lams, rgb, scrib = _batch(24, 3300)
+    d_rgb = torch.from_numpy(rgb).cuda()
+    d_scrib = torch.from_numpy(scrib).cuda()
+    bs = gcfg.BatchSolver(32, scrib.size)
+    ref = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
+    tiles = int(sum(((int(w) + 31) // 32) * ((int(h) + 31) // 32) for w, h in zip(Ws, Hs)))
+    for _ in range(2):
+        ps = bs.phase_split(Ws, Hs, lams, d_rgb, d_scrib)
+        assert ps["ms_relabel"] > 0 and ps["grid_blocks"] >= 1
+        assert ps["relabel_tiles"] >= tiles  # round 0 visits every tile
+        assert ps["active_pixels"] > 0 and ps["push_queue"] > 0
+        assert ps["ms_push"] > 0 and ps["push_tiles"] >= 1 and ps["push_phases"] >= 1
+        assert ps["push_sweeps"] >= ps["push_tiles"]
+        got = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
+        assert np.array_equal(got[0], ref[0])
+        assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2])

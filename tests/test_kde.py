@@ -4,7 +4,11 @@ Goldens: the reference's own DataTerm.cpp run on the CPU emulator
 (tests/golden/make_kde_fixtures.py).  The oracle restatement reproduces them
 bit for bit from their Gaussian table; the GPU reproduces the oracle bit for
 bit from its own table, and the two tables agree to 2 ulp (the emulator
-evaluates expf with the host library, the GPU with CUDA's)."""
+evaluates expf with the host library, the GPU with CUDA's).  On the GPU the
+reference's own data-term kernels (DataTermKernels.cu, built from its sources
+into oracle/_ref/gc_ref_dt_kernels.cubin) run beside this build's: their
+Gaussian table, t-links, selection map and drawSelection output must be equal
+bit for bit, with no condition."""
 import glob
 import os
 
@@ -113,4 +117,84 @@ def test_gpu_kde_edges_resets_and_sigma():
     dt.reset()
     p0, n0 = terms()
     assert (p0 == 0).all() and (n0 == 300000).all()
+    dt.close()
+
+
+def _ref_dt():
+    import ref_cuda
+    why = ref_cuda.unavailable(0)
+    if why:
+        pytest.skip(why)
+    return ref_cuda
+
+
+def _ours_kde(img, points, sigma):
+    import torch
+    import gcfg
+    H, W = img.shape[:2]
+    dt = gcfg.DataTermState(W, H)
+    dt.set_model("kde")
+    if sigma > 0:
+        dt.set_sigma(int(sigma))
+    dt.set_image(img)
+    for x, y in points:
+        dt.select_on_map(int(x), int(y), 1)
+    dt.compute()
+    out = dict(pos=torch.as_tensor(dt.pos(), device="cuda").cpu().numpy().reshape(H, W),
+               neg=torch.as_tensor(dt.neg(), device="cuda").cpu().numpy().reshape(H, W),
+               gauss=dt.kde_table(), dt=dt)
+    return out
+
+
+def _kde_cases():
+    cases = []
+    for path in CASES:
+        g = np.load(path)
+        cases.append((os.path.basename(path), g["img"], [tuple(p) for p in g["points"]], int(g["sigma"])))
+    rng = np.random.default_rng(77)
+    for k, (H, W, sigma, npts) in enumerate([(48, 64, 5, 4), (32, 32, 0, 2), (64, 48, 11, 6)]):
+        img = rng.integers(0, 256, (H, W, 3), dtype=np.uint8)
+        img[H // 4:H // 2, W // 4:W // 2] = (20, 200, 90)  # a uniform patch: many equal colours
+        pts = [(int(rng.integers(0, W - 4)), int(rng.integers(0, H - 4))) for _ in range(npts)]
+        cases.append((f"random{k}", img, pts, sigma))
+    return cases
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,img,points,sigma", _kde_cases(), ids=[c[0] for c in _kde_cases()])
+def test_gpu_kde_equals_reference_gpu_kernels(name, img, points, sigma):
+    """This build's KDE data term against the reference's own kernels on the
+    same GPU: Gaussian table, pos and neg bit for bit (sigma 0 = the default
+    table of init_data_term)."""
+    pytest.importorskip("torch")
+    ref = _ref_dt().kde(img, points, sigma)
+    ours = _ours_kde(img, points, sigma)
+    assert np.array_equal(ours["gauss"], ref["gauss"])
+    assert np.array_equal(ours["pos"], ref["pos"])
+    assert np.array_equal(ours["neg"], ref["neg"])
+    ours["dt"].close()
+
+
+@pytest.mark.gpu
+def test_draw_selection_equals_reference_gpu_kernel():
+    """drawSelection against K_DrawMap on the same GPU: after selectOnMap
+    (map entries 1) and after setSelection with labels 0/1/2 (only 1 marks)."""
+    pytest.importorskip("torch")
+    import gcfg
+    ref_cuda = _ref_dt()
+    rng = np.random.default_rng(5)
+    H, W = 48, 64
+    img = rng.integers(0, 256, (H, W, 3), dtype=np.uint8)
+    pts = [(3, 4), (40, 30), (58, 42)]
+    ref = ref_cuda.kde(img, pts, 0)
+    dt = gcfg.DataTermState(W, H)
+    dt.set_model("kde")
+    dt.set_image(img)
+    for x, y in pts:
+        dt.select_on_map(x, y, 1)
+    other = rng.integers(0, 256, (H, W, 3), dtype=np.uint8)
+    assert np.array_equal(dt.draw_selection(other), ref_cuda.draw(ref["map"], other))
+    labels = rng.integers(0, 3, (H, W)).astype(np.int32)
+    dt.set_selection(labels)
+    assert np.array_equal(dt.draw_selection(other), ref_cuda.draw(labels.astype(np.uint8), other))
     dt.close()

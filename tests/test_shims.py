@@ -123,8 +123,7 @@ def test_dataterm_shim_matches_oracle(programs, tmp_path, seed, W, H, penalty):
     o = O.solve(dp, dn, penalty=penalty)
     assert np.array_equal(np.fromfile(pre + ".label", "<i4").reshape(H, W), o["smax"].astype(np.int32))
     drawn = rgb.copy()
-    drawn[scrib == 1] = (0, 0, 255)
-    drawn[scrib == 2] = (255, 0, 0)
+    drawn[scrib == 1] = (0, 0, 255)  # K_DrawMap: map entries equal to 1 only
     assert np.array_equal(np.fromfile(pre + ".draw", np.uint8).reshape(H, W, 3), drawn)
 
 

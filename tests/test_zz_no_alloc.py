@@ -8,9 +8,13 @@ synchronisation cudaMalloc/cudaFree can cause.  Its working memory is a fixed
 16 MiB device array inside the library, so it accepts images of at most 640
 tiles of 32x32 pixels.  Called through the C ABI, it must return exactly the
 labels and the flow value of gcfg_init + gcfg_optimize, call after call (the
-array keeps the previous call's contents).
+array keeps the previous call's contents), and repeated calls must leave the
+device's free memory unchanged.
 
-This file is collected last on purpose.
+The tests here pass alone in a fresh process as well as after the others; the
+file name only makes pytest collect it last, so that a run that stops at its
+first failure (pytest -x) has already run every other test if one of these
+fails.
 """
 import ctypes as C
 
@@ -80,3 +84,32 @@ def test_noalloc_refuses_images_beyond_its_working_memory():
     rc = lib.gcfg_solve_noalloc(1025, 640, p, p, 5, None, None, None, None, p, None, None)
     assert rc == gcfg.GCFG_ERR_TOO_LARGE
     assert "allocation-free" in gcfg.strerror(rc)
+
+
+def test_noalloc_repeated_calls_leave_free_device_memory_unchanged():
+    dp, dn, penalty, kw = _instance(14, 300, 400, arrays=True)
+    H, W = dp.shape
+    t = [_dev(dp), _dev(dn)] + [_dev(kw[k]) for k in ("up", "down", "left", "right")]
+    label = torch.empty((H, W), dtype=torch.int32, device="cuda")
+    ptr = [C.c_void_p(x.data_ptr()) for x in t]
+    lab = C.c_void_p(label.data_ptr())
+    lib = gcfg.load()
+    flows = []
+
+    def call():
+        flow = C.c_int64(-1)
+        rc = lib.gcfg_solve_noalloc(W, H, ptr[0], ptr[1], penalty, *ptr[2:], lab, C.byref(flow), None)
+        assert rc == gcfg.GCFG_OK, gcfg.strerror(rc)
+        flows.append(flow.value)
+
+    call()  # the first call may load the library's device code and its array
+    torch.cuda.synchronize()
+    first = label.cpu().numpy()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert len(set(flows)) == 1
+    assert np.array_equal(label.cpu().numpy(), first)
