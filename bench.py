@@ -629,6 +629,52 @@ def profiled_roofline(gcfg, flush, run_once, Ws, Hs, batched, px, peak, peak_kin
             "kernels_ms": {k: round(v["ms"], 4) for k, v in prof.items() if v["launches"]}}, recs
 
 
+def tuned_vs_default(gcfg, stream, Ws, Hs, lams, d_rgb, d_scrib, offs, flows, smin_all, smax_all, reps=5):
+    """Each image of a single-image workload solved as a batch of one
+    (gcfg_batch_run, device-resident) under the default solver settings and
+    under the settings gcfg_batch_autotune picks for it (tile shape = the
+    solver's thread block over each 32x32 tile, sweeps per global relabel,
+    blocks per SM = blocks per image / SMs): best-of-`reps` device times
+    (data term, build, solve, extraction) and the check that the tuned run's
+    flow and cuts equal the plain solver's."""
+    import torch
+    out, eq, t_def, t_tun = [], True, 0.0, 0.0
+    for i in range(len(Ws)):
+        o, n = int(offs[i]), int(Ws[i]) * int(Hs[i])
+        w, h, lam = Ws[i:i + 1], Hs[i:i + 1], lams[i:i + 1]
+        rgb, scr = d_rgb[3 * o:3 * (o + n)], d_scrib[o:o + n]
+        smin = torch.empty(n, dtype=torch.uint8, device="cuda")
+        smax = torch.empty(n, dtype=torch.uint8, device="cuda")
+        bs = gcfg.BatchSolver(1, n)
+        bs.set_stream(stream)
+
+        def best_ms():
+            ms, fl = [], None
+            for _ in range(reps):
+                fl, res = bs.run(w, h, lam, rgb, scr, smin, smax, results=True)
+                ms.append(res[0]["ms"])
+            return min(ms), fl
+
+        bs.set_solver()
+        ms_def, fl_def = best_ms()
+        tuning = bs.autotune(w, h, lam, rgb, scr, reps=2)
+        ms_tun, fl_tun = best_ms()
+        eq &= bool(fl_def[0] == flows[i] and fl_tun[0] == flows[i] and
+                   np.array_equal(smin.cpu().numpy(), smin_all[o:o + n]) and
+                   np.array_equal(smax.cpu().numpy(), smax_all[o:o + n]))
+        bs.close()
+        t_def += ms_def
+        t_tun += ms_tun
+        out.append({k: tuning[k] for k in ("threads_y", "push_rounds_per_gr", "max_tile_sweeps",
+                                           "sweeps_per_local_relabel", "blocks_per_sm", "local_relabel_first",
+                                           "push_only")} | {"default_ms": round(ms_def, 4), "tuned_ms": round(ms_tun, 4)})
+    return {"default_ms": round(t_def, 4), "tuned_ms": round(t_tun, 4), "speedup": round(t_def / t_tun, 3),
+            "per_image": out, "results_equal": eq,
+            "how": "each image as a batch of one through gcfg_batch_run; best of 5 device times (data term to cuts) "
+                   "under the default settings (32 x 8 solver block, 2 push rounds per global relabel, 24 sweeps, "
+                   "local relabel every 4) and under gcfg_batch_autotune's choice for that image"}
+
+
 def plain_leg(torch, gcfg, name, steps, warmup, flush, stream, peak, peak_kind, cpu_budget=10.0, ref_budget=5.0):
     """One single-image workload through the plain per-image solver
     (gcfg_seg_run): images resident in HBM (value), the same through
@@ -694,6 +740,7 @@ def plain_leg(torch, gcfg, name, steps, warmup, flush, stream, peak, peak_kind, 
     roof["solve_phases"] = solve_phases(gcfg, stream, Ws, Hs, lams, d_rgb, d_scrib, offs, peak, name, False)
     smin_all, smax_all = d_smin.cpu().numpy(), d_smax.cpu().numpy()
     seg.close()
+    tuned = tuned_vs_default(gcfg, stream, Ws, Hs, lams, d_rgb, d_scrib, offs, flows, smin_all, smax_all)
     cpu_v, n_chk, secs, parity = cpu_baseline(views, lams, budget_s=cpu_budget, flows_gpu=flows,
                                               smin_gpu=smin_all, smax_gpu=smax_all, offs=offs)
     leg = {"desc": spec["desc"], "images": n_img, "pixels": px, "value": px / (ms / 1e3) / 1e6, "unit": UNIT,
@@ -702,7 +749,7 @@ def plain_leg(torch, gcfg, name, steps, warmup, flush, stream, peak, peak_kind, 
                    "h2d_bytes_per_step": 4 * px, "d2h_bytes_per_step": 2 * px,
                    "api": "gcfg_seg_run_host per image, pinned host buffers, wall clock per step",
                    "results_equal_device": host_equal},
-           "roofline": roof,
+           "roofline": roof, "tuned_vs_default": tuned,
            "solver": {k: res[0][k] for k in ("global_relabels", "closure_checks", "push_tiles", "gr_tiles",
                                              "push_sweeps", "push_local_relabels")},
            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": 1, "kind": "port",
@@ -902,7 +949,7 @@ def main():
     ap.add_argument("--no-graph", action="store_true", help="run the batch without CUDA graph replay")
     ap.add_argument("--solver-params", default=None,
                     help="push_rounds,max_sweeps,sweeps_per_local_relabel[,blocks_per_sm[,relabel_first"
-                         "[,push_only]]] for the batch (skips the autotuner)")
+                         "[,push_only[,threads_y]]]] for the batch (skips the autotuner)")
     ap.add_argument("--serve-requests", type=int, default=1200)
     ap.add_argument("--ref-cuda-budget", type=float, default=15.0,
                     help="seconds of reference CUDA solve time for the reference_cuda leg (0 skips it)")
@@ -988,7 +1035,7 @@ def main():
     tuning = None
     if batched and args.solver_params:
         keys = ("push_rounds_per_gr", "max_tile_sweeps", "sweeps_per_local_relabel", "blocks_per_sm",
-                "local_relabel_first", "push_only")
+                "local_relabel_first", "push_only", "threads_y")
         tuning = dict(zip(keys, (int(v) for v in args.solver_params.split(","))))
         bs.set_solver(**tuning)
         tuning["fixed"] = True

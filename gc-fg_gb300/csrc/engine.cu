@@ -365,6 +365,7 @@ __device__ __forceinline__ unsigned long long *ctl_stat(Ctl *c, int k) {
     }
 }
 
+template <int NW>  // warps per block
 struct SmemPush {
     int4 c[TILE_H][TILE_W];
     int e[TILE_H][TILE_W];
@@ -375,15 +376,17 @@ struct SmemPush {
     int lv[NREC];             // and its level
     unsigned sfin[32];        // final reached rows
     int nrec;
-    unsigned long long part[8];
+    unsigned long long part[NW];
     int idx;
 };
+template <int NW>
 struct SmemWarp {
-    int hs[8][32 * 33];
+    int hs[NW][32 * 33];
 };
+template <int NW>
 union Smem {
-    SmemPush p;
-    SmemWarp w;
+    SmemPush<NW> p;
+    SmemWarp<NW> w;
 };
 
 // ---------------------------------------------------------------------------
@@ -601,16 +604,18 @@ __device__ void sink_reach_tile(const Batch &b, int t, bool round0, int tag_next
 // The block's next queue entry is taken (thread 0, from take_ctr) when the
 // sweeps end, so that the atomic overlaps the write-back; it is left in s.idx
 // for the caller.
-__device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int phase, SmemPush &s,
+template <int NW>
+__device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int phase, SmemPush<NW> &s,
                           unsigned long long *st, int *take_ctr) {
+    constexpr int RPW = TILE_H / NW;  // rows per warp: thread (warp, lane) owns rows warp + NW k, column lane
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     long long c0 = clock64(), c1, cb = 0, cs = 0;
     GrGeo g;  // only the neighbours are used
     tile_nbs(b, t, g.nb);
     const size_t base = (size_t)t * TPX;
 #pragma unroll
-    for (int k = 0; k < ROWS_PER_WARP; ++k) {
-        const int r = warp + 8 * k;
+    for (int k = 0; k < RPW; ++k) {
+        const int r = warp + NW * k;
         s.c[r][lane] = __ldcg(b.cap + base + r * 32 + lane);
         s.e[r][lane] = __ldcg(b.exc + base + r * 32 + lane);
         s.h[r + 1][lane + 1] = __ldcg(b.h + base + r * 32 + lane);
@@ -633,8 +638,8 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
         ++bfs;
         since_bfs = 0;
 #pragma unroll
-        for (int k = 0; k < ROWS_PER_WARP; ++k) {
-            const int r = warp + 8 * k;
+        for (int k = 0; k < RPW; ++k) {
+            const int r = warp + NW * k;
             const int4 c = s.c[r][lane];
             const int e = s.e[r][lane];
             const unsigned ml = __ballot_sync(FULL, c.x > 0);
@@ -663,8 +668,8 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
         {
             const int nrec = s.nrec;
 #pragma unroll
-            for (int k = 0; k < ROWS_PER_WARP; ++k) {
-                const int r = warp + 8 * k;
+            for (int k = 0; k < RPW; ++k) {
+                const int r = warp + NW * k;
                 s.h[r + 1][lane + 1] =
                     height_from_records(r, lane, s.m[4][r], s.srec, s.lv, s.sfin, nrec, s.h[r + 1][lane + 1]);
             }
@@ -682,17 +687,17 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
         ++since_bfs;
         // ---- push phase: heights fixed.  All loads first, flows in
         // registers, then fire-and-forget shared atomics. ----
-        int ev[ROWS_PER_WARP], hv[ROWS_PER_WARP];
+        int ev[RPW], hv[RPW];
 #pragma unroll
-        for (int k = 0; k < ROWS_PER_WARP; ++k) {
-            const int r = warp + 8 * k;
+        for (int k = 0; k < RPW; ++k) {
+            const int r = warp + NW * k;
             ev[k] = s.e[r][lane];
             hv[k] = s.h[r + 1][lane + 1];
         }
         bool pushed = false;
 #pragma unroll
-        for (int k = 0; k < ROWS_PER_WARP; ++k) {
-            const int r = warp + 8 * k;
+        for (int k = 0; k < RPW; ++k) {
+            const int r = warp + NW * k;
             const int hh = hv[k];
             if (ev[k] > 0 && hh < INF_H) {
                 const int4 c = s.c[r][lane];
@@ -761,8 +766,8 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
                 local_relabel();
                 int act = 0;
 #pragma unroll
-                for (int k = 0; k < ROWS_PER_WARP; ++k) {
-                    const int r = warp + 8 * k;
+                for (int k = 0; k < RPW; ++k) {
+                    const int r = warp + NW * k;
                     act |= s.e[r][lane] > 0 && s.h[r + 1][lane + 1] < INF_H;
                 }
                 any = __syncthreads_or(act);
@@ -775,13 +780,13 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
         // loaded for the push phase: only their owner writes them) ----
         int act = 0;
 #pragma unroll
-        for (int k = 0; k < ROWS_PER_WARP; ++k) {
-            const int r = warp + 8 * k;
+        for (int k = 0; k < RPW; ++k) {
+            const int r = warp + NW * k;
             ev[k] = s.e[r][lane];
         }
 #pragma unroll
-        for (int k = 0; k < ROWS_PER_WARP; ++k) {
-            const int r = warp + 8 * k;
+        for (int k = 0; k < RPW; ++k) {
+            const int r = warp + NW * k;
             int hh = hv[k];
             if (ev[k] > 0 && hh < INF_H) {
                 const int4 c = s.c[r][lane];
@@ -810,8 +815,8 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
     // ---- write back (and refresh the tile's mask planes and excess sum) ----
     unsigned long long pos = 0;
 #pragma unroll
-    for (int k = 0; k < ROWS_PER_WARP; ++k) {
-        const int r = warp + 8 * k;
+    for (int k = 0; k < RPW; ++k) {
+        const int r = warp + NW * k;
         const int4 c = s.c[r][lane];
         const int e = s.e[r][lane];
         b.cap[base + r * 32 + lane] = c;
@@ -832,7 +837,7 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
     __syncthreads();
     if (threadIdx.x == 0) {
         unsigned long long tot = 0;
-        for (int w = 0; w < 8; ++w) tot += s.part[w];
+        for (int w = 0; w < NW; ++w) tot += s.part[w];
         b.tile_pos[t] = tot;
     }
     // ---- hand halo flow to the (idle) neighbour tiles ----
@@ -893,10 +898,11 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
 // excess.  Returns 1 when every image is finished, 0 when some are not, -1
 // on an error (recorded in the control block).  Called by every thread of the
 // grid; kept out of line so that its registers do not add to the solver's.
+template <int NW>
 __device__ __noinline__ int closure_check(const Batch &b, const SolveParams &prm, int &G) {
     Ctl *ctl = b.ctl;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int gwarp = blockIdx.x * 8 + warp, nwarps = gridDim.x * 8;
+    const int gwarp = blockIdx.x * NW + warp, nwarps = gridDim.x * NW;
     const int swarp = warp * gridDim.x + blockIdx.x;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
     const int nt = batch_ntiles(b);
@@ -973,16 +979,23 @@ __device__ __noinline__ int closure_check(const Batch &b, const SolveParams &prm
     return 1;
 }
 
-#ifndef GCFG_SOLVE_MIN_BLOCKS
-#define GCFG_SOLVE_MIN_BLOCKS 4   // blocks of the persistent kernel per SM (register budget)
-#endif
+// The block is NW warps over one 32x32 tile (thread block 32 x NW, the
+// reference's THREADS_X x THREADS_Y, GraphCut.h:39-53).  Blocks per SM the
+// register budget is set for: 8 warps 4 and 16 warps 2 (64 registers per
+// thread); 4 warps 6, the most its shared memory allows (80 registers, the
+// 8 rows per thread need them).  The phases' shared memory (union Smem<NW>)
+// is dynamic: above 48 KB for 16 warps.
+template <int NW>
+constexpr int solve_min_blocks() { return NW == 4 ? 6 : 32 / NW; }
 
-__global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(Batch b, SolveParams prm) {
-    __shared__ Smem sm;
+template <int NW>
+__global__ void __launch_bounds__(NW * 32, solve_min_blocks<NW>()) k_solve(Batch b, SolveParams prm) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem<NW> &sm = *reinterpret_cast<Smem<NW> *>(smem_raw);
     __shared__ unsigned long long st[ST_N];
     Ctl *ctl = b.ctl;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int gwarp = blockIdx.x * 8 + warp, nwarps = gridDim.x * 8;
+    const int gwarp = blockIdx.x * NW + warp, nwarps = gridDim.x * NW;
     const int swarp = warp * gridDim.x + blockIdx.x;  // block-interleaved warp rank
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
 
@@ -1015,7 +1028,7 @@ __global__ void __launch_bounds__(TILE_THREADS, GCFG_SOLVE_MIN_BLOCKS) k_solve(B
     for (int outer = 0; outer < prm.max_outer; ++outer) {
         if (prm.phase == 2) goto push_rounds;  // the phase-1 launch did the relabel and the count
         if (outer > 0) {
-            const int rc = closure_check(b, prm, G);
+            const int rc = closure_check<NW>(b, prm, G);
             if (rc < 0) return;
             clk.charge(&ctl->t_gr);
             if (rc > 0) {
@@ -1299,39 +1312,70 @@ __global__ void __launch_bounds__(TILE_THREADS) k_extract(Batch b, uint8_t *smin
 
 namespace gcfg {
 
-int solve_grid_blocks(int n_tiles, int max_grid) {
-    // co-resident blocks of k_solve on the current device, computed once per
-    // device ordinal; several host threads (the server's lanes) may race to
-    // fill an entry, and they all store the same value
+namespace {
+
+// The solver kernel of a block shape (warps per block: 4, 8 or 16) and its
+// dynamic shared memory.
+struct SolveKernel {
+    const void *fn;
+    size_t smem;
+};
+
+SolveKernel solve_kernel(int warps) {
+    switch (warps) {
+        case 4: return {(const void *)k_solve<4>, sizeof(Smem<4>)};
+        case 16: return {(const void *)k_solve<16>, sizeof(Smem<16>)};
+        default: return {(const void *)k_solve<8>, sizeof(Smem<8>)};
+    }
+}
+
+int shape_index(int warps) { return warps == 4 ? 0 : warps == 16 ? 2 : 1; }
+
+// Co-resident blocks of the solver kernel of a shape on the current device,
+// computed once per device ordinal and shape (the kernel's dynamic
+// shared-memory limit is raised first where the shape needs it); several
+// host threads (the server's lanes) may race to fill an entry, and they all
+// store the same value.
+int resident_blocks(int warps) {
     constexpr int MAX_DEV = 64;
-    static std::atomic<int> cached[MAX_DEV];
+    static std::atomic<int> cached[MAX_DEV][3];
     int dev = 0;
     cudaGetDevice(&dev);
     const bool slot = dev >= 0 && dev < MAX_DEV;
-    int full = slot ? cached[dev].load(std::memory_order_relaxed) : 0;
+    const int si = shape_index(warps);
+    int full = slot ? cached[dev][si].load(std::memory_order_relaxed) : 0;
     if (!full) {
+        const SolveKernel k = solve_kernel(warps);
+        cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
         int sms = 0, per_sm = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve, TILE_THREADS, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, warps * 32, k.smem);
         full = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
-        if (slot) cached[dev].store(full, std::memory_order_relaxed);
+        if (slot) cached[dev][si].store(full, std::memory_order_relaxed);
     }
+    return full;
+}
+
+}  // namespace
+
+int solve_grid_blocks(int n_tiles, int max_grid, int warps) {
     // half the tiles run in a push phase; more blocks than that only make
     // the grid barrier slower
-    int cap = full;
+    int cap = resident_blocks(warps);
     if (max_grid > 0 && max_grid < cap) cap = max_grid;
     const int want = (n_tiles + 1) / 2;
     return want < 1 ? 1 : (want < cap ? want : cap);
 }
 
 gcfg_status launch_solve(const Batch &b, const SolveParams &prm, int n_tiles, cudaStream_t st, int max_grid) {
-    const int grid = solve_grid_blocks(n_tiles, max_grid);
+    const int warps = prm.warps == 4 || prm.warps == 16 ? prm.warps : 8;
+    const int grid = solve_grid_blocks(n_tiles, max_grid, warps);
+    const SolveKernel k = solve_kernel(warps);
     Batch bb = b;
     SolveParams pp = prm;
     void *args[] = {&bb, &pp};
     prof_begin(st);
-    const cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_solve, dim3(grid), dim3(TILE_THREADS),
-                                                      args, 0, st);
+    const cudaError_t e = cudaLaunchCooperativeKernel(k.fn, dim3(grid), dim3(warps * 32), args, k.smem, st);
     prof_end(GCFG_PK_SOLVE, st);
     g_launches.fetch_add(1, std::memory_order_relaxed);
     return e == cudaSuccess ? GCFG_OK : GCFG_ERR_CUDA;

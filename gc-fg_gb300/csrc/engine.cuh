@@ -120,6 +120,7 @@ struct SolveParams {
     // control block not cleared in between): the push rounds of the first
     // outer iteration, then return.  A split leaves the solve unfinished.
     int phase;
+    int warps;         // warps per block of the solver kernel (block shape 32 x warps over a 32x32 tile): 4, 8 or 16
 };
 
 // Default solver settings of every entry point (before any tuning): 2 push
@@ -128,7 +129,7 @@ struct SolveParams {
 // the 256-image batch, these are at or near the fastest of the settings tried
 // for every case (4 rounds with 64 sweeps and a local relabel every 16 sweeps
 // took up to 2.9x longer on the 1920x1080 image with lambda 200).
-constexpr SolveParams kDefaultSolveParams{64, 2, 24, 4, 0, 1 << 20, 0, 0};
+constexpr SolveParams kDefaultSolveParams{64, 2, 24, 4, 0, 1 << 20, 0, 0, 8};
 
 __host__ __device__ __forceinline__ int batch_ntiles(const Batch &b) { return b.tlist ? b.n_tlist : b.n_tiles; }
 __device__ __forceinline__ int batch_tile(const Batch &b, int k) { return b.tlist ? __ldg(b.tlist + k) : k; }
@@ -150,8 +151,9 @@ enum {
 namespace gcfg {
 
 // Host launchers (engine.cu).
-// Co-resident blocks of the persistent kernel (capped by max_grid when > 0).
-int solve_grid_blocks(int n_tiles, int max_grid = 0);
+// Co-resident blocks of the persistent kernel of a block shape (warps per
+// block), capped by max_grid when > 0 and by half the tiles.
+int solve_grid_blocks(int n_tiles, int max_grid = 0, int warps = 8);
 gcfg_status launch_solve(const Batch &b, const SolveParams &prm, int n_tiles, cudaStream_t st,
                          int max_grid = 0);
 gcfg_status launch_build_arrays(const Batch &b, const int *dp, const int *dn, int penalty, const int *up,

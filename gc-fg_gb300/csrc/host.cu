@@ -1195,7 +1195,8 @@ gcfg_status gcfg_batch_set_params(gcfg_batch *b, int push_rounds_per_gr, int max
 gcfg_status gcfg_batch_set_solver(gcfg_batch *b, const gcfg_tuning *t) {
     if (!b || !t || t->push_rounds_per_gr < 1 || t->max_tile_sweeps < 1 || t->sweeps_per_local_relabel < 1 ||
         t->blocks_per_sm < 0 || (t->local_relabel_first != 0 && t->local_relabel_first != 1) ||
-        (t->push_only != 0 && t->push_only != 1))
+        (t->push_only != 0 && t->push_only != 1) ||
+        (t->threads_y != 0 && t->threads_y != 4 && t->threads_y != 8 && t->threads_y != 16))
         return GCFG_ERR_INVALID;
     int dev = 0, sms = 1;
     GCFG_CK(cudaGetDevice(&dev));
@@ -1205,6 +1206,7 @@ gcfg_status gcfg_batch_set_solver(gcfg_batch *b, const gcfg_tuning *t) {
     b->e.prm.bfs_every = t->sweeps_per_local_relabel;
     b->e.prm.bfs_first = t->local_relabel_first;
     b->e.prm.push_only = t->push_only;
+    b->e.prm.warps = t->threads_y ? t->threads_y : 8;
     b->e.max_grid = t->blocks_per_sm * sms;  // 0: as many as fit
     return GCFG_OK;
 }
@@ -1234,12 +1236,14 @@ gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const i
     const bool graph = e.graph_on;
     e.graph_on = false;  // time the eager runs; the graph is recaptured afterwards
     e.drop_graphs();
-    int dev = 0, sms = 1, per_sm = 1;
+    int dev = 0, sms = 1;
     GCFG_CK(cudaGetDevice(&dev));
     GCFG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int full = solve_grid_blocks(1 << 30);
-    per_sm = full / (sms > 0 ? sms : 1);
-    if (per_sm < 1) per_sm = 1;
+    // co-resident blocks per SM of each block shape
+    auto per_sm_of = [&](int warps) {
+        const int f = solve_grid_blocks(1 << 30, 0, warps) / (sms > 0 ? sms : 1);
+        return f < 1 ? 1 : f;
+    };
 
     std::vector<int64_t> ref(n), got(n);
     std::vector<gcfg_result> rr(n);
@@ -1263,27 +1267,37 @@ gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const i
         return GCFG_OK;
     };
     SolveParams cur = e.prm;
-    int cur_bps = e.max_grid > 0 ? (e.max_grid + sms - 1) / sms : per_sm;
-    if (cur_bps > per_sm) cur_bps = per_sm;
+    if (cur.warps != 4 && cur.warps != 16) cur.warps = 8;
+    int cur_bps = e.max_grid > 0 ? (e.max_grid + sms - 1) / sms : per_sm_of(cur.warps);
+    if (cur_bps > per_sm_of(cur.warps)) cur_bps = per_sm_of(cur.warps);
     float ms_default = 0.f;
     rc = time_cfg(cur, cur_bps, &ms_default);  // warms up, then the default
     if (rc == GCFG_OK) rc = time_cfg(cur, cur_bps, &ms_default);
     float best = ms_default;
+    // Coordinate search: the block shape (warps per block, at the shape's
+    // full occupancy), push rounds per global relabel, sweeps per visit,
+    // sweeps between local relabels, blocks per SM, relabel-first, push-only.
+    static const int c_warps[] = {4, 8, 16};
     static const int c_push[] = {2, 4, 8, 16};
     static const int c_sweeps[] = {16, 24, 32, 64, 128};
     static const int c_bfs[] = {2, 4, 8, 16, 32};
     for (int pass = 0; pass < 2 && rc == GCFG_OK; ++pass) {
-        for (int which = 0; which < 6 && rc == GCFG_OK; ++which) {
-            const int nc = which == 3 ? per_sm : which == 1 || which == 2 ? 5 : which >= 4 ? 2 : 4;
+        for (int which = 0; which < 7 && rc == GCFG_OK; ++which) {
+            const int nc = which == 0 ? 3 : which == 1 ? 4 : which == 2 || which == 3 ? 5
+                         : which == 4 ? per_sm_of(cur.warps) : 2;
             for (int c = 0; c < nc && rc == GCFG_OK; ++c) {
                 SolveParams p = cur;
                 int bps = cur_bps;
-                if (which == 0) p.push_rounds = c_push[c];
-                if (which == 1) p.max_sweeps = c_sweeps[c];
-                if (which == 2) p.bfs_every = c_bfs[c];
-                if (which == 3) bps = c + 1;
-                if (which == 4) p.bfs_first = c;
-                if (which == 5) p.push_only = c;
+                if (which == 0) {
+                    p.warps = c_warps[c];
+                    bps = per_sm_of(p.warps);
+                }
+                if (which == 1) p.push_rounds = c_push[c];
+                if (which == 2) p.max_sweeps = c_sweeps[c];
+                if (which == 3) p.bfs_every = c_bfs[c];
+                if (which == 4) bps = c + 1;
+                if (which == 5) p.bfs_first = c;
+                if (which == 6) p.push_only = c;
                 if (memcmp(&p, &cur, sizeof(p)) == 0 && bps == cur_bps) continue;
                 float ms = 0.f;
                 rc = time_cfg(p, bps, &ms);
@@ -1311,6 +1325,7 @@ gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const i
         out->configs_tried = tried;
         out->tile_w = TILE_W;
         out->tile_h = TILE_H;
+        out->threads_y = cur.warps;
     }
     return GCFG_OK;
 }
@@ -1364,7 +1379,7 @@ gcfg_status gcfg_batch_phase_split(gcfg_batch *b, int n, const int *widths, cons
         if ((rc = e.fetch()) != GCFG_OK) break;
         c1 = *e.h_ctl;
         if (c1.err) { rc = GCFG_ERR_NOT_CONVERGED; break; }
-        out->grid_blocks = solve_grid_blocks(e.n_tiles, e.max_grid);
+        out->grid_blocks = solve_grid_blocks(e.n_tiles, e.max_grid, p.warps);
         out->relabel_tiles = (int64_t)c1.gr_tiles;
         out->relabel_rounds = c1.gr_rounds;
         out->active_pixels = (int64_t)c1.total_active;

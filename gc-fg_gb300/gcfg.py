@@ -76,10 +76,10 @@ class Tuning(C.Structure):
                 ("sweeps_per_local_relabel", C.c_int32), ("blocks_per_sm", C.c_int32),
                 ("ms_default", C.c_float), ("ms_best", C.c_float), ("configs_tried", C.c_int32),
                 ("tile_w", C.c_int32), ("tile_h", C.c_int32), ("local_relabel_first", C.c_int32),
-                ("push_only", C.c_int32), ("pad", C.c_int32)]
+                ("push_only", C.c_int32), ("threads_y", C.c_int32)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class PhaseSplit(C.Structure):
@@ -393,11 +393,13 @@ class BatchSolver:
         return {"active": bool(a.value), "captures": c.value, "replays": r.value, "kernels_per_replay": k.value}
 
     def set_solver(self, push_rounds_per_gr=2, max_tile_sweeps=24, sweeps_per_local_relabel=4,
-                   blocks_per_sm=0, local_relabel_first=0, push_only=0, **_ignored):
-        """Solver settings (keys as autotune() returns them)."""
+                   blocks_per_sm=0, local_relabel_first=0, push_only=0, threads_y=8, **_ignored):
+        """Solver settings (keys as autotune() returns them); threads_y is the
+        solver's block shape 32 x threads_y (4, 8 or 16) over each 32x32 tile."""
         t = Tuning(push_rounds_per_gr=int(push_rounds_per_gr), max_tile_sweeps=int(max_tile_sweeps),
                    sweeps_per_local_relabel=int(sweeps_per_local_relabel), blocks_per_sm=int(blocks_per_sm),
-                   local_relabel_first=int(local_relabel_first), push_only=int(push_only))
+                   local_relabel_first=int(local_relabel_first), push_only=int(push_only),
+                   threads_y=int(threads_y))
         _check(load().gcfg_batch_set_solver(self.handle, C.byref(t)), "gcfg_batch_set_solver")
 
     def autotune(self, widths, heights, lambdas, d_rgb, d_scrib, reps=3) -> dict:

@@ -321,18 +321,22 @@ gcfg_status gcfg_batch_set_graph(gcfg_batch *b, int enable);
 gcfg_status gcfg_batch_graph_info(gcfg_batch *b, int *active, int64_t *captures, int64_t *replays,
                                   int64_t *kernels_per_replay);
 
-/* Autotuner result: the solver settings chosen for a batch. */
+/* Autotuner result: the solver settings chosen for a batch.  The tile shape
+ * is the thread block over each 32x32 tile of the residual graph: 32 x
+ * threads_y threads, the counterpart of the reference's THREADS_X x
+ * THREADS_Y (GraphCut.h:39-53, 32 x 8); the data tile itself stays 32x32,
+ * the width of the bit-plane tile BFS (one 32-bit mask per row). */
 typedef struct {
     int32_t push_rounds_per_gr;       /* checkerboard push rounds between global relabels */
     int32_t max_tile_sweeps;          /* push/relabel sweeps per tile visit */
     int32_t sweeps_per_local_relabel; /* sweeps between exact local (tile BFS) relabels */
-    int32_t blocks_per_sm;            /* persistent solver blocks per SM */
+    int32_t blocks_per_sm;            /* persistent solver blocks per SM (for one image: blocks per image / SMs) */
     float ms_default, ms_best;        /* device time of one run before / after tuning */
     int32_t configs_tried;
-    int32_t tile_w, tile_h;           /* tile shape (fixed: the width of the bit-plane BFS) */
+    int32_t tile_w, tile_h;           /* data tile of the residual graph (32 x 32, fixed) */
     int32_t local_relabel_first;      /* 1: exact local relabel at the start of every tile visit */
     int32_t push_only;                /* 1: sweeps only push; heights change by exact local relabels */
-    int32_t pad;
+    int32_t threads_y;                /* solver block 32 x threads_y: 4, 8 or 16 (0 in gcfg_batch_set_solver: 8) */
 } gcfg_tuning;
 
 /* Use these solver settings for the following runs (for example the record

@@ -137,3 +137,40 @@ def test_phase_split_runs_both_phases_and_changes_no_result():
         got = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
         assert np.array_equal(got[0], ref[0])
         assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2])
+
+
+@pytest.mark.parametrize("threads_y", [4, 8, 16])
+def test_every_solver_block_shape_gives_the_same_results(threads_y):
+    """The solver's thread block over a 32x32 tile (32 x threads_y, the
+    reference's THREADS_X x THREADS_Y) changes only the running time: flows
+    and both cuts equal those of the default 32 x 8 block, also with the
+    push-only sweeps and fewer blocks per SM."""
+    Ws, Hs, lams, rgb, scrib = _batch(20, 3500)
+    d_rgb = torch.from_numpy(rgb).cuda()
+    d_scrib = torch.from_numpy(scrib).cuda()
+    bs = gcfg.BatchSolver(32, scrib.size)
+    ref = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
+    for extra in ({}, {"push_only": 1}, {"blocks_per_sm": 1}, {"max_tile_sweeps": 128, "sweeps_per_local_relabel": 2}):
+        bs.set_solver(threads_y=threads_y, **extra)
+        got = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
+        assert np.array_equal(got[0], ref[0])
+        assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2])
+    ps = bs.phase_split(Ws, Hs, lams, d_rgb, d_scrib)
+    assert ps["push_tiles"] >= 1 and ps["grid_blocks"] >= 1
+    with pytest.raises(gcfg.GcfgError):
+        bs.set_solver(threads_y=5)
+    bs.close()
+
+
+def test_autotuner_reports_the_block_shape():
+    Ws, Hs, lams, rgb, scrib = _batch(12, 3600)
+    d_rgb = torch.from_numpy(rgb).cuda()
+    d_scrib = torch.from_numpy(scrib).cuda()
+    bs = gcfg.BatchSolver(16, scrib.size)
+    ref = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
+    t = bs.autotune(Ws, Hs, lams, d_rgb, d_scrib, reps=1)
+    assert t["threads_y"] in (4, 8, 16) and t["tile_w"] == 32 and t["tile_h"] == 32
+    assert t["configs_tried"] >= 10
+    got = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2])
+    bs.close()
