@@ -405,6 +405,20 @@ def serve_bench(torch, gcfg, n_req=1200, rate=500.0, lanes=2, cap=60 << 30, seed
     lat = done - tarr
     svc = np.array([r["t_done"] - r["t_start"] for r in res])
     is_edit = np.array([q["kind"] == "edit" for q in reqs])
+    side_of = np.array([sides[i] for i in img_of])
+    qwait = np.array([r["t_start"] for r in res]) - tarr
+    slow = sorted(np.nonzero(is_edit)[0], key=lambda k: -lat[k])[:6]
+    edit_tail = {"p50_queue_ms": round(float(np.percentile(qwait[is_edit], 50)) * 1e3, 3),
+                 "p99_queue_ms": round(float(np.percentile(qwait[is_edit], 99)) * 1e3, 3),
+                 "p50_service_ms": round(float(np.percentile(svc[is_edit], 50)) * 1e3, 3),
+                 "p99_service_ms": round(float(np.percentile(svc[is_edit], 99)) * 1e3, 3),
+                 "p99_by_side_ms": {int(sd): round(float(np.percentile(lat[is_edit & (side_of == sd)], 99)) * 1e3, 3)
+                                    for sd in sorted(set(side_of[is_edit].tolist()))},
+                 "slowest": [{"side": int(side_of[k]), "latency_ms": round(float(lat[k]) * 1e3, 3),
+                              "queue_ms": round(float(qwait[k]) * 1e3, 3),
+                              "service_ms": round(float(svc[k]) * 1e3, 3),
+                              "batch_images": int(res[k]["batch_images"]), "lane": int(res[k]["lane"])}
+                             for k in slow]}
     res_sat, tarr_sat, st_sat, dig_sat = served(False)
     make_sat = max(r["t_done"] for r in res_sat) - tarr_sat[0]
 
@@ -446,6 +460,7 @@ def serve_bench(torch, gcfg, n_req=1200, rate=500.0, lanes=2, cap=60 << 30, seed
     seg.close()
     dig_plain = [digest(k, f) for k, f in enumerate(dig_plain)]
     p_lat = np.array(p_lat)
+    p_svc = np.array(p_svc)
     p_span = max(p_done) - reqs[0]["t"]
 
     def ms(a, p):
@@ -465,7 +480,8 @@ def serve_bench(torch, gcfg, n_req=1200, rate=500.0, lanes=2, cap=60 << 30, seed
                    "mean_service_ms": float(np.mean(svc)) * 1e3,
                    "batches": st["batches"], "mean_batch_images": len(reqs) / max(st["batches"], 1),
                    "lane_overlap_frac": round(_lane_overlap(res), 4),
-                   "resident_gb_at_end": st["bytes_in_use"] / 2 ** 30, "evicted": st["evicted"]},
+                   "resident_gb_at_end": st["bytes_in_use"] / 2 ** 30, "evicted": st["evicted"],
+                   "edit_tail": edit_tail},
         "served_saturated": {"mpixel_s": total_px / make_sat / 1e6, "makespan_ms": make_sat * 1e3,
                              "batches": st_sat["batches"]},
         "plain_cold_loop": {"p50_ms": ms(p_lat, 50), "p99_ms": ms(p_lat, 99),
@@ -473,7 +489,11 @@ def serve_bench(torch, gcfg, n_req=1200, rate=500.0, lanes=2, cap=60 << 30, seed
                             "p50_edit_ms": ms(p_lat[is_edit], 50), "p99_edit_ms": ms(p_lat[is_edit], 99),
                             "mpixel_s_over_span": total_px / p_span / 1e6,
                             "mpixel_s_over_busy": total_px / float(np.sum(p_svc)) / 1e6,
-                            "mean_service_ms": float(np.mean(p_svc)) * 1e3},
+                            "mean_service_ms": float(np.mean(p_svc)) * 1e3,
+                            "p99_edit_service_ms": round(float(np.percentile(p_svc[is_edit], 99)) * 1e3, 3),
+                            "p99_edit_by_side_ms": {int(sd): round(float(np.percentile(
+                                p_lat[is_edit & (side_of == sd)], 99)) * 1e3, 3)
+                                for sd in sorted(set(side_of[is_edit].tolist()))}},
         "throughput_note": "mpixel_s_over_span = all pixels / (last completion - first arrival): at 500 req/s the "
                            "arrival rate bounds it for both; mpixel_s_over_busy = all pixels / the time the GPU "
                            "side was busy (union of the lanes' batch intervals; the plain loop's summed service "
