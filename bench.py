@@ -1201,7 +1201,7 @@ def main():
                        for k in ("global_relabels", "closure_checks", "closure_ends", "gr_sweeps", "push_rounds",
                                  "cut_sweeps", "push_tiles",
                                  "gr_tiles", "reach_tiles", "push_sweeps", "push_local_relabels",
-                                 "t_global_relabel_ms", "t_count_ms", "t_push_ms", "t_reach_ms",
+                                 "t_global_relabel_ms", "t_count_ms", "t_push_ms", "t_push_tail_ms", "t_reach_ms",
                                  "cyc_load", "cyc_local_relabel", "cyc_sweeps", "cyc_writeback",
                                  "cyc_take", "bfs_iters_push", "bfs_iters_gr", "cyc_global_relabel")}}
     if plain is not None:

@@ -1178,9 +1178,16 @@ __global__ void __launch_bounds__(NW * 32, solve_min_blocks<NW>()) k_solve(Batch
                     if (idx >= n) break;
                     push_tile(b, b.lists[(size_t)slot * b.list_cap + idx], prm, p, sm.p, st, &ctl->take[slot]);
                 }
+                // the phase's tail: from the first block out of work to the barrier
+                if (threadIdx.x == 0) atomicMax(&ctl->push_idle[p & 1], ~gtimer());
+                if (gtid == 0) ctl->push_idle[(p + 1) & 1] = 0;  // last read after the previous phase
                 __syncthreads();
                 if (!grid_sync(b, 1u << slot)) return;
-                if (gtid == 0) ctl->push_phases++;
+                if (gtid == 0) {
+                    ctl->push_phases++;
+                    const unsigned long long idle = *(volatile unsigned long long *)&ctl->push_idle[p & 1];
+                    if (idle) ctl->t_push_tail += gtimer() - ~idle;
+                }
                 if (vload(&ctl->size[(p + 1) % 3]) == 0 && vload(&ctl->size[(p + 2) % 3]) == 0) {
                     more = false;
                     break;

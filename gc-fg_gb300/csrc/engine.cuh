@@ -70,6 +70,10 @@ struct Ctl {
     // tile-BFS loop iterations (levels and halo jumps) of push and global-
     // relabel visits, and SM cycles summed over global-relabel visits
     unsigned long long bfs_it_push, bfs_it_gr, cyc_gr;
+    // push phases' tail: per phase (by parity) the earliest time a block ran
+    // out of work, stored bit-inverted so that 0 means none and atomicMax
+    // keeps the earliest; t_push_tail sums (phase end - earliest idle)
+    unsigned long long push_idle[2], t_push_tail;
 };
 
 struct Batch {

@@ -526,6 +526,7 @@ struct Engine {
         r->t_count_ms = h_ctl->t_count * 1e-6f;
         r->t_push_ms = h_ctl->t_push * 1e-6f;
         r->t_reach_ms = h_ctl->t_reach * 1e-6f;
+        r->t_push_tail_ms = h_ctl->t_push_tail * 1e-6f;
         r->cyc_load = (long long)h_ctl->cyc_load;
         r->cyc_local_relabel = (long long)h_ctl->cyc_bfs;
         r->cyc_sweeps = (long long)h_ctl->cyc_sweep;

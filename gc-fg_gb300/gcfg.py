@@ -63,12 +63,12 @@ class Result(C.Structure):
                 ("push_local_relabels", C.c_int64), ("t_global_relabel_ms", C.c_float),
                 ("t_count_ms", C.c_float), ("t_push_ms", C.c_float), ("t_reach_ms", C.c_float),
                 ("cyc_load", C.c_int64), ("cyc_local_relabel", C.c_int64), ("cyc_sweeps", C.c_int64),
-                ("cyc_writeback", C.c_int64), ("cyc_take", C.c_int64), ("ms", C.c_float), ("pad_", C.c_float),
+                ("cyc_writeback", C.c_int64), ("cyc_take", C.c_int64), ("ms", C.c_float), ("t_push_tail_ms", C.c_float),
                 ("bfs_iters_push", C.c_int64), ("bfs_iters_gr", C.c_int64), ("cyc_global_relabel", C.c_int64),
                 ("closure_checks", C.c_int32), ("closure_ends", C.c_int32)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad_"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Tuning(C.Structure):

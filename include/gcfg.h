@@ -65,7 +65,7 @@ typedef struct {
      * relabel, sweeps, write-back + hand-over, queue take) */
     int64_t cyc_load, cyc_local_relabel, cyc_sweeps, cyc_writeback, cyc_take;
     float ms;                /* device time of the solve (CUDA events) */
-    float pad_;
+    float t_push_tail_ms;    /* push phases' tails: from the first solver block out of work to the phase's end */
     /* tile-BFS loop iterations summed over push visits' local relabels and
      * over global-relabel visits; SM cycles summed over global-relabel visits */
     int64_t bfs_iters_push, bfs_iters_gr, cyc_global_relabel;
