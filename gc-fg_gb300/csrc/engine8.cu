@@ -463,9 +463,11 @@ __global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
         }
         if (gtid == 0) c->global_relabels++;
         // ---- count: excess that can still reach the sink ----
-        unsigned long long act = 0;
+        // one atomic per warp: per-thread atomics on one address serialise in L2
+        unsigned act = 0;
         for (long long i = gtid; i < g.n; i += nth) act += g.e[i] > 0 && g.h[i] < INF_H;
-        if (act) atomicAdd(&c->active, act);
+        act = __reduce_add_sync(0xffffffffu, act);
+        if ((threadIdx.x & 31) == 0 && act) atomicAdd(&c->active, (unsigned long long)act);
         if (!sync8(c)) return;
         if (*(volatile unsigned long long *)&c->active == 0) {
             finished = true;
@@ -503,7 +505,9 @@ __global__ void __launch_bounds__(256) k8_solve(G8 g, P8 prm) {
         if (e > 0) pos += (unsigned)e;
         g.mark[i] = e > 0;
     }
-    if (pos) atomicAdd(&c->pos_excess, pos);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) pos += __shfl_down_sync(0xffffffffu, pos, o);
+    if ((threadIdx.x & 31) == 0 && pos) atomicAdd(&c->pos_excess, pos);
     if (!sync8(c)) return;
     if (*(volatile unsigned long long *)&c->pos_excess == 0) return;  // nothing marked: S_min is empty
     for (int q = 0;; ++q) {
