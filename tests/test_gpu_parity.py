@@ -375,3 +375,48 @@ def test_nlinks_bit_exact_random_colours(seed, lam):
     gcfg.nlinks(dev(rgb), W, H, lam, *outs)
     for a, b in zip(outs, O.nlinks(rgb, lam)):
         assert np.array_equal(a.cpu().numpy(), b)
+
+
+def _serving_edit(k):
+    """Image and scribbles of request k of the serving trace (seed 4): the
+    edited session's pool image with every edit up to and including k."""
+    import synth
+    pool_specs, reqs = synth.serve_trace(1200, 500.0, 4)
+    news = [q["img"] for q in reqs if q["kind"] == "new"]
+    target = reqs[k]["target"]
+    _, side, _, seed = pool_specs[news[target]]
+    rgb, scrib = synth.generate(4, side, side, seed)
+    scrib = scrib.copy()
+    for q in reqs[:k + 1]:
+        if q["kind"] == "edit" and q["target"] == target:
+            scrib[q["y"]:q["y"] + q["size"], q["x"]:q["x"] + q["size"]] = q["cls"]
+    return rgb, scrib
+
+
+@pytest.mark.parametrize("k", [45, 490])
+def test_hard_serving_edits_vs_oracle(k):
+    """The two slowest solves of the serving trace (15x15 edits of one 1024^2
+    pool image: about ten global relabels and forty push colour phases each)
+    are exact under the default settings and under the settings the
+    autotuner picks for them (32 x 16 block, push-only sweeps, one block per
+    SM)."""
+    rgb, scrib = _serving_edit(k)
+    o = O.segment(rgb, scrib, 50.0)
+    smin, smax, res = gpu_segment(rgb, scrib, 50.0)
+    assert res["global_relabels"] >= 5
+    assert res["flow"] == o["flow"]
+    assert np.array_equal(smin, o["smin"]) and np.array_equal(smax, o["smax"])
+    H, W = scrib.shape
+    bs = gcfg.BatchSolver(1, W * H)
+    Wa = np.array([W], np.int32)
+    d_rgb, d_scrib = dev(rgb.reshape(-1)), dev(scrib.reshape(-1))
+    for kw in ({}, {"threads_y": 16, "push_rounds_per_gr": 4, "sweeps_per_local_relabel": 16, "blocks_per_sm": 1,
+                    "push_only": 1}):
+        bs.set_solver(**kw)
+        d_min = torch.empty(W * H, dtype=torch.uint8, device="cuda")
+        d_max = torch.empty(W * H, dtype=torch.uint8, device="cuda")
+        flows, _ = bs.run(Wa, Wa, np.array([50.0]), d_rgb, d_scrib, d_min, d_max)
+        assert flows[0] == o["flow"]
+        assert np.array_equal(d_min.cpu().numpy().reshape(H, W), o["smin"])
+        assert np.array_equal(d_max.cpu().numpy().reshape(H, W), o["smax"])
+    bs.close()
