@@ -31,6 +31,7 @@
 #include <cstring>
 #include <vector>
 
+#include "dataterm.cuh"  // CHUNK_PX: the data-term pass's chunks, reused by k_extract_rows
 #include "engine.cuh"
 
 namespace gcfg {
@@ -1315,6 +1316,80 @@ __global__ void __launch_bounds__(TILE_THREADS) k_extract(Batch b, uint8_t *smin
     }
 }
 
+// The same cuts written row-major by output windows: block = one chunk of
+// an image (CHUNK_PX consecutive pixels, the data-term pass's chunk map),
+// thread = one 16-byte window of the output arrays, aligned on the arrays'
+// addresses (smin and smax share their alignment mod 16).  A window takes
+// its bits from the row mask words of the tiles it covers, one row segment
+// at a time (one or two segments when W >= 16), spreads them to 16 bytes
+// and writes each cut with one 16-byte store; a window that reaches past
+// the chunk writes only the chunk's bytes, one at a time.
+__device__ __forceinline__ uint32_t spread4(uint32_t nib) { return (nib * 0x00204081u) & 0x01010101u; }
+__device__ __forceinline__ uint4 spread16(uint32_t bits) {
+    return make_uint4(spread4(bits & 15u), spread4((bits >> 4) & 15u), spread4((bits >> 8) & 15u),
+                      spread4((bits >> 12) & 15u));
+}
+
+__global__ void __launch_bounds__(256) k_extract_rows(Batch b, const int2 *__restrict__ chunk_map, uint8_t *smin,
+                                                      uint8_t *smax) {
+    __shared__ long long s_row0;
+    const int2 cm = __ldg(chunk_map + blockIdx.x);
+    const int W = __ldg(&b.img[cm.x].W), H = __ldg(&b.img[cm.x].H);
+    const int tile0 = __ldg(&b.img[cm.x].tile0), tiles_x = __ldg(&b.img[cm.x].tiles_x);
+    const long long out0 = __ldg(&b.img[cm.x].out0);
+    const long long npx = (long long)W * H;
+    const long long lo = (long long)cm.y * CHUNK_PX, hi = min(npx, lo + CHUNK_PX);  // the chunk's pixels
+    if (threadIdx.x == 0) s_row0 = lo / W;  // the chunk's first row
+    __syncthreads();
+    const long long row0 = s_row0;
+    const int xlo = (int)(lo - row0 * W);
+    uint8_t *ref = smax ? smax : smin;
+    const uintptr_t abase = (uintptr_t)(ref + out0);  // address of the image's pixel 0
+    const uintptr_t a0 = (abase + (uintptr_t)lo) & ~(uintptr_t)15;
+    const int lead = (int)(abase + (uintptr_t)lo - a0);  // pixels of window 0 before the chunk
+    const int nwin = (lead + (int)(hi - lo) + 15) >> 4;
+    for (int w = threadIdx.x; w < nwin; w += blockDim.x) {
+        const int q0 = 16 * w - lead;  // the window's first pixel, relative to lo
+        const int s = max(q0, 0), e = min(q0 + 16, (int)(hi - lo));
+        // row and column of pixel lo + s
+        const unsigned xr = (unsigned)(xlo + s);
+        int y = (int)(row0 + xr / (unsigned)W), x = (int)(xr % (unsigned)W);
+        unsigned rb = 0, mb = 0;  // reach bits, smax bits; bit j = pixel q0 + j
+        for (int pos = s, it = 0; pos < e && it < 16; ++it) {
+            const int len = min(e - pos, W - x);
+            const int sh = x & 31, r = y & 31;
+            const size_t t = (size_t)tile0 + (size_t)(y >> 5) * tiles_x + (x >> 5);
+            const unsigned f0 = __ldg(b.hfin + t * 32 + r), r0 = __ldg(b.reach + t * 32 + r);
+            unsigned f1 = 0, r1 = 0;
+            if (sh + len > 32) {  // the segment reaches into the next tile of the row
+                f1 = __ldg(b.hfin + (t + 1) * 32 + r);
+                r1 = __ldg(b.reach + (t + 1) * 32 + r);
+            }
+            const unsigned keep = len >= 32 ? 0xFFFFFFFFu : (1u << len) - 1u;
+            // interior pixels: not on row 0 or H - 1, not at x = 0 or W - 1
+            unsigned in = (y > 0 && y < H - 1) ? keep : 0u;
+            if (x == 0) in &= ~1u;
+            if (x + len == W) in &= ~(1u << (len - 1));
+            const int at = pos - q0;
+            rb |= (__funnelshift_r(r0, r1, sh) & keep) << at;
+            mb |= (~__funnelshift_r(f0, f1, sh) & in) << at;
+            pos += len;
+            x = 0;
+            ++y;
+        }
+        const size_t o = (size_t)(out0 + lo + q0);
+        if (s == q0 && e == q0 + 16) {
+            if (smin) *reinterpret_cast<uint4 *>(smin + o) = spread16(rb);
+            if (smax) *reinterpret_cast<uint4 *>(smax + o) = spread16(mb);
+        } else {
+            for (int j = s - q0; j < e - q0; ++j) {
+                if (smin) smin[o + j] = (uint8_t)((rb >> j) & 1u);
+                if (smax) smax[o + j] = (uint8_t)((mb >> j) & 1u);
+            }
+        }
+    }
+}
+
 }  // namespace gcfg
 
 namespace gcfg {
@@ -1392,6 +1467,18 @@ gcfg_status launch_build_arrays(const Batch &b, const int *dp, const int *dn, in
                                 const int *down, const int *left, const int *right, cudaStream_t st) {
     GCFG_LAUNCH(GCFG_PK_BUILD, st,
                 k_build_arrays<<<batch_ntiles(b), TILE_THREADS, 0, st>>>(b, dp, dn, penalty, up, down, left, right));
+    GCFG_CK(cudaGetLastError());
+    return GCFG_OK;
+}
+
+gcfg_status launch_extract_rows(const Batch &b, const int2 *chunk_map, long long n_chunks, uint8_t *smin,
+                               uint8_t *smax, cudaStream_t st) {
+    if ((!smin && !smax) || n_chunks <= 0) return GCFG_OK;
+    if (smin && smax && (((uintptr_t)smin ^ (uintptr_t)smax) & 15)) {
+        // the windows need one alignment for both arrays: the tile-major kernel instead
+        return launch_extract(b, smin, smax, nullptr, st);
+    }
+    GCFG_LAUNCH(GCFG_PK_EXTRACT, st, k_extract_rows<<<(unsigned)n_chunks, 256, 0, st>>>(b, chunk_map, smin, smax));
     GCFG_CK(cudaGetLastError());
     return GCFG_OK;
 }

@@ -163,6 +163,10 @@ gcfg_status launch_solve(const Batch &b, const SolveParams &prm, int n_tiles, cu
 gcfg_status launch_build_arrays(const Batch &b, const int *dp, const int *dn, int penalty, const int *up,
                                 const int *down, const int *left, const int *right, cudaStream_t st);
 gcfg_status launch_extract(const Batch &b, uint8_t *smin, uint8_t *smax, int *label, cudaStream_t st);
+// The cuts of the images of a chunk map (the data-term pass's blocks: CHUNK_PX
+// consecutive pixels of one image each), written by aligned 16-byte windows.
+gcfg_status launch_extract_rows(const Batch &b, const int2 *chunk_map, long long n_chunks, uint8_t *smin,
+                               uint8_t *smax, cudaStream_t st);
 
 }  // namespace gcfg
 

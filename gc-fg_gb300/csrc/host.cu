@@ -762,7 +762,7 @@ static gcfg_status run_batch_eager(Engine &e, int n, const int *W, const int *H,
     GCFG_TRY(e.solve());
     uint8_t *dmin = staging ? (smin ? e.d_smin : nullptr) : smin;
     uint8_t *dmax = staging ? (smax ? e.d_smax : nullptr) : smax;
-    if (dmin || dmax) GCFG_TRY(launch_extract(e.batch(), dmin, dmax, nullptr, e.st));
+    if (dmin || dmax) GCFG_TRY(launch_extract_rows(e.batch(), e.d_cmap, e.total_chunks, dmin, dmax, e.st));
     if (staging) {
         if (smin) GCFG_CK(cudaMemcpyAsync(smin, e.d_smin, (size_t)e.n_px, cudaMemcpyDeviceToHost, e.st));
         if (smax) GCFG_CK(cudaMemcpyAsync(smax, e.d_smax, (size_t)e.n_px, cudaMemcpyDeviceToHost, e.st));
@@ -832,7 +832,8 @@ static gcfg_status graph_for(Engine &e, int n, const int *W, const int *H, const
             // the state read-back first: a label download queued after the
             // graph must not hold it up on the copy engine
             if (rc == GCFG_OK) rc = e.readback();
-            if (rc == GCFG_OK && (dmin || dmax)) rc = launch_extract(e.batch(), dmin, dmax, nullptr, e.st);
+            if (rc == GCFG_OK && (dmin || dmax))
+                rc = launch_extract_rows(e.batch(), e.d_cmap, e.total_chunks, dmin, dmax, e.st);
             if (cudaStreamEndCapture(e.cap_st, &g) != cudaSuccess && rc == GCFG_OK) rc = GCFG_ERR_CUDA;
         }
         e.st = user;
@@ -957,11 +958,9 @@ static gcfg_status stage_build(Engine &e) {
 static gcfg_status stage_extract(Engine &e, uint8_t *h_smin, uint8_t *h_smax, cudaStream_t out_st) {
     for (int g = 0; g < (int)e.groups.size(); ++g) {
         const Engine::Group &gr = e.groups[g];
-        Batch b = e.batch();
-        b.tlist = e.d_iota + gr.t0;
-        b.n_tlist = gr.t1 - gr.t0;
         if (h_smin || h_smax)
-            GCFG_TRY(launch_extract(b, h_smin ? e.d_smin : nullptr, h_smax ? e.d_smax : nullptr, nullptr, e.st));
+            GCFG_TRY(launch_extract_rows(e.batch(), e.d_cmap + gr.c0, gr.c1 - gr.c0, h_smin ? e.d_smin : nullptr,
+                                         h_smax ? e.d_smax : nullptr, e.st));
         GCFG_CK(cudaEventRecord(e.ev_out[g], e.st));
         GCFG_CK(cudaStreamWaitEvent(out_st, e.ev_out[g], 0));
         const size_t np = (size_t)(gr.p1 - gr.p0);
@@ -1060,7 +1059,8 @@ static gcfg_status submit_staged(Engine &e, Engine::Flight &f, int slot, int n, 
     // download is queued: behind it on the copy engine it would stall st
     GCFG_TRY(e.readback());
     if (h_smin || h_smax)
-        GCFG_TRY(launch_extract(e.batch(), h_smin ? e.d_smin : nullptr, h_smax ? e.d_smax : nullptr, nullptr, e.st));
+        GCFG_TRY(launch_extract_rows(e.batch(), e.d_cmap, e.total_chunks, h_smin ? e.d_smin : nullptr,
+                                     h_smax ? e.d_smax : nullptr, e.st));
     GCFG_CK(cudaEventRecord(f.ev_ext, e.st));
     GCFG_CK(cudaStreamWaitEvent(e.dn_st, f.ev_ext, 0));
     if (h_smin) GCFG_CK(cudaMemcpyAsync(h_smin, e.d_smin, (size_t)e.n_px, cudaMemcpyDeviceToHost, e.dn_st));

@@ -421,7 +421,7 @@ gcfg_status run_batch(Lane &L, std::vector<Req> &batch, const std::vector<Sessio
     GCFG_CK(cudaMemsetAsync(L.ctl, 0, sizeof(Ctl), st));
     SolveParams prm = kDefaultSolveParams;
     GCFG_TRY(launch_solve(b, prm, nt, st, s.cfg.lanes > 1 ? solve_grid_blocks(1 << 30) / s.cfg.lanes : 0));
-    GCFG_TRY(launch_extract(b, s.smin, s.smax, nullptr, st));
+    GCFG_TRY(launch_extract_rows(b, L.d_cmap, ch, s.smin, s.smax, st));
     for (int k = 0; k < n; ++k) {
         const Session &x = snap[k];
         const size_t npx = (size_t)x.W * x.H;
