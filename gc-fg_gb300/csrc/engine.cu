@@ -982,10 +982,11 @@ __device__ __noinline__ int closure_check(const Batch &b, const SolveParams &prm
 
 // The block is NW warps over one 32x32 tile (thread block 32 x NW, the
 // reference's THREADS_X x THREADS_Y, GraphCut.h:39-53).  Blocks per SM the
-// register budget is set for: 8 warps 4 and 16 warps 2 (64 registers per
-// thread); 4 warps 6, the most its shared memory allows (80 registers, the
-// 8 rows per thread need them).  The phases' shared memory (union Smem<NW>)
-// is dynamic: above 48 KB for 16 warps.
+// register budget is set for: 8 warps 4, 16 warps 2 and 32 warps 1 (64
+// registers per thread); 4 warps 6, the most its shared memory allows (80
+// registers, the 8 rows per thread need them).  The phases' shared memory
+// (union Smem<NW>) is dynamic: above 48 KB for 16 and 32 warps (132 KB for
+// 32, the global relabel's per-warp level arrays).
 template <int NW>
 constexpr int solve_min_blocks() { return NW == 4 ? 6 : 32 / NW; }
 
@@ -1396,7 +1397,7 @@ namespace gcfg {
 
 namespace {
 
-// The solver kernel of a block shape (warps per block: 4, 8 or 16) and its
+// The solver kernel of a block shape (warps per block: 4, 8, 16 or 32) and its
 // dynamic shared memory.
 struct SolveKernel {
     const void *fn;
@@ -1407,11 +1408,12 @@ SolveKernel solve_kernel(int warps) {
     switch (warps) {
         case 4: return {(const void *)k_solve<4>, sizeof(Smem<4>)};
         case 16: return {(const void *)k_solve<16>, sizeof(Smem<16>)};
+        case 32: return {(const void *)k_solve<32>, sizeof(Smem<32>)};
         default: return {(const void *)k_solve<8>, sizeof(Smem<8>)};
     }
 }
 
-int shape_index(int warps) { return warps == 4 ? 0 : warps == 16 ? 2 : 1; }
+int shape_index(int warps) { return warps == 4 ? 0 : warps == 16 ? 2 : warps == 32 ? 3 : 1; }
 
 // Co-resident blocks of the solver kernel of a shape on the current device,
 // computed once per device ordinal and shape (the kernel's dynamic
@@ -1420,7 +1422,7 @@ int shape_index(int warps) { return warps == 4 ? 0 : warps == 16 ? 2 : 1; }
 // store the same value.
 int resident_blocks(int warps) {
     constexpr int MAX_DEV = 64;
-    static std::atomic<int> cached[MAX_DEV][3];
+    static std::atomic<int> cached[MAX_DEV][4];
     int dev = 0;
     cudaGetDevice(&dev);
     const bool slot = dev >= 0 && dev < MAX_DEV;
@@ -1450,7 +1452,7 @@ int solve_grid_blocks(int n_tiles, int max_grid, int warps) {
 }
 
 gcfg_status launch_solve(const Batch &b, const SolveParams &prm, int n_tiles, cudaStream_t st, int max_grid) {
-    const int warps = prm.warps == 4 || prm.warps == 16 ? prm.warps : 8;
+    const int warps = prm.warps == 4 || prm.warps == 16 || prm.warps == 32 ? prm.warps : 8;
     const int grid = solve_grid_blocks(n_tiles, max_grid, warps);
     const SolveKernel k = solve_kernel(warps);
     Batch bb = b;

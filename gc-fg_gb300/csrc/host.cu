@@ -1197,7 +1197,8 @@ gcfg_status gcfg_batch_set_solver(gcfg_batch *b, const gcfg_tuning *t) {
     if (!b || !t || t->push_rounds_per_gr < 1 || t->max_tile_sweeps < 1 || t->sweeps_per_local_relabel < 1 ||
         t->blocks_per_sm < 0 || (t->local_relabel_first != 0 && t->local_relabel_first != 1) ||
         (t->push_only != 0 && t->push_only != 1) ||
-        (t->threads_y != 0 && t->threads_y != 4 && t->threads_y != 8 && t->threads_y != 16))
+        (t->threads_y != 0 && t->threads_y != 4 && t->threads_y != 8 && t->threads_y != 16 &&
+         t->threads_y != 32))
         return GCFG_ERR_INVALID;
     int dev = 0, sms = 1;
     GCFG_CK(cudaGetDevice(&dev));
@@ -1268,7 +1269,7 @@ gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const i
         return GCFG_OK;
     };
     SolveParams cur = e.prm;
-    if (cur.warps != 4 && cur.warps != 16) cur.warps = 8;
+    if (cur.warps != 4 && cur.warps != 16 && cur.warps != 32) cur.warps = 8;
     int cur_bps = e.max_grid > 0 ? (e.max_grid + sms - 1) / sms : per_sm_of(cur.warps);
     if (cur_bps > per_sm_of(cur.warps)) cur_bps = per_sm_of(cur.warps);
     float ms_default = 0.f;
@@ -1278,13 +1279,13 @@ gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const i
     // Coordinate search: the block shape (warps per block, at the shape's
     // full occupancy), push rounds per global relabel, sweeps per visit,
     // sweeps between local relabels, blocks per SM, relabel-first, push-only.
-    static const int c_warps[] = {4, 8, 16};
+    static const int c_warps[] = {4, 8, 16, 32};
     static const int c_push[] = {2, 4, 8, 16};
     static const int c_sweeps[] = {16, 24, 32, 64, 128};
     static const int c_bfs[] = {2, 4, 8, 16, 32};
     for (int pass = 0; pass < 2 && rc == GCFG_OK; ++pass) {
         for (int which = 0; which < 7 && rc == GCFG_OK; ++which) {
-            const int nc = which == 0 ? 3 : which == 1 ? 4 : which == 2 || which == 3 ? 5
+            const int nc = which == 0 ? 4 : which == 1 ? 4 : which == 2 || which == 3 ? 5
                          : which == 4 ? per_sm_of(cur.warps) : 2;
             for (int c = 0; c < nc && rc == GCFG_OK; ++c) {
                 SolveParams p = cur;
