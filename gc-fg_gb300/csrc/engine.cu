@@ -264,46 +264,53 @@ __device__ unsigned tile_bfs(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd,
 
 // The push visits' exact local relabel: the same levels as tile_bfs, but
 // instead of storing each new pixel's level on the spot (a divergent loop on
-// the loop-carried path of a single warp) the k-th expansion that grows the
-// frontier records the reached rows srec[k][row] and its level lv[k], while
-// two more records fit (k < NREC); later expansions store their pixels'
-// levels directly, as tile_bfs does.  sfin gets the final reached rows.
-// Returns the number of records (warp-uniform); the whole block then fills in
-// the heights (heights_from_records).
-constexpr int NREC = 48;
+// the loop-carried path of a single warp) every expansion records the reached
+// rows, srec[row * NRS + k], and its level lv[k], while four more records
+// fit (k + 4 <= NREC); later expansions store their pixels' levels directly,
+// as tile_bfs does.  sfin gets the final reached rows.  Four expansions
+// (levels lvl + 1 .. lvl + 4, each from the previous one's result) share one
+// vote and one branch, so the loop-carried path holds one vote per four
+// levels; a level that adds nothing is recorded all the same (its record
+// repeats the previous set, which the records' search tolerates).  When none
+// of the four grows the frontier, the level jumps to the next halo level
+// above lvl + 3.  Returns the number of records (warp-uniform); the whole
+// block then fills in the heights (height_from_records).
+constexpr int NREC = 64;
+constexpr int NRS = NREC + 1;  // odd row stride: a warp's record stores and searches spread over the banks
 __device__ int tile_bfs_rec(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd, unsigned sink, int hl, int hr,
-                            int ht, int hb, int *hs, int stride, unsigned (*srec)[32], int *lv, unsigned *sfin,
+                            int ht, int hb, int *hs, int stride, unsigned *srec, int *lv, unsigned *sfin,
                             int *iters) {
     const int lane = threadIdx.x & 31;
     int *row = hs + lane * stride;
+    unsigned *rec = srec + lane * NRS;
     unsigned S = sink;
     int lvl = 1, nrec = 0, it = 0;
     for (; it < BFS_MAX_ITERS; ++it) {
         const unsigned nw1 = bfs_expand(S, lvl, Rl, Rr, Ru, Rd, hl, hr, ht, hb, lane);
         const unsigned S1 = S | nw1;
         const unsigned nw2 = bfs_expand(S1, lvl + 1, Rl, Rr, Ru, Rd, hl, hr, ht, hb, lane);
-        const bool a1 = __any_sync(FULL, nw1 != 0);
-        const bool a2 = __any_sync(FULL, nw2 != 0);
-        if (a1 || a2) {
-            S = S1 | nw2;
-            if (nrec + 2 <= NREC) {  // the usual case: both levels recorded
-                if (a1) {
-                    srec[nrec][lane] = S1;
-                    if (lane == 0) lv[nrec] = lvl + 1;
-                    ++nrec;
-                }
-                if (a2) {
-                    srec[nrec][lane] = S;
-                    if (lane == 0) lv[nrec] = lvl + 2;
-                    ++nrec;
-                }
+        const unsigned S2 = S1 | nw2;
+        const unsigned nw3 = bfs_expand(S2, lvl + 2, Rl, Rr, Ru, Rd, hl, hr, ht, hb, lane);
+        const unsigned S3 = S2 | nw3;
+        const unsigned nw4 = bfs_expand(S3, lvl + 3, Rl, Rr, Ru, Rd, hl, hr, ht, hb, lane);
+        if (__any_sync(FULL, (nw1 | nw2 | nw3 | nw4) != 0)) {
+            S = S3 | nw4;
+            if (nrec + 4 <= NREC) {  // the usual case: the four levels recorded
+                rec[nrec] = S1;
+                rec[nrec + 1] = S2;
+                rec[nrec + 2] = S3;
+                rec[nrec + 3] = S;
+                if (lane < 4) lv[nrec + lane] = lvl + 1 + lane;
+                nrec += 4;
             } else {
                 for (unsigned m = nw1; m; m &= m - 1) row[__ffs(m) - 1] = lvl + 1;
                 for (unsigned m = nw2; m; m &= m - 1) row[__ffs(m) - 1] = lvl + 2;
+                for (unsigned m = nw3; m; m &= m - 1) row[__ffs(m) - 1] = lvl + 3;
+                for (unsigned m = nw4; m; m &= m - 1) row[__ffs(m) - 1] = lvl + 4;
             }
-            lvl += 2;
+            lvl += 4;
         } else {
-            const int nxt = bfs_next_halo(lvl + 1, hl, hr, ht, hb);
+            const int nxt = bfs_next_halo(lvl + 3, hl, hr, ht, hb);
             if (nxt >= INF_H) break;
             lvl = nxt;
         }
@@ -315,20 +322,23 @@ __device__ int tile_bfs_rec(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd, 
 
 // Height of pixel x of row r after tile_bfs_rec: INF outside the final
 // reached set, 1 on the seeds, else the level of the first record that holds
-// it (records are cumulative, so a binary search finds it), else the level
-// stored directly by an expansion past the records.
-__device__ __forceinline__ int height_from_records(int r, int x, unsigned seed, const unsigned (*srec)[32],
+// it, else the level stored directly by an expansion past the records.  The
+// records are cumulative (a set bit stays set), so the first record holding
+// the bit is found by a fixed six-step search with no loop or branch: the
+// four rows a thread fills run their searches side by side.
+__device__ __forceinline__ int height_from_records(int r, int x, unsigned seed, const unsigned *srec,
                                                    const int *lv, const unsigned *sfin, int nrec, int stored) {
-    if (!((sfin[r] >> x) & 1u)) return INF_H;
-    if ((seed >> x) & 1u) return 1;
-    if (nrec == 0 || !((srec[nrec - 1][r] >> x) & 1u)) return stored;
-    int lo = 0, hi = nrec - 1;  // smallest k with the bit set lies in [lo, hi]
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if ((srec[mid][r] >> x) & 1u) hi = mid;
-        else lo = mid + 1;
+    const unsigned *rec = srec + r * NRS;
+    const bool fin = (sfin[r] >> x) & 1u;
+    const bool in_rec = nrec > 0 && ((rec[nrec > 0 ? nrec - 1 : 0] >> x) & 1u);
+    int pos = -1;  // the last record without the bit (-1: none)
+#pragma unroll
+    for (int step = NREC / 2; step >= 1; step >>= 1) {
+        const int q = pos + step;
+        if (q < nrec - 1 && !((rec[q] >> x) & 1u)) pos = q;
     }
-    return lv[lo];
+    const int level = lv[pos + 1];
+    return !fin ? INF_H : ((seed >> x) & 1u) ? 1 : !in_rec ? stored : level;
 }
 
 // ---------------------------------------------------------------------------
@@ -373,7 +383,7 @@ struct SmemPush {
     int h[TILE_H + 2][TILE_W + 2];
     int halo_in[4][32];
     unsigned m[5][32];  // left, right, up, down, sink row masks
-    unsigned srec[NREC][32];  // local relabel: reached rows after each recorded expansion
+    unsigned srec[32 * NRS];  // local relabel: reached rows after each recorded expansion, [row * NRS + k]
     int lv[NREC];             // and its level
     unsigned sfin[32];        // final reached rows
     int nrec;
