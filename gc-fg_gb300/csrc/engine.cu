@@ -1462,7 +1462,7 @@ int solve_grid_blocks(int n_tiles, int max_grid, int warps) {
 }
 
 gcfg_status launch_solve(const Batch &b, const SolveParams &prm, int n_tiles, cudaStream_t st, int max_grid) {
-    const int warps = prm.warps == 4 || prm.warps == 16 || prm.warps == 32 ? prm.warps : 8;
+    const int warps = solve_warps(prm.warps, n_tiles);
     const int grid = solve_grid_blocks(n_tiles, max_grid, warps);
     const SolveKernel k = solve_kernel(warps);
     Batch bb = b;

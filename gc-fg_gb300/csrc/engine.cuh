@@ -124,7 +124,8 @@ struct SolveParams {
     // control block not cleared in between): the push rounds of the first
     // outer iteration, then return.  A split leaves the solve unfinished.
     int phase;
-    int warps;         // warps per block of the solver kernel (block shape 32 x warps over a 32x32 tile): 4, 8 or 16
+    int warps;         // warps per block of the solver kernel (block shape 32 x warps over a 32x32 tile):
+                       // 4, 8, 16 or 32; 0: by the solve's size (solve_warps)
 };
 
 // Default solver settings of every entry point (before any tuning): 2 push
@@ -132,8 +133,20 @@ struct SolveParams {
 // every 4 sweeps.  Measured on single images from 256x256 to 4096x4096 and on
 // the 256-image batch, these are at or near the fastest of the settings tried
 // for every case (4 rounds with 64 sweeps and a local relabel every 16 sweeps
-// took up to 2.9x longer on the 1920x1080 image with lambda 200).
-constexpr SolveParams kDefaultSolveParams{64, 2, 24, 4, 0, 1 << 20, 0, 0, 8};
+// took up to 2.9x longer on the 1920x1080 image with lambda 200).  The block
+// shape goes by the solve's size (solve_warps).
+constexpr SolveParams kDefaultSolveParams{64, 2, 24, 4, 0, 1 << 20, 0, 0, 0};
+
+// The block shape of a solve of n_tiles tiles: the shape asked for, or for 0
+// 32 x 16 up to 2048 tiles (a 1920x1080 image has 2040) and 32 x 8 above.
+// A small solve keeps few tiles busy at once, so its time is the latency of
+// single tile visits, which 16 warps (2 rows each) shorten; a large one keeps
+// every SM busy, where 8 warps at 4 blocks per SM do more per cycle.
+constexpr int kSmallSolveTiles = 2048;
+inline int solve_warps(int warps, int n_tiles) {
+    if (warps == 4 || warps == 8 || warps == 16 || warps == 32) return warps;
+    return n_tiles <= kSmallSolveTiles ? 16 : 8;
+}
 
 __host__ __device__ __forceinline__ int batch_ntiles(const Batch &b) { return b.tlist ? b.n_tlist : b.n_tiles; }
 __device__ __forceinline__ int batch_tile(const Batch &b, int k) { return b.tlist ? __ldg(b.tlist + k) : k; }

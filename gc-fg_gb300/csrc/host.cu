@@ -1208,7 +1208,7 @@ gcfg_status gcfg_batch_set_solver(gcfg_batch *b, const gcfg_tuning *t) {
     b->e.prm.bfs_every = t->sweeps_per_local_relabel;
     b->e.prm.bfs_first = t->local_relabel_first;
     b->e.prm.push_only = t->push_only;
-    b->e.prm.warps = t->threads_y ? t->threads_y : 8;
+    b->e.prm.warps = t->threads_y;  // 0: by the solve's size
     b->e.max_grid = t->blocks_per_sm * sms;  // 0: as many as fit
     return GCFG_OK;
 }
@@ -1269,7 +1269,11 @@ gcfg_status gcfg_batch_autotune(gcfg_batch *b, int n, const int *widths, const i
         return GCFG_OK;
     };
     SolveParams cur = e.prm;
-    if (cur.warps != 4 && cur.warps != 16 && cur.warps != 32) cur.warps = 8;
+    {
+        long long tiles = 0;  // the batch's tiles, for the size-chosen block shape
+        for (int i = 0; i < n; ++i) tiles += (long long)((widths[i] + 31) / 32) * ((heights[i] + 31) / 32);
+        cur.warps = solve_warps(cur.warps, (int)(tiles < (1 << 30) ? tiles : (1 << 30)));
+    }
     int cur_bps = e.max_grid > 0 ? (e.max_grid + sms - 1) / sms : per_sm_of(cur.warps);
     if (cur_bps > per_sm_of(cur.warps)) cur_bps = per_sm_of(cur.warps);
     float ms_default = 0.f;
@@ -1381,7 +1385,7 @@ gcfg_status gcfg_batch_phase_split(gcfg_batch *b, int n, const int *widths, cons
         if ((rc = e.fetch()) != GCFG_OK) break;
         c1 = *e.h_ctl;
         if (c1.err) { rc = GCFG_ERR_NOT_CONVERGED; break; }
-        out->grid_blocks = solve_grid_blocks(e.n_tiles, e.max_grid, p.warps);
+        out->grid_blocks = solve_grid_blocks(e.n_tiles, e.max_grid, solve_warps(p.warps, e.n_tiles));
         out->relabel_tiles = (int64_t)c1.gr_tiles;
         out->relabel_rounds = c1.gr_rounds;
         out->active_pixels = (int64_t)c1.total_active;

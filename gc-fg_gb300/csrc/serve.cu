@@ -420,7 +420,9 @@ gcfg_status run_batch(Lane &L, std::vector<Req> &batch, const std::vector<Sessio
     b.n_ilist = n;
     GCFG_CK(cudaMemsetAsync(L.ctl, 0, sizeof(Ctl), st));
     SolveParams prm = kDefaultSolveParams;
-    GCFG_TRY(launch_solve(b, prm, nt, st, s.cfg.lanes > 1 ? solve_grid_blocks(1 << 30) / s.cfg.lanes : 0));
+    prm.warps = solve_warps(prm.warps, nt);  // the lanes share the GPU in blocks of this shape
+    GCFG_TRY(launch_solve(b, prm, nt, st,
+                          s.cfg.lanes > 1 ? solve_grid_blocks(1 << 30, 0, prm.warps) / s.cfg.lanes : 0));
     GCFG_TRY(launch_extract_rows(b, L.d_cmap, ch, s.smin, s.smax, st));
     for (int k = 0; k < n; ++k) {
         const Session &x = snap[k];

@@ -393,9 +393,10 @@ class BatchSolver:
         return {"active": bool(a.value), "captures": c.value, "replays": r.value, "kernels_per_replay": k.value}
 
     def set_solver(self, push_rounds_per_gr=2, max_tile_sweeps=24, sweeps_per_local_relabel=4,
-                   blocks_per_sm=0, local_relabel_first=0, push_only=0, threads_y=8, **_ignored):
+                   blocks_per_sm=0, local_relabel_first=0, push_only=0, threads_y=0, **_ignored):
         """Solver settings (keys as autotune() returns them); threads_y is the
-        solver's block shape 32 x threads_y (4, 8, 16 or 32) over each 32x32 tile."""
+        solver's block shape 32 x threads_y (4, 8, 16 or 32) over each 32x32 tile,
+        0 (the default) by the solve's size: 16 up to 2048 tiles, else 8."""
         t = Tuning(push_rounds_per_gr=int(push_rounds_per_gr), max_tile_sweeps=int(max_tile_sweeps),
                    sweeps_per_local_relabel=int(sweeps_per_local_relabel), blocks_per_sm=int(blocks_per_sm),
                    local_relabel_first=int(local_relabel_first), push_only=int(push_only),

@@ -336,7 +336,8 @@ typedef struct {
     int32_t tile_w, tile_h;           /* data tile of the residual graph (32 x 32, fixed) */
     int32_t local_relabel_first;      /* 1: exact local relabel at the start of every tile visit */
     int32_t push_only;                /* 1: sweeps only push; heights change by exact local relabels */
-    int32_t threads_y;                /* solver block 32 x threads_y: 4, 8, 16 or 32 (0 in gcfg_batch_set_solver: 8) */
+    int32_t threads_y;                /* solver block 32 x threads_y: 4, 8, 16 or 32; 0 in gcfg_batch_set_solver:
+                                         by the solve's size, 16 up to 2048 tiles, else 8 (the default) */
 } gcfg_tuning;
 
 /* Use these solver settings for the following runs (for example the record
