@@ -580,6 +580,7 @@ def solve_phases(gcfg, stream, Ws, Hs, lams, d_rgb, d_scrib, offs, peak, workloa
     tot = {"ms_relabel": 0.0, "ms_push": 0.0, "relabel_tiles": 0, "push_tiles": 0, "push_sweeps": 0,
            "push_local_relabels": 0, "relabel_rounds": 0, "push_phases": 0, "active_pixels": 0, "tiles": 0}
     grid = []
+    timeline = None
     for g in groups:
         w, h, lam = Ws[g], Hs[g], lams[g]
         if batched:
@@ -590,6 +591,11 @@ def solve_phases(gcfg, stream, Ws, Hs, lams, d_rgb, d_scrib, offs, peak, workloa
             rgb, scr = d_rgb[3 * o:3 * (o + n)], d_scrib[o:o + n]
         with nvtx_range("phase_split"):
             ps = bs.phase_split(w, h, lam, rgb, scr)
+        if timeline is None:  # the first launch's relabel, round by round (device clock)
+            timeline = {"round0_us": round(ps["relabel_round0_us"], 2), "pull_check_us": round(ps["relabel_pull_us"], 2),
+                        "frontier_round_us": ps["relabel_front_us"], "frontier_round_tiles": ps["relabel_front_tiles"],
+                        "frontier_round_work_us": ps["relabel_front_work_us"],
+                        "frontier_round_longest_visit_kcyc": ps["relabel_front_maxvisit_kcyc"]}
         for k in tot:
             if k != "tiles":
                 tot[k] += ps[k]
@@ -604,6 +610,7 @@ def solve_phases(gcfg, stream, Ws, Hs, lams, d_rgb, d_scrib, offs, peak, workloa
                       ncu_phase_traffic("gr", workload_name), peak,
                       launches=len(groups), tile_visits=tot["relabel_tiles"], frontier_rounds=tot["relabel_rounds"],
                       tiles=nt)
+    gr["timeline_first_launch"] = timeline
     push = phase_record(tot["ms_push"], 1024 * B_PUSH * tot["push_tiles"], MOVED_PUSH_VISIT * tot["push_tiles"],
                         ncu_phase_traffic("push", workload_name), peak,
                         launches=len(groups), tile_visits=tot["push_tiles"], sweeps=tot["push_sweeps"],
@@ -691,8 +698,9 @@ def tuned_vs_default(gcfg, stream, Ws, Hs, lams, d_rgb, d_scrib, offs, flows, sm
     return {"default_ms": round(t_def, 4), "tuned_ms": round(t_tun, 4), "speedup": round(t_def / t_tun, 3),
             "per_image": out, "results_equal": eq,
             "how": "each image as a batch of one through gcfg_batch_run; best of 5 device times (data term to cuts) "
-                   "under the default settings (32 x 8 solver block, 2 push rounds per global relabel, 24 sweeps, "
-                   "local relabel every 4) and under gcfg_batch_autotune's choice for that image"}
+                   "under the default settings (solver block by size: 32 x 16 up to 2048 tiles, else 32 x 8; 2 push "
+                   "rounds per global relabel, 24 sweeps, local relabel every 4) and under gcfg_batch_autotune's "
+                   "choice for that image"}
 
 
 def plain_leg(torch, gcfg, name, steps, warmup, flush, stream, peak, peak_kind, cpu_budget=10.0, ref_budget=5.0):

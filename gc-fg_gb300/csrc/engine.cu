@@ -223,17 +223,33 @@ __device__ __forceinline__ int bfs_next_halo(int lvl, int hl, int hr, int ht, in
     return __reduce_min_sync(FULL, cand);
 }
 
-// Both BFS loops below take two levels per round (lvl -> lvl + 1 -> lvl + 2,
-// the second expansion from the first's result) and decide once, so the
-// loop-carried path holds one vote and one branch per two levels.  When
-// neither level grows the frontier, the level jumps to the next halo level
-// above lvl + 1; when only the first grows, the next round's expansions at
-// lvl + 2 and lvl + 3 find what a jump would (halo levels <= lvl + 1 have
-// already been used).
+// Both BFS loops below take four levels per round (lvl -> lvl + 1 -> ... ->
+// lvl + 4, each expansion from the previous one's result) and decide once, so
+// the loop-carried path holds one vote and one branch per four levels.  When
+// no level grows the frontier, the level jumps to the next halo level above
+// lvl + 3; when only the first ones grow, the next round's expansions find
+// what a jump would (halo levels <= lvl + 3 have already been used).
 
-// Levels of the tile are written to hs[row * stride + col]; unreachable nodes
-// get INF.  Returns this row's reached set.
-__device__ unsigned tile_bfs(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd, unsigned sink, int hl,
+// Scratch of one warp's global-relabel tile BFS: the index of the expansion
+// that reached each pixel, as GR_NPL bit planes per row (lane = row, bit =
+// column), and the level of each index.
+constexpr int GR_NPL = 7;
+constexpr int GR_NIDX = 1 << GR_NPL;  // expansions per segment (the seeds are index 0)
+struct GrScratch {
+    unsigned pl[GR_NPL][32];  // plane b of row r: pixels whose index has bit b set
+    unsigned reached[32], base[32];
+    int lv[GR_NIDX];
+};
+
+// The same levels, each new pixel's level stored into hs[row * stride + col]
+// as it is reached (unreachable pixels get INF); returns this lane's row of the
+// reached set.  Two levels per vote.  Its instruction count is small when the
+// BFS is short, as in round 0 of a relabel, where most tiles hold many sinks:
+// there, with every SM busy and several tiles per warp, issue bounds the round
+// and this loop is the faster one (batch256 round 0: 76 us against 115 us with
+// tile_bfs_gr); the divergent stores make it the slower one wherever a visit's
+// latency bounds the round.
+__device__ unsigned tile_bfs_direct(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd, unsigned sink, int hl,
                          int hr, int ht, int hb, int *hs, int stride, int *iters) {
     const int lane = threadIdx.x & 31;
     int *row = hs + lane * stride;
@@ -262,12 +278,113 @@ __device__ unsigned tile_bfs(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd,
     return S;
 }
 
-// The push visits' exact local relabel: the same levels as tile_bfs, but
+// The global relabel's tile BFS: writes the level of every pixel of the tile
+// to h (the tile's 32x32 heights, row-major; INF where unreachable) and
+// returns this lane's row of the reached set; vt / vb get this lane's column's
+// top and bottom heights, vl / vr its row's first and last.
+//
+// Each expansion only ORs its new pixels into the bit planes of its index
+// (the same few uniform instructions for every lane); the heights are written
+// afterwards with lane = column, row by row: the planes of the row give each
+// pixel's index, the index its level, and the stores are coalesced.  (Storing
+// each new pixel's level as it is reached takes a loop over the new bits of
+// the lane's row, which diverges: a frontier that enters the tile along a
+// side reaches a whole row per level, 32 stores in a row for one lane, and a
+// one-warp micro-benchmark measured 61K cycles for such a tile against 5.3K
+// this way, and 4.1–6.0K against 7.4–11.1K on random tiles.)  After GR_NIDX
+// expansions the levels found so far are written out and the planes start a
+// new segment.
+__device__ unsigned tile_bfs_gr(unsigned Rl, unsigned Rr, unsigned Ru, unsigned Rd, unsigned sink, int hl, int hr,
+                                int ht, int hb, int *h, GrScratch &sc, int *iters, int &vt, int &vb, int &vl,
+                                int &vr) {
+    const int lane = threadIdx.x & 31;
+    unsigned S = sink, base = 0u;
+    unsigned P[GR_NPL];
+#pragma unroll
+    for (int k = 0; k < GR_NPL; ++k) P[k] = 0u;
+    if (lane == 0) sc.lv[0] = 1;  // index 0: the seeds
+    int nidx = 1, lvl = 1, it = 0;
+    vt = vb = vl = vr = INF_H;
+    // write the levels of the pixels reached in this segment (and, at the end,
+    // INF for the pixels never reached)
+    auto flush = [&](bool final) {
+#pragma unroll
+        for (int k = 0; k < GR_NPL; ++k) sc.pl[k][lane] = P[k];
+        sc.reached[lane] = S;
+        sc.base[lane] = base;
+        {
+            // this lane's row: its first and last pixel, from its own planes
+            const unsigned fresh = S & ~base;
+            int i0 = 0, i31 = 0;
+#pragma unroll
+            for (int k = 0; k < GR_NPL; ++k) {
+                i0 |= (int)(P[k] & 1u) << k;
+                i31 |= (int)(P[k] >> 31) << k;
+            }
+            const int a0 = sc.lv[i0], a31 = sc.lv[i31];
+            if (fresh & 1u) vl = a0;
+            if (fresh >> 31) vr = a31;
+        }
+        __syncwarp();
+        const unsigned bit = 1u << lane;
+#pragma unroll 8
+        for (int r = 0; r < 32; ++r) {
+            const unsigned sr = sc.reached[r], br = sc.base[r];
+            int idx = 0;
+#pragma unroll
+            for (int k = 0; k < GR_NPL; ++k) idx |= (int)((sc.pl[k][r] >> lane) & 1u) << k;
+            const bool fresh = ((sr & ~br) & bit) != 0;
+            const bool wr = fresh || (final && !(sr & bit));
+            const int v = fresh ? sc.lv[idx] : INF_H;
+            if (wr) h[r * 32 + lane] = v;
+            if (r == 0) vt = wr ? v : vt;
+            if (r == 31) vb = wr ? v : vb;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < GR_NPL; ++k) P[k] = 0u;
+        base = S;
+        nidx = 0;
+    };
+    for (; it < BFS_MAX_ITERS; ++it) {
+        const unsigned nw1 = bfs_expand(S, lvl, Rl, Rr, Ru, Rd, hl, hr, ht, hb, lane);
+        const unsigned S1 = S | nw1;
+        const unsigned nw2 = bfs_expand(S1, lvl + 1, Rl, Rr, Ru, Rd, hl, hr, ht, hb, lane);
+        const unsigned S2 = S1 | nw2;
+        const unsigned nw3 = bfs_expand(S2, lvl + 2, Rl, Rr, Ru, Rd, hl, hr, ht, hb, lane);
+        const unsigned S3 = S2 | nw3;
+        const unsigned nw4 = bfs_expand(S3, lvl + 3, Rl, Rr, Ru, Rd, hl, hr, ht, hb, lane);
+        if (__any_sync(FULL, (nw1 | nw2 | nw3 | nw4) != 0)) {
+            if (nidx + 4 > GR_NIDX) flush(false);
+            const unsigned nw[4] = {nw1, nw2, nw3, nw4};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int idx = nidx + j;  // warp-uniform
+#pragma unroll
+                for (int k = 0; k < GR_NPL; ++k)
+                    if ((idx >> k) & 1) P[k] |= nw[j];
+            }
+            if (lane < 4) sc.lv[nidx + lane] = lvl + 1 + lane;
+            S = S3 | nw4;
+            nidx += 4;
+            lvl += 4;
+        } else {
+            const int nxt = bfs_next_halo(lvl + 3, hl, hr, ht, hb);
+            if (nxt >= INF_H) break;
+            lvl = nxt;
+        }
+    }
+    flush(true);
+    *iters = it;
+    return S;
+}
+
+// The push visits' exact local relabel: the same levels as tile_bfs_gr, but
 // instead of storing each new pixel's level on the spot (a divergent loop on
 // the loop-carried path of a single warp) every expansion records the reached
 // rows, srec[row * NRS + k], and its level lv[k], while four more records
-// fit (k + 4 <= NREC); later expansions store their pixels' levels directly,
-// as tile_bfs does.  sfin gets the final reached rows.  Four expansions
+// fit (k + 4 <= NREC); later expansions store their pixels' levels directly
+// in the level array hs.  sfin gets the final reached rows.  Four expansions
 // (levels lvl + 1 .. lvl + 4, each from the previous one's result) share one
 // vote and one branch, so the loop-carried path holds one vote per four
 // levels; a level that adds nothing is recorded all the same (its record
@@ -391,7 +508,8 @@ struct SmemPush {
     int idx;
 };
 template <int NW>
-struct SmemWarp {
+struct SmemWarp {  // one of each per warp: the global relabel's tile BFS
+    GrScratch g[NW];
     int hs[NW][32 * 33];
 };
 template <int NW>
@@ -440,8 +558,8 @@ __device__ __forceinline__ void gr_prefetch(const Batch &b, int t, GrGeo &gg, bo
 // shorter path than its current height; the heights read for that are at
 // least current (distances only fall during a relabel), so no needed visit is
 // missed.
-__device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int tag_next, int slot_next, int *hs,
-                       unsigned long long *st) {
+__device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, bool direct, int tag_next, int slot_next,
+                       GrScratch &sc, int *hs, unsigned long long *st) {
     const int lane = threadIdx.x & 31;
     const size_t base = (size_t)t * TPX;
     unsigned m[6];
@@ -468,17 +586,26 @@ __device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, int t
         fr = g.nb[1] >= 0 ? mask_word(b, g.nb[1], 0, lane) & 1u : 0u;
     }
     int its = 0;
-    const unsigned reached = tile_bfs(m[0], m[1], m[2], m[3], m[4], hl, hr, ht, hb, hs, 33, &its);
+    int vt, vb, vl, vr;  // the tile's border heights (this lane's column / row)
+    unsigned reached;
+    if (direct) {  // warp-uniform
+        reached = tile_bfs_direct(m[0], m[1], m[2], m[3], m[4], hl, hr, ht, hb, hs, 33, &its);
+        __syncwarp();
+#pragma unroll 4
+        for (int r = 0; r < 32; ++r) b.h[base + r * 32 + lane] = hs[r * 33 + lane];
+        vt = hs[lane];
+        vb = hs[31 * 33 + lane];
+        vl = hs[lane * 33];
+        vr = hs[lane * 33 + 31];
+    } else {
+        reached = tile_bfs_gr(m[0], m[1], m[2], m[3], m[4], hl, hr, ht, hb, b.h + base, sc, &its, vt, vb, vl, vr);
+    }
     if (lane == 0) stat_add(st, ST_BFS_IT_GR, (unsigned long long)its);
     b.hfin[(size_t)t * 32 + lane] = reached;  // finite heights of this row (the extraction's S_max)
     int act = __popc(m[5] & reached);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) act += __shfl_down_sync(FULL, act, o);
     if (lane == 0) b.tile_act[t] = act;
-    __syncwarp();
-#pragma unroll 4
-    for (int r = 0; r < 32; ++r) b.h[base + r * 32 + lane] = hs[r * 33 + lane];
-    const int vt = hs[lane], vb = hs[31 * 33 + lane], vl = hs[lane * 33], vr = hs[lane * 33 + 31];
     {
         int *own = b.hb + (size_t)t * 128;
         own[HB_TOP + lane] = vt;
@@ -1037,6 +1164,7 @@ __global__ void __launch_bounds__(NW * 32, solve_min_blocks<NW>()) k_solve(Batch
     int P = 0;  // push phase counter (even at the start of every outer iteration)
     int G = 0;  // global relabel round counter (tags of the tile frontier)
     bool finished = false;
+    bool timeline = false;  // block 0, thread 0 during the first global relabel: records its timeline
     for (int outer = 0; outer < prm.max_outer; ++outer) {
         if (prm.phase == 2) goto push_rounds;  // the phase-1 launch did the relabel and the count
         if (outer > 0) {
@@ -1049,6 +1177,8 @@ __global__ void __launch_bounds__(NW * 32, solve_min_blocks<NW>()) k_solve(Batch
             }
         }
         // ------------------------ exact global relabel ------------------------
+        timeline = outer == 0 && blockIdx.x == 0 && threadIdx.x == 0;
+        if (timeline) ctl->gr_time[0] = gtimer();
         for (int k = gtid; k < batch_nimg(b); k += nthreads) {
             const int i = batch_img(b, k);
             if (!b.ist[i].done) {
@@ -1057,25 +1187,30 @@ __global__ void __launch_bounds__(NW * 32, solve_min_blocks<NW>()) k_solve(Batch
             }
         }
         if (gtid == 0) ctl->total_active = 0;
+        // round 0 visits every tile: with two or more per warp it is bound by
+        // issue, and the short BFS with direct level stores is the cheaper one
+        // (nt >= 2 * nwarps below)
         for (int k = gwarp; k < nt; k += nwarps) {
             const int t = batch_tile(b, k);
             GrGeo g;
             gr_prefetch(b, t, g, true);
             if (g.skip) continue;
             const long long c0 = clock64();
-            gr_run(b, t, g, true, G + 1, L_GR0 + ((G + 1) & 1), sm.w.hs[warp], st);
+            gr_run(b, t, g, true, nt >= 2 * nwarps, G + 1, L_GR0 + ((G + 1) & 1), sm.w.g[warp], sm.w.hs[warp], st);
             if (lane == 0) {
                 stat_add(st, ST_CYC_GR, (unsigned long long)(clock64() - c0));
                 stat_add(st, ST_GR_TILES, 1ull);
             }
         }
         if (!grid_sync(b, (1u << L_PUSH0) | (1u << L_PUSH1) | (1u << L_PUSH2))) return;
+        if (timeline) ctl->gr_time[1] = gtimer();
         for (int k = gwarp; k < nt; k += nwarps) {
             const int t = batch_tile(b, k);
             if (vload(&b.ist[__ldg(b.tile_img + t)].done)) continue;  // warp-uniform
             gr_pull_check(b, t, G + 1, L_GR0 + ((G + 1) & 1));
         }
         if (!grid_sync(b, 0)) return;
+        if (timeline) ctl->gr_time[2] = gtimer();
         ++G;
         for (int k = 1;; ++k) {
             const int slot = L_GR0 + (G & 1);
@@ -1092,13 +1227,22 @@ __global__ void __launch_bounds__(NW * 32, solve_min_blocks<NW>()) k_solve(Batch
                 const long long c0 = clock64();
                 GrGeo g;
                 gr_prefetch(b, t, g, false);
-                gr_run(b, t, g, false, G + 1, L_GR0 + ((G + 1) & 1), sm.w.hs[warp], st);
+                gr_run(b, t, g, false, false, G + 1, L_GR0 + ((G + 1) & 1), sm.w.g[warp], sm.w.hs[warp], st);
                 if (lane == 0) {
-                    stat_add(st, ST_CYC_GR, (unsigned long long)(clock64() - c0));
+                    const unsigned long long cyc = (unsigned long long)(clock64() - c0);
+                    stat_add(st, ST_CYC_GR, cyc);
                     stat_add(st, ST_GR_TILES, 1ull);
+                    if (outer == 0 && k <= GR_TIMELINE) {
+                        atomicMax(&ctl->gr_front_end[k - 1], gtimer());
+                        atomicMax(&ctl->gr_front_maxcyc[k - 1], cyc);
+                    }
                 }
             }
             if (!grid_sync(b, 1u << slot)) return;
+            if (timeline && k <= GR_TIMELINE) {
+                ctl->gr_time[2 + k] = gtimer();
+                ctl->gr_front[k - 1] = n;
+            }
             ++G;
             if (gtid == 0) ctl->gr_rounds++;
         }

@@ -48,6 +48,8 @@ struct ImgState {
 enum { L_PUSH0 = 0, L_PUSH1, L_PUSH2, L_GR0, L_GR1, L_NLISTS };
 
 // Control block of one solve (zeroed before every launch).
+constexpr int GR_TIMELINE = 32;
+
 struct Ctl {
     unsigned bar_count;
     unsigned bar_gen;
@@ -74,6 +76,15 @@ struct Ctl {
     // out of work, stored bit-inverted so that 0 means none and atomicMax
     // keeps the earliest; t_push_tail sums (phase end - earliest idle)
     unsigned long long push_idle[2], t_push_tail;
+    // timeline of the solve's first global relabel (%globaltimer ns, block 0
+    // after each grid barrier): gr_time[0] its start, [1] after round 0, [2]
+    // after the pull check, [3 + k] after frontier round k (k < GR_TIMELINE);
+    // gr_front[k] the tiles of frontier round k
+    unsigned long long gr_time[3 + GR_TIMELINE];
+    int gr_front[GR_TIMELINE];
+    // per frontier round of that relabel: the latest end of a tile visit
+    // (%globaltimer ns) and the longest visit (SM cycles)
+    unsigned long long gr_front_end[GR_TIMELINE], gr_front_maxcyc[GR_TIMELINE];
 };
 
 struct Batch {

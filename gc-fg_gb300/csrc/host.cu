@@ -1390,6 +1390,15 @@ gcfg_status gcfg_batch_phase_split(gcfg_batch *b, int n, const int *widths, cons
         out->relabel_rounds = c1.gr_rounds;
         out->active_pixels = (int64_t)c1.total_active;
         out->push_queue = c1.size[L_PUSH0] + c1.size[L_PUSH1];
+        out->relabel_round0_us = (float)((double)(c1.gr_time[1] - c1.gr_time[0]) * 1e-3);
+        out->relabel_pull_us = (float)((double)(c1.gr_time[2] - c1.gr_time[1]) * 1e-3);
+        for (int k = 0; k < GR_TIMELINE && k < c1.gr_rounds; ++k) {
+            out->relabel_front_us[k] = (float)((double)(c1.gr_time[3 + k] - c1.gr_time[2 + k]) * 1e-3);
+            out->relabel_front_tiles[k] = c1.gr_front[k];
+            if (c1.gr_front_end[k] > c1.gr_time[2 + k])
+                out->relabel_front_work_us[k] = (float)((double)(c1.gr_front_end[k] - c1.gr_time[2 + k]) * 1e-3);
+            out->relabel_front_maxvisit_kcyc[k] = (float)((double)c1.gr_front_maxcyc[k] * 1e-3);
+        }
         cudaEventElapsedTime(&out->ms_relabel, ev[0], ev[1]);
         if (c1.total_active == 0) break;  // nothing to push: the solve is over after the relabel
         p.phase = 2;  // the control block keeps the first push round's queues

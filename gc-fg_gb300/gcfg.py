@@ -86,10 +86,19 @@ class PhaseSplit(C.Structure):
     _fields_ = [("ms_relabel", C.c_float), ("ms_push", C.c_float), ("relabel_tiles", C.c_int64),
                 ("active_pixels", C.c_int64), ("push_tiles", C.c_int64), ("push_sweeps", C.c_int64),
                 ("push_local_relabels", C.c_int64), ("relabel_rounds", C.c_int32), ("push_phases", C.c_int32),
-                ("push_queue", C.c_int32), ("grid_blocks", C.c_int32)]
+                ("push_queue", C.c_int32), ("grid_blocks", C.c_int32),
+                ("relabel_round0_us", C.c_float), ("relabel_pull_us", C.c_float),
+                ("relabel_front_us", C.c_float * 32), ("relabel_front_tiles", C.c_int32 * 32),
+                ("relabel_front_work_us", C.c_float * 32), ("relabel_front_maxvisit_kcyc", C.c_float * 32)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        n = min(int(self.relabel_rounds), 32)
+        d["relabel_front_us"] = [round(float(x), 2) for x in self.relabel_front_us[:n]]
+        d["relabel_front_tiles"] = [int(x) for x in self.relabel_front_tiles[:n]]
+        d["relabel_front_work_us"] = [round(float(x), 2) for x in self.relabel_front_work_us[:n]]
+        d["relabel_front_maxvisit_kcyc"] = [round(float(x), 2) for x in self.relabel_front_maxvisit_kcyc[:n]]
+        return d
 
 
 class ProfEntry(C.Structure):

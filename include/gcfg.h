@@ -375,6 +375,17 @@ typedef struct {
     int32_t push_phases;          /* checkerboard colour phases of launch 2 */
     int32_t push_queue;           /* tiles queued for the first two colour phases */
     int32_t grid_blocks;          /* blocks of each launch */
+    /* timeline of launch 1's global relabel (device clock, microseconds):
+     * round 0 (every tile, halos from the neighbours' sink pixels), the pull
+     * check that picks the first frontier, then frontier round k with
+     * relabel_front_tiles[k] tiles, for k < min(relabel_rounds, 32) */
+    float relabel_round0_us, relabel_pull_us;
+    float relabel_front_us[32];
+    int32_t relabel_front_tiles[32];
+    /* per frontier round: from its start to the end of its last tile visit
+     * (the rest of the round is the grid barrier), and its longest visit */
+    float relabel_front_work_us[32];
+    float relabel_front_maxvisit_kcyc[32];
 } gcfg_phase_split;
 
 gcfg_status gcfg_batch_phase_split(gcfg_batch *b, int n, const int *widths, const int *heights,
