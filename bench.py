@@ -42,7 +42,7 @@ cpu_baseline: the oracle's Boykov-Kolmogorov solver (oracle/, the CPU
 reference_cuda: the reference's own CUDA path on the same GPU (its kernels
         compiled from its sources into a cubin, launched in GC_Optimize's
         order by oracle/refgpu/ref_gpu.cpp), one image at a time, on a bounded
-        sample of the workload; its labels are compared with this build's
+        sample of the workload; its labels are compared with libgcfg's
         S_max.
 --impl reference: the reference has no CPU implementation of this path, so
         this arm times the CPU port (oracle BK) on all host threads, one image
@@ -83,7 +83,7 @@ UNIT = "Mpixel/s"
 #   extract: read height (4 B) + reach bit, write two label bytes (2 B)
 B_GR, B_PUSH, B_REACH, B_COUNT, B_BUILD, B_EXTRACT = 24, 48, 20, 8, 23, 6
 
-# Bytes a solver phase really moves per tile visit in this build's layout
+# Bytes a solver phase really moves per tile visit in the tile-arena layout
 # (what DRAM counters see when nothing is served from L2):
 #   global-relabel visit: read the tile's six residual mask planes (768 B),
 #     the neighbours' facing border-height lines (4 x 128 B) and their
@@ -264,7 +264,7 @@ def reference_cuda_leg(views, lams, smax_all, offs, budget_s=15.0):
     workload order until budget_s of reference solve time).  The t-links and
     n-links are computed on the host by the oracle (outside every timed span).
     value = pixels / the sum of the GC_SetGraph + GC_Optimize wall times; the
-    reference's labels are compared with this build's S_max."""
+    reference's labels are compared with libgcfg's S_max."""
     import oracle as O
     import ref_cuda
     why = ref_cuda.unavailable()

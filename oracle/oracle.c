@@ -2,7 +2,8 @@
  * oracle.c -- CPU oracle for the gc-fg binary-MRF graph-cut path.
  *
  * TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
- * cpu_baseline leg of bench.py as the checker; never by the product library.
+ * cpu_baseline leg of bench.py to check and time against; never by the
+ * product library.
  *
  * Compile with -ffp-contract=off so that the double arithmetic below is the
  * plain IEEE evaluation on every host.

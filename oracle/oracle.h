@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links, loads or
  * calls this code; only the test suite, the smoke check and the CPU-baseline
- * leg of bench.py use it, and only as the checker.
+ * leg of bench.py use it, and only to check and time against.
  *
  * It restates, in plain C:
  *   - the colour-histogram data term and the contrast-sensitive n-links;

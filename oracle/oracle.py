@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
-cpu_baseline leg of bench.py, where it is the checker.  The product library
+cpu_baseline leg of bench.py, to check and time against.  The product library
 (libgcfg.so) neither links nor calls it.
 """
 from __future__ import annotations

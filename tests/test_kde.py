@@ -6,7 +6,7 @@ bit for bit from their Gaussian table; the GPU reproduces the oracle bit for
 bit from its own table, and the two tables agree to 2 ulp (the emulator
 evaluates expf with the host library, the GPU with CUDA's).  On the GPU the
 reference's own data-term kernels (DataTermKernels.cu, built from its sources
-into oracle/_ref/gc_ref_dt_kernels.cubin) run beside this build's: their
+into oracle/_ref/gc_ref_dt_kernels.cubin) run beside libgcfg's: their
 Gaussian table, t-links, selection map and drawSelection output must be equal
 bit for bit, with no condition."""
 import glob
@@ -163,7 +163,7 @@ def _kde_cases():
 @pytest.mark.gpu
 @pytest.mark.parametrize("name,img,points,sigma", _kde_cases(), ids=[c[0] for c in _kde_cases()])
 def test_gpu_kde_equals_reference_gpu_kernels(name, img, points, sigma):
-    """This build's KDE data term against the reference's own kernels on the
+    """libgcfg's KDE data term against the reference's own kernels on the
     same GPU: Gaussian table, pos and neg bit for bit (sigma 0 = the default
     table of init_data_term)."""
     pytest.importorskip("torch")
