@@ -223,12 +223,14 @@ __device__ __forceinline__ int bfs_next_halo(int lvl, int hl, int hr, int ht, in
     return __reduce_min_sync(FULL, cand);
 }
 
-// Both BFS loops below take four levels per round (lvl -> lvl + 1 -> ... ->
-// lvl + 4, each expansion from the previous one's result) and decide once, so
-// the loop-carried path holds one vote and one branch per four levels.  When
-// no level grows the frontier, the level jumps to the next halo level above
-// lvl + 3; when only the first ones grow, the next round's expansions find
-// what a jump would (halo levels <= lvl + 3 have already been used).
+// The tile BFS loops below take several levels per round (lvl -> lvl + 1 ->
+// ..., each expansion from the previous one's result) and decide once, so
+// the loop-carried path holds one vote and one branch per round: four levels
+// in tile_bfs_gr and tile_bfs_rec, two in tile_bfs_direct.  When no level of
+// a round grows the frontier, the level jumps to the next halo level above
+// the round's last; when only the first ones grow, the next round's
+// expansions find what a jump would (the halo levels up to the round's last
+// have already been used).
 
 // Scratch of one warp's global-relabel tile BFS: the index of the expansion
 // that reached each pixel, as GR_NPL bit planes per row (lane = row, bit =
@@ -241,9 +243,9 @@ struct GrScratch {
     int lv[GR_NIDX];
 };
 
-// The same levels, each new pixel's level stored into hs[row * stride + col]
-// as it is reached (unreachable pixels get INF); returns this lane's row of the
-// reached set.  Two levels per vote.  Its instruction count is small when the
+// The global relabel's tile BFS with each new pixel's level stored into
+// hs[row * stride + col] as it is reached (unreachable pixels get INF);
+// returns this lane's row of the reached set.  Two levels per vote.  Its instruction count is small when the
 // BFS is short, as in round 0 of a relabel, where most tiles hold many sinks:
 // there, with every SM busy and several tiles per warp, issue bounds the round
 // and this loop is the faster one (batch256 round 0: 76 us against 115 us with
