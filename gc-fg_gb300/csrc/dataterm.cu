@@ -287,7 +287,10 @@ __device__ __forceinline__ uint32_t sigma_chunk(uintptr_t lo, uintptr_t hi, uint
 // k + 3 inside the image, minus the pairs that straddle a row end; down pairs
 // = sum of (B[k] - B[k + 3W])^2 over the chunk's bytes above the image's last
 // row.  Per 4 bytes: one __vabsdiffu4 + __dp4a for each direction.
-__global__ void __launch_bounds__(256, 6) k_hist_sigma_b(const uint8_t *__restrict__ rgb,
+// Eight blocks per SM (32 registers, 16 bytes of spills): the pass waits on
+// memory, and the fuller SM hides more of it than six blocks with 40
+// registers (batch256 0.130 -> 0.112 ms).
+__global__ void __launch_bounds__(256, 8) k_hist_sigma_b(const uint8_t *__restrict__ rgb,
                                                       const uint8_t *__restrict__ scrib,
                                                       const ImgDesc *__restrict__ img,
                                                       const int2 *__restrict__ chunk_map,
@@ -473,8 +476,10 @@ __device__ __forceinline__ int nlink_w(int d2, const NlinkParams &q) {
 // (the weight is symmetric in its two pixels) into a right-edge and a
 // down-edge table, and each pixel then reads its four capacities from them.
 // An edge that touches the 1-pixel image border has capacity 0, as in the
-// reference's graph (GraphCutKernels.cu:112-214).
-__global__ void __launch_bounds__(TILE_THREADS, 5) k_build_img_b(Batch b, const uint8_t *__restrict__ rgb,
+// reference's graph (GraphCutKernels.cu:112-214).  Eight blocks per SM
+// (32 registers, a few spilled): more tiles in flight hide the staging loads
+// (batch256 0.426 ms at five blocks, 0.408 at six, 0.399 at eight).
+__global__ void __launch_bounds__(TILE_THREADS, 8) k_build_img_b(Batch b, const uint8_t *__restrict__ rgb,
                                                                const int *__restrict__ dp_lut,
                                                                const int *__restrict__ dn_lut) {
     constexpr int SW = TILE_W + 2, SH = TILE_H + 2;
