@@ -255,10 +255,11 @@ __device__ unsigned tile_bfs_direct(unsigned Rl, unsigned Rr, unsigned Ru, unsig
                          int hr, int ht, int hb, int *hs, int stride, int *iters) {
     const int lane = threadIdx.x & 31;
     int *row = hs + lane * stride;
+    // INF, and level 1 on the seeds, in one uniform pass (a loop over the
+    // seed bits would run as long as the row with the most seeds)
 #pragma unroll 8
-    for (int x = 0; x < 32; ++x) row[x] = INF_H;
+    for (int x = 0; x < 32; ++x) row[x] = (sink >> x) & 1u ? 1 : INF_H;
     unsigned S = sink;
-    for (unsigned m = sink; m; m &= m - 1) row[__ffs(m) - 1] = 1;
     int lvl = 1;
     int it = 0;
     for (; it < BFS_MAX_ITERS; ++it) {
@@ -632,24 +633,47 @@ __device__ void gr_run(const Batch &b, int t, const GrGeo &g, bool round0, bool 
 // when a neighbour's border, as round 0 left it, gives one of t's border
 // pixels (through its residual edge out of the tile) a shorter path than its
 // own round-0 distance.
-__device__ void gr_pull_check(const Batch &b, int t, int tag_next, int slot_next) {
+// Two tiles per call (t1 < 0: one), every load that depends only on the
+// tile issued first for both (image, neighbour table, own border lines and
+// masks), then the image's finished flag and the neighbours' border lines:
+// two memory round trips for the pair where one tile alone took four.  A
+// tile of a finished image is not checked.
+__device__ void gr_pull_check(const Batch &b, int t0, int t1, int tag_next, int slot_next) {
     const int lane = threadIdx.x & 31;
-    int nb[4];
-    tile_nbs(b, t, nb);
-    const int *own = b.hb + (size_t)t * 128;
-    const int ot = __ldcg(own + HB_TOP + lane), ob = __ldcg(own + HB_BOT + lane);
-    const int ol = __ldcg(own + HB_LFT + lane), orr = __ldcg(own + HB_RGT + lane);
-    const unsigned ru = mask_word(b, t, 2, 0), rd = mask_word(b, t, 3, 31);  // bit = column
-    const unsigned rl = mask_word(b, t, 0, lane) & 1u, rr = mask_word(b, t, 1, lane) >> 31;
-    const int ht = nb[2] >= 0 ? __ldcg(b.hb + (size_t)nb[2] * 128 + HB_BOT + lane) : INF_H;
-    const int hb = nb[3] >= 0 ? __ldcg(b.hb + (size_t)nb[3] * 128 + HB_TOP + lane) : INF_H;
-    const int hl = nb[0] >= 0 ? __ldcg(b.hb + (size_t)nb[0] * 128 + HB_RGT + lane) : INF_H;
-    const int hr = nb[1] >= 0 ? __ldcg(b.hb + (size_t)nb[1] * 128 + HB_LFT + lane) : INF_H;
-    const bool imp = (((ru >> lane) & 1u) && ht < INF_H && ht + 1 < ot) ||
-                     (((rd >> lane) & 1u) && hb < INF_H && hb + 1 < ob) || (rl && hl < INF_H && hl + 1 < ol) ||
-                     (rr && hr < INF_H && hr + 1 < orr);
-    const bool any = __any_sync(FULL, imp);
-    enqueue_warp(b, b.mark_gr, slot_next, tag_next, t, lane == 0 && any);
+    const int tt[2] = {t0, t1 >= 0 ? t1 : t0};
+    int img[2], ot[2], ob[2], ol[2], orr[2];
+    int4 nb[2];
+    unsigned ru[2], rd[2], rl[2], rr[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int t = tt[q];
+        img[q] = __ldg(b.tile_img + t);
+        nb[q] = __ldcg(b.tile_nb + t);
+        const int *own = b.hb + (size_t)t * 128;
+        ot[q] = __ldcg(own + HB_TOP + lane);
+        ob[q] = __ldcg(own + HB_BOT + lane);
+        ol[q] = __ldcg(own + HB_LFT + lane);
+        orr[q] = __ldcg(own + HB_RGT + lane);
+        ru[q] = mask_word(b, t, 2, 0);  // bit = column
+        rd[q] = mask_word(b, t, 3, 31);
+        rl[q] = mask_word(b, t, 0, lane) & 1u;
+        rr[q] = mask_word(b, t, 1, lane) >> 31;
+    }
+    bool want[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int done = __ldcg(&b.ist[img[q]].done);
+        const int ht = nb[q].z >= 0 ? __ldcg(b.hb + (size_t)nb[q].z * 128 + HB_BOT + lane) : INF_H;
+        const int hb = nb[q].w >= 0 ? __ldcg(b.hb + (size_t)nb[q].w * 128 + HB_TOP + lane) : INF_H;
+        const int hl = nb[q].x >= 0 ? __ldcg(b.hb + (size_t)nb[q].x * 128 + HB_RGT + lane) : INF_H;
+        const int hr = nb[q].y >= 0 ? __ldcg(b.hb + (size_t)nb[q].y * 128 + HB_LFT + lane) : INF_H;
+        const bool imp = (((ru[q] >> lane) & 1u) && ht < INF_H && ht + 1 < ot[q]) ||
+                         (((rd[q] >> lane) & 1u) && hb < INF_H && hb + 1 < ob[q]) ||
+                         (rl[q] && hl < INF_H && hl + 1 < ol[q]) || (rr[q] && hr < INF_H && hr + 1 < orr[q]);
+        want[q] = !done && __any_sync(FULL, imp);  // done is warp-uniform
+    }
+    enqueue_warp(b, b.mark_gr, slot_next, tag_next, t0, lane == 0 && want[0]);
+    if (t1 >= 0) enqueue_warp(b, b.mark_gr, slot_next, tag_next, t1, lane == 0 && want[1]);
 }
 // Source-side reachability closure of tile t given the halo's reach bits.
 __device__ void reach_tile(const Batch &b, int t, bool round0, int tag_next, int slot_next) {
@@ -1206,10 +1230,10 @@ __global__ void __launch_bounds__(NW * 32, solve_min_blocks<NW>()) k_solve(Batch
         }
         if (!grid_sync(b, (1u << L_PUSH0) | (1u << L_PUSH1) | (1u << L_PUSH2))) return;
         if (timeline) ctl->gr_time[1] = gtimer();
-        for (int k = gwarp; k < nt; k += nwarps) {
-            const int t = batch_tile(b, k);
-            if (vload(&b.ist[__ldg(b.tile_img + t)].done)) continue;  // warp-uniform
-            gr_pull_check(b, t, G + 1, L_GR0 + ((G + 1) & 1));
+        for (int k = gwarp; k < nt; k += 2 * nwarps) {
+            const int t0 = batch_tile(b, k);
+            const int t1 = k + nwarps < nt ? batch_tile(b, k + nwarps) : -1;
+            gr_pull_check(b, t0, t1, G + 1, L_GR0 + ((G + 1) & 1));
         }
         if (!grid_sync(b, 0)) return;
         if (timeline) ctl->gr_time[2] = gtimer();
