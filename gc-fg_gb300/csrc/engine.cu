@@ -975,6 +975,13 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
     const long long c2 = clock64();
     int next_idx = 0;
     if (threadIdx.x == 0) next_idx = atomicAdd(take_ctr, 1);
+    // A tile still active queues itself for its colour's next phase.  The
+    // queue append is two dependent atomics; with 8 or more warps, warp 4 (no
+    // hand-over duty) issues it here, so that its round trips overlap the
+    // write-back and the hand-over of warps 0..3 instead of following them
+    // (the slot of phase + 2 was emptied at the last barrier and is not read
+    // in this phase)
+    if (NW >= 8 && any && threadIdx.x == 4 * 32) enqueue(b, b.mark_push, (phase + 2) % 3, phase + 2, t);
     cs = c2 - c1 - cb;
     // ---- write back (and refresh the tile's mask planes and excess sum) ----
     unsigned long long pos = 0;
@@ -1035,7 +1042,7 @@ __device__ void push_tile(const Batch &b, int t, const SolveParams &prm, int pha
         if (__any_sync(FULL, activated) && lane == 0)
             enqueue(b, b.mark_push, (phase + 1) % 3, phase + 1, nt);
     }
-    if (any && threadIdx.x == 0) enqueue(b, b.mark_push, (phase + 2) % 3, phase + 2, t);
+    if (NW < 8 && any && threadIdx.x == 0) enqueue(b, b.mark_push, (phase + 2) % 3, phase + 2, t);
     if (threadIdx.x == 0) s.idx = next_idx;
     __syncthreads();
     if (threadIdx.x == 0) {
