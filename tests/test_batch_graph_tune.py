@@ -134,6 +134,15 @@ def test_phase_split_runs_both_phases_and_changes_no_result():
         assert ps["active_pixels"] > 0 and ps["push_queue"] > 0
         assert ps["ms_push"] > 0 and ps["push_tiles"] >= 1 and ps["push_phases"] >= 1
         assert ps["push_sweeps"] >= ps["push_tiles"]
+        # the relabel's timeline: round 0 visits every tile, then one entry
+        # per frontier round with its tile count
+        n = min(ps["relabel_rounds"], 32)
+        assert len(ps["relabel_front_tiles"]) == n and len(ps["relabel_front_us"]) == n
+        assert ps["relabel_round0_us"] > 0 and ps["relabel_pull_us"] > 0
+        assert all(k > 0 for k in ps["relabel_front_tiles"]) and all(u > 0 for u in ps["relabel_front_us"])
+        assert all(0 <= w <= u for w, u in zip(ps["relabel_front_work_us"], ps["relabel_front_us"]))
+        if ps["relabel_rounds"] <= 32:
+            assert sum(ps["relabel_front_tiles"]) == ps["relabel_tiles"] - tiles
         got = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
         assert np.array_equal(got[0], ref[0])
         assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2])
