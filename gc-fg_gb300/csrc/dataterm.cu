@@ -508,7 +508,64 @@ __global__ void __launch_bounds__(TILE_THREADS, 8) k_build_img_b(Batch b, const 
     // this image's bytes is assembled from the bytes inside), and each lane
     // cuts its pixel out of two adjacent words (warp shuffles + a funnel
     // shift); lanes 0 and 1 then cut the row's last two pixels.
-    {
+    if (3LL * W * H < (1LL << 30)) {  // block-uniform: the image's byte offsets fit 32 bits
+        // The same staging with 32-bit offsets from the 4-byte-aligned
+        // address at or below the image's first byte (mis = the image's
+        // misalignment): 64-bit address arithmetic costs several
+        // instructions per operation, and every thread runs it per row.
+        const uintptr_t lo = (uintptr_t)base;
+        const int mis = (int)(lo & 3);
+        const uint8_t *abase = base - mis;  // 4-byte aligned
+        const int nbytes = 3 * W * H;
+        const int xs = x0 > 0 ? x0 - 1 : 0;
+        const int xe = x0 + TILE_W < W ? x0 + TILE_W : W - 1;
+        constexpr int NW = TILE_THREADS / 32, RPW = (SH + NW - 1) / NW;  // rows per warp
+        uint32_t words[RPW];
+        int phs[RPW];
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) {  // every load first
+            const int i = warp + NW * r;
+            const int y = y0 - 1 + i;
+            uint32_t word = 0;
+            const int rs = mis + 3 * (y * W + xs);  // aligned-base offset of the row's first byte
+            phs[r] = rs & 3;
+            if (i < SH && y >= 0 && y < H) {
+                const int re = mis + 3 * (y * W + xe) + 3;  // one past its last byte
+                const int aw = rs & ~3;
+                if (lane < ((re - aw + 3) >> 2)) {
+                    const int wa = aw + 4 * lane;   // aligned-base offset of the lane's word
+                    const int k0 = wa - mis;        // image byte offset of its first byte
+                    if (k0 >= 0 && k0 + 4 <= nbytes) {
+                        word = __ldg(reinterpret_cast<const uint32_t *>(abase + wa));
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if (k0 + k >= 0 && k0 + k < nbytes) word |= (uint32_t)__ldg(abase + wa + k) << (8 * k);
+                    }
+                }
+            }
+            words[r] = word;
+        }
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) {
+            const int i = warp + NW * r;
+            if (i >= SH) break;  // warp-uniform
+            const int y = y0 - 1 + i;
+            const bool row_in = y >= 0 && y < H;
+            const int ph = phs[r];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int j = lane + 32 * h;
+                const int x = x0 - 1 + j;
+                const bool in = row_in && x >= 0 && x < W;
+                const int off = in ? ph + 3 * (x - xs) : 0;  // <= 3 + 3 * 33 = 102: words 0..26
+                const uint32_t wlo = __shfl_sync(0xffffffffu, words[r], off >> 2);
+                const uint32_t whi = __shfl_sync(0xffffffffu, words[r], (off >> 2) + 1);
+                const uint32_t v = in ? __funnelshift_r(wlo, whi, (off & 3) * 8) & 0xFFFFFFu : 0u;
+                if (j < SW) col[i][j] = v;
+            }
+        }
+    } else {
         const uintptr_t lo = (uintptr_t)base, hi = lo + 3 * (uintptr_t)W * (uintptr_t)H;
         const int xs = x0 > 0 ? x0 - 1 : 0;
         const int xe = x0 + TILE_W < W ? x0 + TILE_W : W - 1;
