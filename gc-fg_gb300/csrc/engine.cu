@@ -1210,7 +1210,7 @@ __global__ void __launch_bounds__(NW * 32, solve_min_blocks<NW>()) k_solve(Batch
             }
         }
         // ------------------------ exact global relabel ------------------------
-        timeline = outer == 0 && blockIdx.x == 0 && threadIdx.x == 0;
+        timeline = prm.phase == 1 && blockIdx.x == 0 && threadIdx.x == 0;  // the phase-split diagnostic
         if (timeline) ctl->gr_time[0] = gtimer();
         for (int k = gtid; k < batch_nimg(b); k += nthreads) {
             const int i = batch_img(b, k);
@@ -1265,7 +1265,7 @@ __global__ void __launch_bounds__(NW * 32, solve_min_blocks<NW>()) k_solve(Batch
                     const unsigned long long cyc = (unsigned long long)(clock64() - c0);
                     stat_add(st, ST_CYC_GR, cyc);
                     stat_add(st, ST_GR_TILES, 1ull);
-                    if (outer == 0 && k <= GR_TIMELINE) {
+                    if (prm.phase == 1 && k <= GR_TIMELINE) {  // the phase-split diagnostic only
                         atomicMax(&ctl->gr_front_end[k - 1], gtimer());
                         atomicMax(&ctl->gr_front_maxcyc[k - 1], cyc);
                     }

@@ -76,14 +76,16 @@ struct Ctl {
     // out of work, stored bit-inverted so that 0 means none and atomicMax
     // keeps the earliest; t_push_tail sums (phase end - earliest idle)
     unsigned long long push_idle[2], t_push_tail;
-    // timeline of the solve's first global relabel (%globaltimer ns, block 0
-    // after each grid barrier): gr_time[0] its start, [1] after round 0, [2]
+    // timeline of the global relabel of a phase-1 launch (the phase-split
+    // diagnostic; %globaltimer ns, block 0 after each grid barrier):
+    // gr_time[0] its start, [1] after round 0, [2]
     // after the pull check, [3 + k] after frontier round k (k < GR_TIMELINE);
     // gr_front[k] the tiles of frontier round k
     unsigned long long gr_time[3 + GR_TIMELINE];
     int gr_front[GR_TIMELINE];
     // per frontier round of that relabel: the latest end of a tile visit
-    // (%globaltimer ns) and the longest visit (SM cycles)
+    // (%globaltimer ns) and the longest visit (SM cycles); other launches
+    // leave these alone (their global atomics would serialise on one address)
     unsigned long long gr_front_end[GR_TIMELINE], gr_front_maxcyc[GR_TIMELINE];
 };
 
