@@ -183,3 +183,39 @@ def test_autotuner_reports_the_block_shape():
     got = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
     assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2])
     bs.close()
+
+
+def test_cut_outputs_at_any_alignment():
+    """The cut pass writes whole 16-byte windows when S_min and S_max share
+    their address modulo 16 (at any offset) and falls back to the tile-major
+    pass when they do not; either output may be left out.  Every case gives
+    the cuts of the aligned run, and no byte outside the outputs changes."""
+    Ws, Hs, lams, rgb, scrib = _batch(16, 3800)
+    d_rgb = torch.from_numpy(rgb).cuda()
+    d_scrib = torch.from_numpy(scrib).cuda()
+    bs = gcfg.BatchSolver(16, scrib.size)
+    ref = _run(bs, Ws, Hs, lams, d_rgb, d_scrib)
+    n_px = scrib.size
+    buf_a = torch.empty(n_px + 64, dtype=torch.uint8, device="cuda")
+    buf_b = torch.empty(n_px + 64, dtype=torch.uint8, device="cuda")
+    for oa, ob in ((0, 0), (5, 5), (13, 13), (1, 0), (0, 7), (3, 11)):
+        buf_a.fill_(7)
+        buf_b.fill_(9)
+        smin, smax = buf_a[oa:oa + n_px], buf_b[ob:ob + n_px]
+        flows, _ = bs.run(Ws, Hs, lams, d_rgb, d_scrib, smin, smax)
+        assert np.array_equal(flows, ref[0])
+        assert np.array_equal(smin.cpu().numpy(), ref[1]), (oa, ob)
+        assert np.array_equal(smax.cpu().numpy(), ref[2]), (oa, ob)
+        a, b = buf_a.cpu().numpy(), buf_b.cpu().numpy()
+        assert (a[:oa] == 7).all() and (a[oa + n_px:] == 7).all()
+        assert (b[:ob] == 9).all() and (b[ob + n_px:] == 9).all()
+    for oa in (0, 6):
+        buf_b.fill_(9)
+        smax = buf_b[oa:oa + n_px]
+        flows, _ = bs.run(Ws, Hs, lams, d_rgb, d_scrib, None, smax)
+        assert np.array_equal(flows, ref[0]) and np.array_equal(smax.cpu().numpy(), ref[2])
+        buf_a.fill_(7)
+        smin = buf_a[oa:oa + n_px]
+        flows, _ = bs.run(Ws, Hs, lams, d_rgb, d_scrib, smin, None)
+        assert np.array_equal(flows, ref[0]) and np.array_equal(smin.cpu().numpy(), ref[1])
+    bs.close()
